@@ -1,0 +1,105 @@
+"""ctypes binding of libaarambam_gpu.so (the C ABI declared in include/aarambam.h).
+
+The library is built in-tree by aarambam_gb300.build; loading fails loudly
+when it is missing -- there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from . import build as _build
+
+AAR_OK = 0
+AAR_ERR_ARG = 1
+AAR_ERR_CUDA = 2
+AAR_ERR_OOM = 3
+AAR_ERR_STATE = 4
+AAR_ERR_NMAX = 200
+AAR_ERR_TRANSFER = 1111
+AAR_ERR_TRANSFER_DUP = 777
+AAR_FUSED_FP32 = 0
+AAR_PLAIN_FP64 = 1
+
+# every symbol include/aarambam.h declares
+EXPORTS = [
+    "aar_plan_create", "aar_set_tables", "aar_set_transfer", "aar_get_scalars", "aar_set_seed", "aar_run",
+    "aar_run_glass", "aar_run_host", "aar_seedtable", "aar_stage_noise", "aar_stage_modal", "aar_stage_lpt",
+    "aar_stage_readout", "aar_copy_spectrum", "aar_copy_field", "aar_c2r", "aar_r2c", "aar_last_launch_count", "aar_profile_enable", "aar_profile_report",
+    "aar_last_error", "aar_plan_destroy", "aar_version",
+]
+
+
+class Params(C.Structure):
+    _fields_ = [("nmesh", C.c_int32), ("nsample", C.c_int32), ("nmax", C.c_int32), ("seed", C.c_int32),
+                ("box", C.c_double), ("omega", C.c_double), ("omega_lambda", C.c_double),
+                ("hubble_param", C.c_double), ("sigma8", C.c_double), ("primordial_index", C.c_double),
+                ("redshift", C.c_double), ("fnl", C.c_double), ("unit_length_in_cm", C.c_double),
+                ("unit_mass_in_g", C.c_double), ("unit_velocity_in_cm_per_s", C.c_double),
+                ("input_spectrum_unit_length_in_cm", C.c_double), ("fixed_amplitude", C.c_int32),
+                ("phase_flip", C.c_int32), ("sphere_mode", C.c_int32), ("precision", C.c_int32),
+                ("mem_limit_bytes", C.c_int64)]
+
+
+class Scalars(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("norm", "anorm", "d0", "dplus", "init_time", "hubble", "beta",
+                                          "vel_prefac", "vel_prefac2")]
+
+
+class AarError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = False):
+    """Load the library (optionally building it first)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(_build.LIB):
+        if not build_if_missing:
+            raise RuntimeError(f"{_build.LIB} is not built; run aarambam_gb300.build.build() "
+                               "(the CUDA extension is required, there is no CPU path)")
+        _build.build()
+    L = C.CDLL(_build.LIB)
+    vp, i32, i64 = C.c_void_p, C.c_int32, C.c_int64
+    dp = C.POINTER(C.c_double)
+    L.aar_plan_create.argtypes = [C.POINTER(Params), C.POINTER(vp)]
+    L.aar_set_tables.argtypes = [vp, dp, dp, i32]
+    L.aar_set_transfer.argtypes = [vp, dp, dp, i32]
+    L.aar_get_scalars.argtypes = [vp, C.POINTER(Scalars)]
+    L.aar_set_seed.argtypes = [vp, i32]
+    L.aar_run.argtypes = [vp, vp, i64, vp, vp, vp]
+    L.aar_run_glass.argtypes = [vp, vp, i64, C.c_double, i32, vp, vp, vp, vp]
+    L.aar_run_host.argtypes = [vp, vp, i64, vp, vp, vp]
+    L.aar_seedtable.argtypes = [vp, vp, vp]
+    for n in ("aar_stage_noise", "aar_stage_modal", "aar_stage_lpt"):
+        getattr(L, n).argtypes = [vp, vp]
+    L.aar_stage_readout.argtypes = [vp, vp, i64, vp, vp, vp]
+    L.aar_copy_spectrum.argtypes = [vp, vp, vp]
+    L.aar_copy_field.argtypes = [vp, i32, vp, vp]
+    L.aar_c2r.argtypes = [vp, vp, vp, vp]
+    L.aar_r2c.argtypes = [vp, vp, vp, vp]
+    L.aar_last_launch_count.argtypes = [vp]
+    L.aar_profile_enable.argtypes = [vp, i32]
+    L.aar_profile_report.argtypes = [vp, C.c_char_p, i32]
+    L.aar_last_error.argtypes = [vp]
+    L.aar_last_error.restype = C.c_char_p
+    L.aar_plan_destroy.argtypes = [vp]
+    L.aar_plan_destroy.restype = None
+    _lib = L
+    return L
+
+
+def check(L, plan, rc: int) -> None:
+    if rc != AAR_OK:
+        msg = L.aar_last_error(plan)
+        raise AarError(rc, msg.decode() if msg else "")

@@ -1,0 +1,135 @@
+// Internal declarations shared by the CUDA translation units of
+// libaarambam_gpu.so (not part of the C ABI).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/aarambam.h"
+
+namespace aar {
+
+constexpr double kPi = 3.14159265358979323846;  // PI as the reference defines it
+
+// signed wavenumber index of grid index i (main.c:410-423): N/2 -> -N/2
+__host__ __device__ __forceinline__ int sidx(int i, int N) { return i < N / 2 ? i : i - N; }
+
+// Geometry and scalars of one plan, passed by value to kernels.
+struct Grid {
+  int N;       // Nmesh
+  int HP;      // padded half-spectrum row length (complex entries), >= N/2+1
+  int kcut;    // cube mode: keep |k index| <= kcut on every axis
+  int sphere;  // SphereMode
+  int nsq_bnd; // sphere mode: (Nsample/2)^2, the only n^2 whose keep depends on rounding
+  int nsample_half;
+  double box;
+  float kF;    // 2 pi / Box
+};
+
+// Keep / cut decision of the reference (main.c:428-441, :591-604), exact.
+// Cube mode reduces to an integer bound on each axis (host-computed).  In
+// sphere mode only n^2 == (Nsample/2)^2 sits on the rounding boundary; those
+// cells repeat the reference's FP64 expression with unfused operations.
+__device__ __forceinline__ bool keep_cell(const Grid& g, int kx, int ky, int kz) {
+  if (!g.sphere) return abs(kx) <= g.kcut && abs(ky) <= g.kcut && abs(kz) <= g.kcut;
+  int n2 = kx * kx + ky * ky + kz * kz;
+  if (n2 != g.nsq_bnd) return n2 < g.nsq_bnd;
+  double fx = __ddiv_rn(__dmul_rn((double)(2 * kx), kPi), g.box);
+  double fy = __ddiv_rn(__dmul_rn((double)(2 * ky), kPi), g.box);
+  double fz = __ddiv_rn(__dmul_rn((double)(2 * kz), kPi), g.box);
+  double k2 = __dadd_rn(__dadd_rn(__dmul_rn(fx, fx), __dmul_rn(fy, fy)), __dmul_rn(fz, fz));
+  double km = __dsqrt_rn(k2);
+  return !(__ddiv_rn(__dmul_rn(km, g.box), __dmul_rn(2.0, kPi)) > (double)g.nsample_half);
+}
+
+// Host twin of keep_cell's cube bound.
+int host_kcut(int nsample, double box);
+
+// ----------------------------------------------------------- plan state
+struct Plan {
+  aar_params prm;
+  std::string err;
+  int N = 0, HP = 0, M = 0;
+  Grid grid{};
+  // host scalars (power.c:391-448, main.c:305-372)
+  double Norm = 0, Anorm = 0, D0 = 0, Dplus = 0, InitTime = 0, Hubble = 0, Beta = 0;
+  double vel_prefac = 0, vel_prefac2 = 0, kconv = 1;
+  std::vector<double> logk, logT;  // sorted, normalised transfer table
+  std::vector<double> alpha;       // M^3 symmetric
+  std::vector<double> x0;          // M
+  bool have_tables = false, have_transfer = false;
+  // device resources (fused FP32 form)
+  int dev = -1;
+  float2* d_phik = nullptr;   // Gaussian / total potential spectrum [N][N][HP]
+  float2* d_work = nullptr;   // nwork fields [N][N][HP]
+  int nwork = 0;
+  uint32_t* d_seed = nullptr; // seed table [N][N]
+  float2* d_twN = nullptr;    // exp(-2 pi i m / N), m < N
+  float2* d_twH = nullptr;    // exp(-2 pi i m / (N/2)), m < N/2
+  float* d_amp = nullptr;     // per n^2 noise amplitude
+  float* d_twb = nullptr;     // per n^2 T(k) / (Dplus Beta)
+  void* d_rlxpow = nullptr;   // skip-ahead powers (U576[32])
+  int rlx_seg = 0;            // refills per seed-table thread
+  // modal term list (device)
+  void* d_terms = nullptr;
+  int nterms = 0, nr_active = 0;
+  // plain FP64 form
+  void* plain = nullptr;
+  int last_launches = 0;      // kernels launched by the last run
+  size_t used_bytes = 0;      // device bytes this plan holds
+  // optional per-kernel timing: events recorded around every launch
+  bool profiling = false;
+  struct ProfRec {
+    const char* name;
+    cudaEvent_t a, b;
+  };
+  std::vector<ProfRec> prof;
+  std::vector<cudaEvent_t> event_pool;
+  // staging buffers of aar_run_host (grown on demand, kept for reuse)
+  float* d_io = nullptr;
+  int64_t io_cap = 0;
+};
+
+// Records CUDA events around the kernels launched in its scope (when the
+// plan's profiling is on), on the launching stream.
+struct ProfScope {
+  Plan* p;
+  int idx = -1;
+  cudaStream_t st;
+  ProfScope(Plan* pl, const char* name, cudaStream_t s);
+  ~ProfScope();
+};
+
+int plan_alloc(Plan* p, void** ptr, size_t bytes);
+size_t terms_bytes();
+
+const char* set_err(Plan* p, const std::string& e);
+
+// launchers (return 0 or an error code; errors leave a message on the plan)
+int launch_seedtable(Plan* p, uint32_t seed, uint32_t* d_out, cudaStream_t st);
+int launch_noise_fp32(Plan* p, const uint32_t* d_seed, float2* d_phik, cudaStream_t st);
+int launch_noise_fp64(Plan* p, const uint32_t* d_seed, double2* d_phik, int hp, cudaStream_t st);
+int fused_prepare(Plan* p);
+int fused_modal(Plan* p, cudaStream_t st);
+int fused_lpt(Plan* p, cudaStream_t st);
+int fused_readout(Plan* p, const float* d_lagr, int64_t npart, float* d_pos, float* d_vel, cudaStream_t st);
+int fused_readout_glass(Plan* p, const float* d_glass, int64_t nglass, double glass_box, int tile, float* d_pos,
+                        float* d_vel, int* d_ids, cudaStream_t st);
+int plain_run(Plan* p, const float* d_lagr, int64_t npart, float* d_pos, float* d_vel, cudaStream_t st);
+void plain_free(Plan* p);
+int fused_c2r(Plan* p, const float2* in, float* out, cudaStream_t st);
+int fused_r2c(Plan* p, const float* in, float2* out, cudaStream_t st);
+int fused_configure_xform(Plan* p);
+
+}  // namespace aar
+
+#define AAR_CUDA_TRY(p, call)                                                                  \
+  do {                                                                                         \
+    cudaError_t e_ = (call);                                                                   \
+    if (e_ != cudaSuccess) {                                                                   \
+      aar::set_err((p), std::string(#call) + ": " + cudaGetErrorString(e_));                  \
+      return AAR_ERR_CUDA;                                                                     \
+    }                                                                                          \
+  } while (0)

@@ -1,0 +1,603 @@
+// C ABI of libaarambam_gpu.so: plan life cycle, host set-up and the run
+// entry points.  Host scalars follow Aarambam/LPT/Basis/power.c:391-448
+// (sigma8 normalisation and growth factors, by Romberg integration as in
+// nrsrc/qromb.c), power.c:66-153 (transfer table), main.c:305-372.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <new>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "aar_internal.cuh"
+#include "ranlux.cuh"
+
+struct aar_plan {
+  aar::Plan p;
+};
+
+namespace aar {
+
+const char* set_err(Plan* p, const std::string& e) {
+  p->err = e;
+  return p->err.c_str();
+}
+
+int host_kcut(int nsample, double box) {
+  // largest m with (m*2*PI/Box)*Box/(2*PI) <= Nsample/2 (integer division),
+  // evaluated in the reference's operation order (main.c:410-441)
+  int half = nsample / 2;
+  int m = half + 1;
+  while (m >= 0) {
+    double kv = (double)(m * 2) * kPi / box;
+    if (!(fabs(kv) * box / (2 * kPi) > half)) break;
+    --m;
+  }
+  return m;
+}
+
+static cudaEvent_t pool_event(Plan* p) {
+  if (!p->event_pool.empty()) {
+    cudaEvent_t e = p->event_pool.back();
+    p->event_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+ProfScope::ProfScope(Plan* pl, const char* name, cudaStream_t s) : p(pl), st(s) {
+  if (!p->profiling) return;
+  Plan::ProfRec r{name, pool_event(p), pool_event(p)};
+  cudaEventRecord(r.a, st);
+  p->prof.push_back(r);
+  idx = (int)p->prof.size() - 1;
+}
+ProfScope::~ProfScope() {
+  if (idx >= 0) cudaEventRecord(p->prof[idx].b, st);
+}
+
+// ------------------------------------------------------------ cosmology
+struct Cosmo {
+  const Plan* p;
+  double norm;
+  double transfer(double k) const {  // power.c:181-217
+    k *= p->kconv;
+    double lk = log10(k);
+    const std::vector<double>& L = p->logk;
+    if (lk < L.front() || lk > L.back()) return 0;
+    int lo = 0, hi = (int)L.size() - 1;
+    while (hi - lo > 1) {
+      int mid = (hi + lo) / 2;
+      if (lk < L[mid]) hi = mid;
+      else lo = mid;
+    }
+    double u = (lk - L[lo]) / (L[hi] - L[lo]);
+    return pow(10.0, (1 - u) * p->logT[lo] + u * p->logT[hi]);
+  }
+};
+
+// Romberg quadrature: trapezoid refinements extrapolated to zero step with
+// Neville's algorithm over the last five estimates, relative tolerance 1e-8.
+template <class F>
+static double romberg(F&& f, double a, double b) {
+  const int K = 5, JMAX = 40;
+  std::vector<double> h(JMAX + 2), s(JMAX + 2);
+  double trap = 0;
+  h[1] = 1.0;
+  for (int j = 1; j <= JMAX; ++j) {
+    if (j == 1) {
+      trap = 0.5 * (b - a) * (f(a) + f(b));
+    } else {
+      long it = 1L << (j - 2);
+      double del = (b - a) / (double)it, x = a + 0.5 * del, sum = 0;
+      for (long q = 0; q < it; ++q, x += del) sum += f(x);
+      trap = 0.5 * (trap + (b - a) * sum / (double)it);
+    }
+    s[j] = trap;
+    if (j >= K) {
+      const double* xa = &h[j - K + 1];
+      const double* ya = &s[j - K + 1];
+      double c[5], d[5];
+      int ns = 0;
+      double dif = fabs(xa[0]);
+      for (int i = 0; i < K; ++i) {
+        if (fabs(xa[i]) < dif) {
+          ns = i;
+          dif = fabs(xa[i]);
+        }
+        c[i] = d[i] = ya[i];
+      }
+      double y = ya[ns--], dy = 0;
+      for (int m = 1; m < K; ++m) {
+        for (int i = 0; i < K - m; ++i) {
+          double ho = xa[i], hp = xa[i + m], w = c[i + 1] - d[i], den = w / (ho - hp);
+          d[i] = hp * den;
+          c[i] = ho * den;
+        }
+        dy = (2 * (ns + 1) < (K - m)) ? c[ns + 1] : d[ns--];
+        y += dy;
+      }
+      if (fabs(dy) <= 1e-8 * fabs(y)) return y;
+    }
+    h[j + 1] = 0.25 * h[j];
+  }
+  return NAN;
+}
+
+static double growth(double a, double Om, double OL) {  // power.c:587-598
+  double ha = sqrt(Om / (a * a * a) + (1 - Om - OL) / (a * a) + OL);
+  return ha * romberg([&](double x) { return pow(x / (Om + (1 - Om - OL) * x + OL * x * x * x), 1.5); }, 0, a);
+}
+
+static int set_transfer(Plan* p, const double* k, const double* t, int n) {
+  if (n < 2 || !k || !t) return set_err(p, "transfer table needs at least 2 rows"), AAR_ERR_ARG;
+  std::vector<std::pair<double, double>> rows(n);
+  for (int i = 0; i < n; ++i) {
+    if (!(k[i] > 0) || !(t[i] > 0)) return set_err(p, "transfer table needs positive k and T"), AAR_ERR_ARG;
+    rows[i] = {log10(k[i]), log10(t[i])};
+  }
+  std::stable_sort(rows.begin(), rows.end(), [](auto& a, auto& b) { return a.first < b.first; });
+  if (rows[0].first >= -4.6)
+    return set_err(p, "klower of the transfer table is too large to normalise (first log10 k >= -4.6)"),
+           AAR_ERR_TRANSFER;
+  for (int i = 1; i < n; ++i)
+    if (rows[i].first == rows[i - 1].first)
+      return set_err(p, "two transfer rows share one k"), AAR_ERR_TRANSFER_DUP;
+  p->logk.resize(n);
+  p->logT.resize(n);
+  for (int i = 0; i < n; ++i) {
+    p->logk[i] = rows[i].first;
+    p->logT[i] = rows[i].second - rows[0].second;
+  }
+  const aar_params& q = p->prm;
+  p->kconv = q.input_spectrum_unit_length_in_cm / q.unit_length_in_cm;
+  double UnitTime_in_s = q.unit_length_in_cm / q.unit_velocity_in_cm_per_s;
+  p->Hubble = 3.2407789e-18 * UnitTime_in_s;
+  p->InitTime = 1 / (1 + q.redshift);
+  double R8 = 8 * (3.085678e24 / q.unit_length_in_cm);
+  Cosmo cz{p, 1.0};
+  double res = romberg(
+      [&](double kk) {
+        double kr = R8 * kk, kr2 = kr * kr, kr3 = kr2 * kr;
+        if (kr < 1e-8) return 0.0;
+        double w = 3 * (sin(kr) / kr3 - cos(kr) / kr2);
+        double T = cz.transfer(kk);
+        double P = 1.0 * exp(q.primordial_index * log(kk)) * T * T;
+        return 4 * kPi * kk * kk * w * w * P;
+      },
+      0, 500.0 * 1 / R8);
+  p->Norm = q.sigma8 * q.sigma8 / res;
+  p->Anorm = p->Norm;
+  double Om = q.omega, OL = q.omega_lambda;
+  p->D0 = growth(1.0, Om, OL) / growth(1.e-8, Om, OL) * 1.e-8;
+  p->Dplus = growth(1.0, Om, OL) / growth(p->InitTime, Om, OL);
+  double a = p->InitTime;
+  double hubble_a = p->Hubble * sqrt(Om / pow(a, 3) + (1 - Om - OL) / pow(a, 2) + OL);
+  double om_a = Om / (Om + a * (1 - Om - OL) + a * a * a * OL);
+  p->vel_prefac = a * hubble_a * pow(om_a, 0.6) / sqrt(a);
+  p->vel_prefac2 = a * hubble_a * (2 * pow(om_a, 4. / 7.)) / sqrt(a);
+  p->Beta = 1.5 * Om / (2998. * 2998. / q.unit_length_in_cm / q.unit_length_in_cm * 3.085678e24 * 3.085678e24) /
+            p->D0;
+  p->have_transfer = true;
+
+  // per-n^2 tables for the FP32 form: noise amplitude and T / (D Beta)
+  if (p->prm.precision == AAR_FUSED_FP32) {
+    int N = p->N;
+    int64_t nsq = 3LL * (N / 2) * (N / 2) + 1;
+    std::vector<float> amp(nsq), twb(nsq);
+    double kF = 2 * kPi / q.box;
+    double fac = pow(2 * kPi / q.box, 1.5);
+    for (int64_t n2 = 0; n2 < nsq; ++n2) {
+      double km = kF * sqrt((double)n2), k2 = km * km;
+      amp[n2] = n2 ? (float)(sqrt(p->Anorm * exp(q.primordial_index * log(km))) * fac * p->Beta / k2) : 0.f;
+      twb[n2] = (float)(cz.transfer(km) / p->Dplus / p->Beta);
+    }
+    AAR_CUDA_TRY(p, cudaMemcpy(p->d_amp, amp.data(), sizeof(float) * nsq, cudaMemcpyHostToDevice));
+    AAR_CUDA_TRY(p, cudaMemcpy(p->d_twb, twb.data(), sizeof(float) * nsq, cudaMemcpyHostToDevice));
+  }
+  return AAR_OK;
+}
+
+// ------------------------------------------------------------ allocation
+int plan_alloc(Plan* p, void** ptr, size_t bytes) {
+  if (p->prm.mem_limit_bytes > 0 && p->used_bytes + bytes > (size_t)p->prm.mem_limit_bytes)
+    return set_err(p, "plan allocation above mem_limit_bytes"), AAR_ERR_OOM;
+  cudaError_t e = cudaMalloc(ptr, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    *ptr = nullptr;
+    return set_err(p, std::string("cudaMalloc: ") + cudaGetErrorString(e)), AAR_ERR_OOM;
+  }
+  p->used_bytes += bytes;
+  return AAR_OK;
+}
+
+static void plan_release(Plan* p) {
+  for (auto& r : p->prof) {
+    cudaEventDestroy(r.a);
+    cudaEventDestroy(r.b);
+  }
+  p->prof.clear();
+  for (auto e : p->event_pool) cudaEventDestroy(e);
+  p->event_pool.clear();
+  void* ptrs[] = {p->d_phik, p->d_work, p->d_seed, p->d_twN, p->d_twH, p->d_amp, p->d_twb, p->d_rlxpow, p->d_terms, p->d_io};
+  for (void* q : ptrs)
+    if (q) cudaFree(q);
+  p->d_phik = p->d_work = nullptr;
+  p->d_seed = nullptr;
+  p->d_twN = p->d_twH = nullptr;
+  p->d_amp = p->d_twb = nullptr;
+  p->d_rlxpow = p->d_terms = nullptr;
+  p->d_io = nullptr;
+  p->io_cap = 0;
+  plain_free(p);
+}
+
+static bool pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
+
+static int alloc_fused(Plan* p, int M) {
+  int N = p->N;
+  size_t fbytes = sizeof(float2) * (size_t)N * N * p->HP;
+  int nwork = std::max(M, 7);
+  if (p->d_work && p->nwork >= nwork) return AAR_OK;
+  if (p->d_work) {
+    cudaFree(p->d_work);
+    p->used_bytes -= fbytes * p->nwork;
+    p->d_work = nullptr;
+  }
+  int rc = plan_alloc(p, (void**)&p->d_work, fbytes * nwork);
+  if (rc) return rc;
+  p->nwork = nwork;
+  return AAR_OK;
+}
+
+static int create(Plan* p) {
+  const aar_params& q = p->prm;
+  int N = q.nmesh;
+  if (q.nsample > q.nmax) return set_err(p, "Nmax must be >= Nsample (main.c:200)"), AAR_ERR_NMAX;
+  if (q.precision != AAR_FUSED_FP32 && q.precision != AAR_PLAIN_FP64)
+    return set_err(p, "unknown precision"), AAR_ERR_ARG;
+  if (q.precision == AAR_FUSED_FP32 && !(pow2(N) && N >= 16 && N <= 1024))
+    return set_err(p, "fused FP32 form supports Nmesh = 16..1024, powers of two"), AAR_ERR_ARG;
+  if (q.precision == AAR_PLAIN_FP64 && !(N >= 4 && N % 2 == 0 && N <= 2048))
+    return set_err(p, "plain FP64 form supports even Nmesh up to 2048"), AAR_ERR_ARG;
+  if (!(q.box > 0) || q.nsample <= 0) return set_err(p, "Box and Nsample must be positive"), AAR_ERR_ARG;
+  if (q.seed < 0) return set_err(p, "Seed must be >= 0"), AAR_ERR_ARG;
+  AAR_CUDA_TRY(p, cudaGetDevice(&p->dev));
+  p->N = N;
+  p->HP = ((N / 2 + 1) + 7) / 8 * 8;
+  p->grid.N = N;
+  p->grid.HP = p->HP;
+  p->grid.kcut = host_kcut(q.nsample, q.box);
+  p->grid.sphere = q.sphere_mode == 1;
+  p->grid.nsq_bnd = (q.nsample / 2) * (q.nsample / 2);
+  p->grid.nsample_half = q.nsample / 2;
+  p->grid.box = q.box;
+  p->grid.kF = (float)(2 * kPi / q.box);
+
+  int rc;
+  if ((rc = plan_alloc(p, (void**)&p->d_seed, sizeof(uint32_t) * (size_t)N * N))) return rc;
+  // ranlux skip-ahead: seed-table threads own rlx_seg refills; powers
+  // (b^{-202 rlx_seg})^{2^i} mod m, i < 32
+  p->rlx_seg = 8;
+  {
+    std::vector<U576> pw(32);
+    U576 a = modpow576(u576_binv(), (uint64_t)kRlxLux * p->rlx_seg);
+    for (int i = 0; i < 32; ++i) {
+      pw[i] = a;
+      a = modmul576(a, a);
+    }
+    if ((rc = plan_alloc(p, &p->d_rlxpow, sizeof(U576) * 32))) return rc;
+    AAR_CUDA_TRY(p, cudaMemcpy(p->d_rlxpow, pw.data(), sizeof(U576) * 32, cudaMemcpyHostToDevice));
+  }
+  if (q.precision == AAR_FUSED_FP32) {
+    size_t fbytes = sizeof(float2) * (size_t)N * N * p->HP;
+    if ((rc = plan_alloc(p, (void**)&p->d_phik, fbytes))) return rc;
+    std::vector<float2> twN(N), twH(N / 2);
+    for (int m = 0; m < N; ++m) {
+      long double ang = -2.0L * 3.141592653589793238462643383279502884L * m / N;
+      twN[m] = make_float2((float)cosl(ang), (float)sinl(ang));
+    }
+    for (int m = 0; m < N / 2; ++m) twH[m] = twN[2 * m];
+    if ((rc = plan_alloc(p, (void**)&p->d_twN, sizeof(float2) * N))) return rc;
+    if ((rc = plan_alloc(p, (void**)&p->d_twH, sizeof(float2) * (N / 2)))) return rc;
+    AAR_CUDA_TRY(p, cudaMemcpy(p->d_twN, twN.data(), sizeof(float2) * N, cudaMemcpyHostToDevice));
+    AAR_CUDA_TRY(p, cudaMemcpy(p->d_twH, twH.data(), sizeof(float2) * (N / 2), cudaMemcpyHostToDevice));
+    int64_t nsq = 3LL * (N / 2) * (N / 2) + 1;
+    if ((rc = plan_alloc(p, (void**)&p->d_amp, sizeof(float) * nsq))) return rc;
+    if ((rc = plan_alloc(p, (void**)&p->d_twb, sizeof(float) * nsq))) return rc;
+  }
+  return AAR_OK;
+}
+
+static cudaStream_t S(void* s) { return (cudaStream_t)s; }
+
+static int ready(Plan* p) {
+  if (!p->have_tables) return set_err(p, "coefficient tables not set"), AAR_ERR_STATE;
+  if (!p->have_transfer) return set_err(p, "transfer function not set"), AAR_ERR_STATE;
+  return AAR_OK;
+}
+
+static int run_noise(Plan* p, cudaStream_t st) {
+  int rc = launch_seedtable(p, (uint32_t)p->prm.seed, p->d_seed, st);
+  if (rc) return rc;
+  return launch_noise_fp32(p, p->d_seed, p->d_phik, st);
+}
+
+}  // namespace aar
+
+using namespace aar;
+
+extern "C" {
+
+int aar_version(void) { return 1; }
+
+int aar_plan_create(const aar_params* prm, aar_plan** out) {
+  if (!prm || !out) return AAR_ERR_ARG;
+  *out = nullptr;
+  aar_plan* h = new (std::nothrow) aar_plan();
+  if (!h) return AAR_ERR_OOM;
+  h->p.prm = *prm;
+  int rc = create(&h->p);
+  if (rc) {
+    // keep the plan so the caller can read the message, but free device memory
+    plan_release(&h->p);
+    *out = h;
+    return rc;
+  }
+  *out = h;
+  return AAR_OK;
+}
+
+void aar_plan_destroy(aar_plan* h) {
+  if (!h) return;
+  plan_release(&h->p);
+  delete h;
+}
+
+const char* aar_last_error(const aar_plan* h) { return h ? h->p.err.c_str() : "null plan"; }
+
+int aar_last_launch_count(const aar_plan* h) { return h ? h->p.last_launches : 0; }
+
+int aar_set_tables(aar_plan* h, const double* alpha, const double* x0, int32_t M) {
+  if (!h) return AAR_ERR_ARG;
+  Plan* p = &h->p;
+  if (M < 1 || M > 32 || !alpha || !x0) return set_err(p, "N_modes must be 1..32 with non-null tables"), AAR_ERR_ARG;
+  size_t n3 = (size_t)M * M * M;
+  for (size_t i = 0; i < n3; ++i)
+    if (!isfinite(alpha[i])) return set_err(p, "non-finite alpha coefficient"), AAR_ERR_ARG;
+  for (int i = 0; i < M; ++i)
+    if (!isfinite(x0[i])) return set_err(p, "non-finite X0 coefficient"), AAR_ERR_ARG;
+  p->alpha.assign(alpha, alpha + n3);
+  p->x0.assign(x0, x0 + M);
+  p->M = M;
+  int rc;
+  if (p->prm.precision == AAR_FUSED_FP32) {
+    if ((rc = alloc_fused(p, M))) return rc;
+    if (!p->d_terms && (rc = plan_alloc(p, &p->d_terms, terms_bytes()))) return rc;
+    if ((rc = fused_prepare(p))) return rc;
+    if ((rc = fused_configure_xform(p))) return rc;
+  }
+  p->have_tables = true;
+  return AAR_OK;
+}
+
+int aar_set_transfer(aar_plan* h, const double* k, const double* t, int32_t n) {
+  if (!h) return AAR_ERR_ARG;
+  return set_transfer(&h->p, k, t, n);
+}
+
+int aar_get_scalars(const aar_plan* h, aar_scalars* o) {
+  if (!h || !o) return AAR_ERR_ARG;
+  const Plan* p = &h->p;
+  *o = aar_scalars{p->Norm, p->Anorm, p->D0, p->Dplus, p->InitTime, p->Hubble, p->Beta, p->vel_prefac, p->vel_prefac2};
+  return AAR_OK;
+}
+
+int aar_set_seed(aar_plan* h, int32_t seed) {
+  if (!h) return AAR_ERR_ARG;
+  if (seed < 0) return set_err(&h->p, "Seed must be >= 0"), AAR_ERR_ARG;
+  h->p.prm.seed = seed;
+  return AAR_OK;
+}
+
+int aar_seedtable(aar_plan* h, uint32_t* d_out, void* stream) {
+  if (!h || !d_out) return AAR_ERR_ARG;
+  h->p.last_launches = 0;
+  return launch_seedtable(&h->p, (uint32_t)h->p.prm.seed, d_out, S(stream));
+}
+
+int aar_stage_noise(aar_plan* h, void* stream) {
+  if (!h) return AAR_ERR_ARG;
+  Plan* p = &h->p;
+  int rc = ready(p);
+  if (rc) return rc;
+  p->last_launches = 0;
+  if (p->prm.precision != AAR_FUSED_FP32) return set_err(p, "stage calls are for the fused form"), AAR_ERR_ARG;
+  return run_noise(p, S(stream));
+}
+
+int aar_stage_modal(aar_plan* h, void* stream) {
+  if (!h) return AAR_ERR_ARG;
+  Plan* p = &h->p;
+  int rc = ready(p);
+  if (rc) return rc;
+  p->last_launches = 0;
+  if (p->prm.precision != AAR_FUSED_FP32) return set_err(p, "stage calls are for the fused form"), AAR_ERR_ARG;
+  return fused_modal(p, S(stream));
+}
+
+int aar_stage_lpt(aar_plan* h, void* stream) {
+  if (!h) return AAR_ERR_ARG;
+  Plan* p = &h->p;
+  int rc = ready(p);
+  if (rc) return rc;
+  p->last_launches = 0;
+  if (p->prm.precision != AAR_FUSED_FP32) return set_err(p, "stage calls are for the fused form"), AAR_ERR_ARG;
+  return fused_lpt(p, S(stream));
+}
+
+int aar_stage_readout(aar_plan* h, const float* d_lagr, int64_t npart, float* d_pos, float* d_vel, void* stream) {
+  if (!h || npart < 0 || (npart > 0 && (!d_lagr || !d_pos || !d_vel))) return AAR_ERR_ARG;
+  Plan* p = &h->p;
+  p->last_launches = 0;
+  if (p->prm.precision != AAR_FUSED_FP32) return set_err(p, "stage calls are for the fused form"), AAR_ERR_ARG;
+  return fused_readout(p, d_lagr, npart, d_pos, d_vel, S(stream));
+}
+
+int aar_run(aar_plan* h, const float* d_lagr, int64_t npart, float* d_pos, float* d_vel, void* stream) {
+  if (!h || npart < 0 || (npart > 0 && (!d_lagr || !d_pos || !d_vel))) return AAR_ERR_ARG;
+  Plan* p = &h->p;
+  int rc = ready(p);
+  if (rc) return rc;
+  p->last_launches = 0;
+  cudaStream_t st = S(stream);
+  if (p->prm.precision == AAR_PLAIN_FP64) return plain_run(p, d_lagr, npart, d_pos, d_vel, st);
+  if ((rc = run_noise(p, st))) return rc;
+  if ((rc = fused_modal(p, st))) return rc;
+  if ((rc = fused_lpt(p, st))) return rc;
+  return fused_readout(p, d_lagr, npart, d_pos, d_vel, st);
+}
+
+int aar_run_glass(aar_plan* h, const float* d_glass, int64_t nglass, double glass_box, int32_t tile, float* d_pos,
+                  float* d_vel, int32_t* d_ids, void* stream) {
+  if (!h || nglass < 0 || tile < 1 || !(glass_box > 0)) return AAR_ERR_ARG;
+  Plan* p = &h->p;
+  int rc = ready(p);
+  if (rc) return rc;
+  if (p->prm.precision != AAR_FUSED_FP32) return set_err(p, "aar_run_glass is for the fused form"), AAR_ERR_ARG;
+  p->last_launches = 0;
+  cudaStream_t st = S(stream);
+  if ((rc = run_noise(p, st))) return rc;
+  if ((rc = fused_modal(p, st))) return rc;
+  if ((rc = fused_lpt(p, st))) return rc;
+  return fused_readout_glass(p, d_glass, nglass, glass_box, tile, d_pos, d_vel, d_ids, st);
+}
+
+int aar_run_host(aar_plan* h, const float* h_lagr, int64_t npart, float* h_pos, float* h_vel, void* stream) {
+  if (!h || npart < 0 || (npart > 0 && (!h_lagr || !h_pos || !h_vel))) return AAR_ERR_ARG;
+  Plan* p = &h->p;
+  cudaStream_t st = S(stream);
+  size_t bytes = sizeof(float) * 3 * (size_t)npart;
+  if (npart > p->io_cap) {  // plan-owned staging: in, pos, vel
+    if (p->d_io) {
+      cudaFree(p->d_io);
+      p->used_bytes -= 3 * sizeof(float) * 3 * (size_t)p->io_cap;
+      p->d_io = nullptr;
+      p->io_cap = 0;
+    }
+    int rc = plan_alloc(p, (void**)&p->d_io, 3 * bytes);
+    if (rc) return rc;
+    p->io_cap = npart;
+  }
+  float* d_in = p->d_io;
+  float* d_pos = d_in + 3 * (size_t)npart;
+  float* d_vel = d_pos + 3 * (size_t)npart;
+  if (npart > 0) AAR_CUDA_TRY(p, cudaMemcpyAsync(d_in, h_lagr, bytes, cudaMemcpyHostToDevice, st));
+  int rc = aar_run(h, d_in, npart, d_pos, d_vel, stream);
+  if (rc) return rc;
+  if (npart > 0) {
+    AAR_CUDA_TRY(p, cudaMemcpyAsync(h_pos, d_pos, bytes, cudaMemcpyDeviceToHost, st));
+    AAR_CUDA_TRY(p, cudaMemcpyAsync(h_vel, d_vel, bytes, cudaMemcpyDeviceToHost, st));
+  }
+  AAR_CUDA_TRY(p, cudaStreamSynchronize(st));
+  return AAR_OK;
+}
+
+int aar_copy_spectrum(aar_plan* h, void* d_out, void* stream) {
+  if (!h || !d_out) return AAR_ERR_ARG;
+  Plan* p = &h->p;
+  if (p->prm.precision != AAR_FUSED_FP32 || !p->d_phik) return set_err(p, "no FP32 spectrum in this plan"), AAR_ERR_STATE;
+  int N = p->N, H = N / 2 + 1;
+  AAR_CUDA_TRY(p, cudaMemcpy2DAsync(d_out, sizeof(float2) * H, p->d_phik, sizeof(float2) * p->HP, sizeof(float2) * H,
+                                    (size_t)N * N, cudaMemcpyDeviceToDevice, S(stream)));
+  return AAR_OK;
+}
+
+static int need_work(Plan* p) {
+  if (p->prm.precision != AAR_FUSED_FP32) return set_err(p, "transforms are for the fused form"), AAR_ERR_ARG;
+  if (!p->d_work) {
+    int rc = alloc_fused(p, 1);
+    if (rc) return rc;
+    if ((rc = fused_configure_xform(p))) return rc;
+  }
+  return AAR_OK;
+}
+
+int aar_c2r(aar_plan* h, const void* d_in, float* d_out, void* stream) {
+  if (!h || !d_in || !d_out) return AAR_ERR_ARG;
+  Plan* p = &h->p;
+  int rc = need_work(p);
+  if (rc) return rc;
+  p->last_launches = 0;
+  return fused_c2r(p, (const float2*)d_in, d_out, S(stream));
+}
+
+int aar_r2c(aar_plan* h, const float* d_in, void* d_out, void* stream) {
+  if (!h || !d_in || !d_out) return AAR_ERR_ARG;
+  Plan* p = &h->p;
+  int rc = need_work(p);
+  if (rc) return rc;
+  p->last_launches = 0;
+  return fused_r2c(p, d_in, (float2*)d_out, S(stream));
+}
+
+int aar_profile_enable(aar_plan* h, int32_t on) {
+  if (!h) return AAR_ERR_ARG;
+  h->p.profiling = on != 0;
+  return AAR_OK;
+}
+
+int aar_profile_report(aar_plan* h, char* buf, int32_t len) {
+  if (!h || !buf || len <= 0) return AAR_ERR_ARG;
+  Plan* p = &h->p;
+  AAR_CUDA_TRY(p, cudaDeviceSynchronize());
+  std::vector<std::string> names;
+  std::vector<double> ms;
+  std::vector<int> cnt;
+  for (auto& r : p->prof) {
+    float t = 0;
+    cudaEventElapsedTime(&t, r.a, r.b);
+    size_t i = 0;
+    while (i < names.size() && names[i] != r.name) ++i;
+    if (i == names.size()) {
+      names.push_back(r.name);
+      ms.push_back(0);
+      cnt.push_back(0);
+    }
+    ms[i] += t;
+    cnt[i] += 1;
+    p->event_pool.push_back(r.a);
+    p->event_pool.push_back(r.b);
+  }
+  p->prof.clear();
+  std::string out;
+  for (size_t i = 0; i < names.size(); ++i) {
+    char line[256];
+    snprintf(line, sizeof(line), "%s,%d,%.6f\n", names[i].c_str(), cnt[i], ms[i]);
+    out += line;
+  }
+  if ((int)out.size() + 1 > len) return set_err(p, "profile report buffer too small"), AAR_ERR_ARG;
+  memcpy(buf, out.c_str(), out.size() + 1);
+  return AAR_OK;
+}
+
+int aar_copy_field(aar_plan* h, int32_t which, float* d_out, void* stream) {
+  if (!h || !d_out || which < 0 || which > 5) return AAR_ERR_ARG;
+  Plan* p = &h->p;
+  if (p->prm.precision != AAR_FUSED_FP32 || !p->d_work) return set_err(p, "no FP32 fields in this plan"), AAR_ERR_STATE;
+  int N = p->N;
+  const float* src = (const float*)(p->d_work + (size_t)which * N * N * p->HP);
+  AAR_CUDA_TRY(p, cudaMemcpy2DAsync(d_out, sizeof(float) * N, src, sizeof(float) * 2 * p->HP, sizeof(float) * N,
+                                    (size_t)N * N, cudaMemcpyDeviceToDevice, S(stream)));
+  return AAR_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,225 @@
+// FP32 line FFTs for sm_103a: register DFTs of radix 2..32 with compile-time
+// twiddles, composed into Stockham auto-sort stages that exchange through a
+// padded shared-memory line buffer.  A line of length N is owned by T lanes of
+// one warp (E = N / T values per lane); a warp may own several short lines.
+//
+// Stage formulation: Govindaraju et al., "High performance discrete Fourier
+// transforms on graphics processors", SC'08, Fig. 2 (iteration j, radix R,
+// span Ns: inputs x[j + r N/R], twiddle exp(s 2 pi i r (j mod Ns)/(Ns R)),
+// outputs y[(j/Ns) Ns R + (j mod Ns) + r Ns]).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace aar {
+
+// ---------------------------------------------------------------- complex
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
+__device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+
+// --------------------------------------------- compile-time trigonometry
+// cos / sin of 2 pi k / n evaluated by quadrant reduction and Taylor series
+// in double precision during compilation.
+__host__ __device__ constexpr double ce_sin_small(double x) {
+  double x2 = x * x, term = x, sum = x;
+  for (int n = 1; n < 14; ++n) {
+    term *= -x2 / ((2.0 * n) * (2.0 * n + 1));
+    sum += term;
+  }
+  return sum;
+}
+__host__ __device__ constexpr double ce_cos_small(double x) {
+  double x2 = x * x, term = 1, sum = 1;
+  for (int n = 1; n < 14; ++n) {
+    term *= -x2 / ((2.0 * n - 1) * (2.0 * n));
+    sum += term;
+  }
+  return sum;
+}
+__host__ __device__ constexpr double ce_cos2pi(long k, long n) {
+  long t = ((k % n) + n) % n;
+  long q = (4 * t) / n, r = 4 * t - q * n;
+  double a = 1.5707963267948966192313216916397514 * (double)r / (double)n;
+  double c = ce_cos_small(a), s = ce_sin_small(a);
+  return q == 0 ? c : q == 1 ? -s : q == 2 ? -c : s;
+}
+__host__ __device__ constexpr double ce_sin2pi(long k, long n) {
+  long t = ((k % n) + n) % n;
+  long q = (4 * t) / n, r = 4 * t - q * n;
+  double a = 1.5707963267948966192313216916397514 * (double)r / (double)n;
+  double c = ce_cos_small(a), s = ce_sin_small(a);
+  return q == 0 ? s : q == 1 ? c : q == 2 ? -s : -c;
+}
+
+// multiply by exp(SIGN * 2 pi i K / R) with the trivial angles special-cased
+template <int R, int K, int SIGN>
+__device__ __forceinline__ float2 twiddle_ct(float2 v) {
+  constexpr int k = ((K % R) + R) % R;
+  if constexpr (k == 0) {
+    return v;
+  } else if constexpr (4 * k == R) {  // SIGN * i
+    return SIGN < 0 ? make_float2(v.y, -v.x) : make_float2(-v.y, v.x);
+  } else if constexpr (2 * k == R) {
+    return make_float2(-v.x, -v.y);
+  } else if constexpr (4 * k == 3 * R) {  // -SIGN * i
+    return SIGN < 0 ? make_float2(-v.y, v.x) : make_float2(v.y, -v.x);
+  } else {
+    constexpr float c = (float)ce_cos2pi(k, R);
+    constexpr float s = (float)(SIGN * ce_sin2pi(k, R));
+    return make_float2(v.x * c - v.y * s, v.x * s + v.y * c);
+  }
+}
+
+// ------------------------------------------------------ register DFTs
+// In-place DFT of R values, natural order in and out: X_k = sum x_r w^{rk},
+// w = exp(SIGN 2 pi i / R).  Radix-2 decimation in time, fully unrolled.
+template <int R, int SIGN>
+struct DFT {
+  template <int K>
+  static __device__ __forceinline__ void combine(float2* v, const float2* e, const float2* o) {
+    if constexpr (K < R / 2) {
+      float2 t = twiddle_ct<R, K, SIGN>(o[K]);
+      v[K] = cadd(e[K], t);
+      v[K + R / 2] = csub(e[K], t);
+      combine<K + 1>(v, e, o);
+    }
+  }
+  static __device__ __forceinline__ void run(float2* v) {
+    if constexpr (R == 1) {
+      return;
+    } else if constexpr (R == 2) {
+      float2 a = v[0], b = v[1];
+      v[0] = cadd(a, b);
+      v[1] = csub(a, b);
+    } else if constexpr (R == 4) {
+      float2 s0 = cadd(v[0], v[2]), d0 = csub(v[0], v[2]);
+      float2 s1 = cadd(v[1], v[3]), d1 = csub(v[1], v[3]);
+      float2 rd1 = twiddle_ct<4, 1, SIGN>(d1);
+      v[0] = cadd(s0, s1);
+      v[2] = csub(s0, s1);
+      v[1] = cadd(d0, rd1);
+      v[3] = csub(d0, rd1);
+    } else {
+      float2 e[R / 2], o[R / 2];
+#pragma unroll
+      for (int i = 0; i < R / 2; ++i) {
+        e[i] = v[2 * i];
+        o[i] = v[2 * i + 1];
+      }
+      DFT<R / 2, SIGN>::run(e);
+      DFT<R / 2, SIGN>::run(o);
+      combine<0>(v, e, o);
+    }
+  }
+};
+
+// ------------------------------------------------------ stage planning
+// Radix of stage s for a line of length N with E values per lane: the
+// largest power of two <= E that divides what is left of N.
+__host__ __device__ constexpr int stage_radix(int N, int E, int s) {
+  int left = N, r = 1;
+  for (int i = 0; i <= s; ++i) {
+    r = 1;
+    while (r * 2 <= E && left % (r * 2) == 0) r *= 2;
+    if (i < s) left /= r;
+  }
+  return left == 1 ? 1 : r;
+}
+__host__ __device__ constexpr int stage_span(int N, int E, int s) {  // Ns before stage s
+  int ns = 1;
+  for (int i = 0; i < s; ++i) ns *= stage_radix(N, E, i);
+  return ns;
+}
+__host__ __device__ constexpr int num_stages(int N, int E) {
+  int s = 0;
+  while (stage_span(N, E, s) < N) ++s;
+  return s;
+}
+
+// padded shared-memory index: one spare slot per 32 entries
+__device__ __forceinline__ int spad(int i) { return i + (i >> 5); }
+__host__ __device__ constexpr int spad_len(int n) { return n + n / 32 + 4; }
+
+// Twiddle table for length N in global memory: tw[m] = exp(-2 pi i m / N).
+// Runtime twiddle exp(SIGN 2 pi i m / N).
+template <int SIGN>
+__device__ __forceinline__ float2 tw_load(const float2* __restrict__ tw, int m) {
+  float2 w = __ldg(tw + m);
+  return SIGN < 0 ? w : make_float2(w.x, -w.y);
+}
+
+// One Stockham stage on the values a lane holds: v[b*R + r] = x[j + r N/R],
+// j = t + T b.  On return v[b*R + r] = y[(j/Ns) Ns R + j%Ns + r Ns].
+template <int N, int T, int R, int Ns, int SIGN>
+__device__ __forceinline__ void stage_compute(float2* v, int t, const float2* __restrict__ tw) {
+  constexpr int E = N / T;
+#pragma unroll
+  for (int b = 0; b < E / R; ++b) {
+    int j = t + T * b;
+    if constexpr (Ns > 1) {
+      int k = j % Ns;
+#pragma unroll
+      for (int r = 1; r < R; ++r) v[b * R + r] = cmul(v[b * R + r], tw_load<SIGN>(tw, r * k * (N / (Ns * R))));
+    }
+    DFT<R, SIGN>::run(v + b * R);
+  }
+}
+
+// Write stage outputs into the line buffer (natural index, padded).
+template <int N, int T, int R, int Ns>
+__device__ __forceinline__ void stage_store(const float2* v, float2* s, int t) {
+  constexpr int E = N / T;
+#pragma unroll
+  for (int b = 0; b < E / R; ++b) {
+    int j = t + T * b;
+    int base = (j / Ns) * Ns * R + (j % Ns);
+#pragma unroll
+    for (int r = 0; r < R; ++r) s[spad(base + r * Ns)] = v[b * R + r];
+  }
+}
+
+// Read the inputs of a stage of radix R from the line buffer.
+template <int N, int T, int R>
+__device__ __forceinline__ void stage_load(float2* v, const float2* s, int t) {
+  constexpr int E = N / T;
+#pragma unroll
+  for (int b = 0; b < E / R; ++b) {
+    int j = t + T * b;
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[b * R + r] = s[spad(j + r * (N / R))];
+  }
+}
+
+// Full line FFT.  On entry the line (natural order) is in the buffer s; on
+// exit the transform is in s (natural order).  All T lanes of the line call
+// this together; `sync` is the barrier among the lanes sharing s.
+// Lanes with act == false (no line of their own) only take part in the
+// warp barriers.
+template <int N, int T, int SIGN, int S = 0>
+__device__ __forceinline__ void line_fft_smem(float2* s, int t, const float2* __restrict__ tw, bool act) {
+  constexpr int E = N / T;
+  constexpr int NS = num_stages(N, E);
+  if constexpr (S < NS) {
+    constexpr int R = stage_radix(N, E, S);
+    constexpr int Ns = stage_span(N, E, S);
+    float2 v[E];
+    if (act) stage_load<N, T, R>(v, s, t);
+    __syncwarp();
+    if (act) {
+      stage_compute<N, T, R, Ns, SIGN>(v, t, tw);
+      stage_store<N, T, R, Ns>(v, s, t);
+    }
+    __syncwarp();
+    line_fft_smem<N, T, SIGN, S + 1>(s, t, tw, act);
+  }
+}
+
+// lanes per line and values per lane for a line of length N
+__host__ __device__ constexpr int lanes_for(int N) { return N >= 256 ? 32 : (N / 8 >= 1 ? (N / 8 < 32 ? N / 8 : 32) : 1); }
+
+}  // namespace aar

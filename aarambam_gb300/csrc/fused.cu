@@ -1,0 +1,1023 @@
+// Fused FP32 form of the Aarambam IC path on sm_103a.
+//
+// Fields live in HBM as complex half spectra float2 [N][N][HP] (HP >= N/2+1,
+// a multiple of 8 so rows are 64-byte aligned); after a c2r the same buffer
+// holds the real field as float [N][N][2 HP] (z fastest).  A 3-D transform is
+// three passes, each reading and writing a field once:
+//   x pass / y pass  -- strided complex FFTs on tiles of W consecutive kz
+//                       columns x N rows, staged through shared memory;
+//   z pass (rows)    -- the real<->half-complex transform of contiguous rows
+//                       as an N/2-point complex FFT plus the usual
+//                       even/odd split twiddle step.
+// The reference's per-pass work is fused into these passes:
+//   modal potential (Aarambam/LPT/Basis/main.c:564-1151) regrouped exactly by
+//   linearity of the DFT: acc = sum_r rho_r(k) r2c[ g_r ],
+//   g_r(x) = sum_{p<=q} a'_{pqr} f_p(x) f_q(x), f_p = c2r[ q_p(k) phi(k) ],
+//   with a' = alpha on sorted triples plus the two counter-terms of
+//   main.c:1045-1050.  The x pass that starts every f_p reads phi once and
+//   applies q_p; one row kernel does all c2r's, products and r2c's of a row;
+//   the last x pass applies rho_r, sums over r and adds Fnl acc / N^3.
+//   2LPT (main.c:1156-1381): Hessians straight from phi (-k_a k_b T/(D Beta)),
+//   the source in the row kernel, Poisson + CIC deconvolution fused into the
+//   x pass that also starts the six displacement c2r's.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "aar_internal.cuh"
+#include "fft.cuh"
+
+namespace aar {
+
+// ----------------------------------------------------------- parameters
+struct ModalArgs {
+  Grid g;
+  float s;          // (4 - ns) / 3
+  float ns;
+  float kmin_s;     // kmin^s
+  float inv_dks;    // 1 / (kmax^s - kmin^s)
+  float ln_kF;      // log(kF)
+  int M;
+  float x0[32];     // X0[n]
+};
+
+struct Term {      // one product f_p f_q with coefficient c into g_r
+  int p, q, r;
+  float c;
+};
+
+constexpr int kMaxModes = 32;
+constexpr int kMaxTerms = 2048;
+
+struct TermList {
+  int nterms, nr;
+  int r_of_slot[kMaxModes];       // active r values (ascending)
+  int begin[kMaxModes + 1];       // terms of slot s: [begin[s], begin[s+1])
+};
+
+// term list in plan-owned device memory (read uniformly by all threads)
+struct DevTerms {
+  TermList tl;
+  Term t[kMaxTerms];
+};
+size_t terms_bytes() { return sizeof(DevTerms); }
+
+// ----------------------------------------------------------- k helpers
+struct KCell {
+  float k2, k1, kbar;
+  bool keep;
+};
+
+__device__ __forceinline__ KCell kcell(const ModalArgs& a, int kx, int ky, int kz) {
+  KCell c;
+  int n2 = kx * kx + ky * ky + kz * kz;
+  c.keep = n2 != 0 && keep_cell(a.g, kx, ky, kz);
+  float nn = (float)(n2 ? n2 : 1);
+  c.k2 = a.g.kF * a.g.kF * nn;
+  c.k1 = a.g.kF * sqrtf(nn);
+  // k^s = exp(s (ln kF + ln n / 2))
+  float ks = expf(a.s * (a.ln_kF + 0.5f * logf(nn)));
+  c.kbar = -1.f + 2.f * (ks - a.kmin_s) * a.inv_dks;
+  return c;
+}
+
+// P_l(x) by the Bonnet recurrence
+__device__ __forceinline__ float legendre(int l, float x) {
+  if (l == 0) return 1.f;
+  float p0 = 1.f, p1 = x;
+  for (int n = 2; n <= l; ++n) {
+    float p2 = ((2 * n - 1) * x * p1 - (n - 1) * p0) / (float)n;
+    p0 = p1;
+    p1 = p2;
+  }
+  return p1;
+}
+
+// radial part of mode n (main.c:833-860): k^{s(n-3)} (n <= 3) or
+// (P_{n-1}(kbar) - X0[n-1]) / k^2
+__device__ __forceinline__ float mode_out(const ModalArgs& a, int n, const KCell& c) {
+  if (n <= 3) return expf(a.s * (float)(n - 3) * logf(c.k1));
+  return (legendre(n - 1, c.kbar) - a.x0[n - 1]) / c.k2;
+}
+// field filter (main.c:606-637): mode_out * k^{4-ns}
+__device__ __forceinline__ float mode_in(const ModalArgs& a, int n, const KCell& c) {
+  float lk = logf(c.k1);
+  if (n <= 3) return expf((a.s * (float)(n - 3) + 4.f - a.ns) * lk);
+  return (legendre(n - 1, c.kbar) - a.x0[n - 1]) * expf((2.f - a.ns) * lk);
+}
+
+// ----------------------------------------------------------- tile passes
+template <int N, int W>
+struct AxisCfg {
+  static constexpr int T = lanes_for(N);
+  static constexpr int E = N / T;
+  static constexpr int LPW = 32 / T;  // lines per warp
+  static constexpr int WARPS = (W + LPW - 1) / LPW;
+  static constexpr int THREADS = WARPS * 32;
+  static constexpr int LS = spad_len(N);  // smem line stride (float2)
+  static constexpr size_t SMEM = sizeof(float2) * (size_t)W * LS;
+};
+
+// run the W line FFTs of a tile held in shared memory
+template <int N, int W, int SIGN>
+__device__ __forceinline__ void tile_fft(float2* sm, const float2* __restrict__ tw) {
+  using C = AxisCfg<N, W>;
+  int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int line = warp * C::LPW + lane / C::T;
+  int t = lane % C::T;
+  bool act = line < W;
+  line_fft_smem<N, C::T, SIGN>(sm + (act ? line : 0) * C::LS, t, tw, act);
+}
+
+// Tile indexing.  Axis 0 (x): rows n = x, other index o = y.  Axis 1 (y):
+// rows n = y, o = x.  Column w covers kz = c0 + w.
+template <int AXIS>
+__device__ __forceinline__ int64_t tile_elem(int N, int HP, int o, int c0, int n, int w) {
+  if (AXIS == 0) return ((int64_t)n * N + o) * HP + c0 + w;
+  return ((int64_t)o * N + n) * HP + c0 + w;
+}
+
+// In-place complex pass along AXIS over fields [0, nf) of `base` (field
+// stride fs).  blockIdx.x = tile, blockIdx.y = field.
+template <int N, int W, int AXIS, int SIGN>
+__global__ void __launch_bounds__(AxisCfg<N, W>::THREADS) k_axis_inplace(float2* base, int64_t fs, int HP,
+                                                                          const float2* __restrict__ tw) {
+  using C = AxisCfg<N, W>;
+  extern __shared__ float2 sm[];
+  int ncol = HP / W;
+  int o = blockIdx.x / ncol, c0 = (blockIdx.x % ncol) * W;
+  float2* f = base + (int64_t)blockIdx.y * fs;
+  for (int e = threadIdx.x; e < N * W; e += C::THREADS) {
+    int n = e / W, w = e % W;
+    sm[w * C::LS + spad(n)] = f[tile_elem<AXIS>(N, HP, o, c0, n, w)];
+  }
+  __syncthreads();
+  tile_fft<N, W, SIGN>(sm, tw);
+  __syncthreads();
+  for (int e = threadIdx.x; e < N * W; e += C::THREADS) {
+    int n = e / W, w = e % W;
+    f[tile_elem<AXIS>(N, HP, o, c0, n, w)] = sm[w * C::LS + spad(n)];
+  }
+}
+
+// In-place forward y pass over the active slots r = r_of_slot[blockIdx.y].
+template <int N, int W>
+__global__ void __launch_bounds__(AxisCfg<N, W>::THREADS) k_axis_slots(float2* base, int64_t fs, int HP,
+                                                                        const float2* __restrict__ tw,
+                                                                        const DevTerms* __restrict__ dt) {
+  using C = AxisCfg<N, W>;
+  extern __shared__ float2 sm[];
+  int ncol = HP / W;
+  int o = blockIdx.x / ncol, c0 = (blockIdx.x % ncol) * W;
+  float2* f = base + (int64_t)dt->tl.r_of_slot[blockIdx.y] * fs;
+  for (int e = threadIdx.x; e < N * W; e += C::THREADS) {
+    int n = e / W, w = e % W;
+    sm[w * C::LS + spad(n)] = f[tile_elem<1>(N, HP, o, c0, n, w)];
+  }
+  __syncthreads();
+  tile_fft<N, W, -1>(sm, tw);
+  __syncthreads();
+  for (int e = threadIdx.x; e < N * W; e += C::THREADS) {
+    int n = e / W, w = e % W;
+    f[tile_elem<1>(N, HP, o, c0, n, w)] = sm[w * C::LS + spad(n)];
+  }
+}
+
+// First modal pass: field p = blockIdx.y gets the inverse x transform of
+// q_p(k) phi(k).  phi is read once per tile per p (the M reads of one tile
+// follow each other and hit L2).
+template <int N, int W>
+__global__ void __launch_bounds__(AxisCfg<N, W>::THREADS) k_modal_xinv(ModalArgs a, const float2* __restrict__ phi,
+                                                                        float2* work, int64_t fs, int HP,
+                                                                        const float2* __restrict__ tw) {
+  using C = AxisCfg<N, W>;
+  extern __shared__ float2 sm[];
+  int ncol = HP / W;
+  int tile = blockIdx.x / a.M, p = blockIdx.x % a.M;
+  int o = tile / ncol, c0 = (tile % ncol) * W;
+  const int ky = sidx(o, N);
+  for (int e = threadIdx.x; e < N * W; e += C::THREADS) {
+    int n = e / W, w = e % W;
+    int kz = c0 + w;
+    float2 v = make_float2(0.f, 0.f);
+    if (kz <= N / 2) {
+      KCell c = kcell(a, sidx(n, N), ky, kz);
+      if (c.keep) {
+        float q = mode_in(a, p, c);
+        float2 ph = phi[tile_elem<0>(N, HP, o, c0, n, w)];
+        v = make_float2(ph.x * q, ph.y * q);
+      }
+    }
+    sm[w * C::LS + spad(n)] = v;
+  }
+  __syncthreads();
+  tile_fft<N, W, +1>(sm, tw);
+  __syncthreads();
+  float2* f = work + (int64_t)p * fs;
+  for (int e = threadIdx.x; e < N * W; e += C::THREADS) {
+    int n = e / W, w = e % W;
+    f[tile_elem<0>(N, HP, o, c0, n, w)] = sm[w * C::LS + spad(n)];
+  }
+}
+
+// Last modal pass: for each active r, forward x transform of slot r, times
+// rho_r(k), summed (Neumaier-compensated) over r; then
+// phi <- phi + fnl_n3 * acc, DC = 0 (main.c:1101-1126).
+template <int N, int W>
+__global__ void __launch_bounds__(AxisCfg<N, W>::THREADS) k_modal_xacc(ModalArgs a, float2* phi, const float2* work,
+                                                                        int64_t fs, int HP, float fnl_n3,
+                                                                        const float2* __restrict__ tw,
+                                                                        const DevTerms* __restrict__ dt) {
+  using C = AxisCfg<N, W>;
+  extern __shared__ float2 sm[];
+  float2* acc = sm + W * C::LS;
+  float2* cmp = acc + W * C::LS;
+  int ncol = HP / W;
+  int o = blockIdx.x / ncol, c0 = (blockIdx.x % ncol) * W;
+  const int ky = sidx(o, N);
+  for (int e = threadIdx.x; e < N * W; e += C::THREADS) {
+    int n = e / W, w = e % W;
+    acc[w * C::LS + spad(n)] = make_float2(0.f, 0.f);
+    cmp[w * C::LS + spad(n)] = make_float2(0.f, 0.f);
+  }
+  const int nr = dt->tl.nr;
+  for (int sl = 0; sl < nr; ++sl) {
+    int r = dt->tl.r_of_slot[sl];
+    const float2* f = work + (int64_t)r * fs;
+    __syncthreads();
+    for (int e = threadIdx.x; e < N * W; e += C::THREADS) {
+      int n = e / W, w = e % W;
+      sm[w * C::LS + spad(n)] = f[tile_elem<0>(N, HP, o, c0, n, w)];
+    }
+    __syncthreads();
+    tile_fft<N, W, -1>(sm, tw);
+    __syncthreads();
+    for (int e = threadIdx.x; e < N * W; e += C::THREADS) {
+      int n = e / W, w = e % W;
+      int kz = c0 + w;
+      if (kz > N / 2) continue;
+      KCell c = kcell(a, sidx(n, N), ky, kz);
+      if (!c.keep) continue;
+      float rho = mode_out(a, r, c);
+      float2 v = sm[w * C::LS + spad(n)];
+      int idx = w * C::LS + spad(n);
+      float2 s0 = acc[idx], cc = cmp[idx];
+      float tx = v.x * rho, ty = v.y * rho;
+      float sx = s0.x + tx, sy = s0.y + ty;
+      cc.x += (fabsf(s0.x) >= fabsf(tx)) ? (s0.x - sx) + tx : (tx - sx) + s0.x;
+      cc.y += (fabsf(s0.y) >= fabsf(ty)) ? (s0.y - sy) + ty : (ty - sy) + s0.y;
+      acc[idx] = make_float2(sx, sy);
+      cmp[idx] = cc;
+    }
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < N * W; e += C::THREADS) {
+    int n = e / W, w = e % W;
+    int kz = c0 + w;
+    if (kz > N / 2) continue;
+    int64_t gi = tile_elem<0>(N, HP, o, c0, n, w);
+    int idx = w * C::LS + spad(n);
+    float2 s0 = acc[idx], cc = cmp[idx];
+    float2 ph = phi[gi];
+    ph.x += fnl_n3 * (s0.x + cc.x);
+    ph.y += fnl_n3 * (s0.y + cc.y);
+    if (n == 0 && o == 0 && kz == 0) ph = make_float2(0.f, 0.f);
+    phi[gi] = ph;
+  }
+}
+
+// ----------------------------------------------------------- row passes
+// Row layout: complex row X[0..N/2] at field + (x N + y) HP; the real row
+// x[0..N-1] occupies the same bytes (float2 z_n = (x_{2n}, x_{2n+1})).
+template <int N>
+struct RowCfg {
+  static constexpr int H = N / 2;             // complex FFT length
+  static constexpr int T = lanes_for(H);
+  static constexpr int LPW = 32 / T;
+  static constexpr int LS = spad_len(H);
+};
+
+// load X_k (k = 0..N/2) of a row and form Z_k = E_k + i O_k for the
+// inverse half-length FFT (FFTW c2r semantics: Im X_0, Im X_{N/2} dropped)
+template <int N>
+__device__ __forceinline__ void row_c2r_pre(const float2* __restrict__ X, float2* line, int t, int T,
+                                            const float2* __restrict__ twN) {
+  constexpr int H = N / 2;
+  for (int k = t; k <= H / 2; k += T) {
+    int k2 = H - k;
+    float2 a = X[k], b = X[k2];
+    if (k == 0) {
+      a.y = 0.f;
+      b.y = 0.f;
+    }
+    // E_k = X_k + conj(X_{H-k}); O_k = (X_k - conj(X_{H-k})) e^{+2 pi i k / N}
+    float2 w = __ldg(twN + k);
+    w.y = -w.y;
+    float2 e = make_float2(a.x + b.x, a.y - b.y);
+    float2 d = make_float2(a.x - b.x, a.y + b.y);
+    float2 o = cmul(d, w);
+    line[spad(k)] = make_float2(e.x - o.y, e.y + o.x);
+    if (k2 != k && k2 < H) {
+      // Z_{H-k}: E = X_{H-k} + conj(X_k), O = (X_{H-k} - conj(X_k)) e^{+2 pi i (H-k)/N}
+      float2 w2 = __ldg(twN + k2);
+      w2.y = -w2.y;
+      float2 e2 = make_float2(b.x + a.x, b.y - a.y);
+      float2 d2 = make_float2(b.x - a.x, b.y + a.y);
+      float2 o2 = cmul(d2, w2);
+      line[spad(k2)] = make_float2(e2.x - o2.y, e2.y + o2.x);
+    }
+  }
+}
+
+// after the forward half-length FFT of z_n = (x_{2n}, x_{2n+1}) in `line`,
+// write X_k = (Z_k + conj Z_{H-k})/2 - i e^{-2 pi i k/N} (Z_k - conj Z_{H-k})/2
+template <int N>
+__device__ __forceinline__ void row_r2c_post(const float2* line, float2* __restrict__ X, int t, int T,
+                                             const float2* __restrict__ twN) {
+  constexpr int H = N / 2;
+  for (int k = t; k <= H; k += T) {
+    float2 z = line[spad(k % H)], zc = line[spad((H - k) % H)];
+    zc.y = -zc.y;
+    float2 e = make_float2(0.5f * (z.x + zc.x), 0.5f * (z.y + zc.y));
+    float2 d = make_float2(0.5f * (z.x - zc.x), 0.5f * (z.y - zc.y));
+    float2 w = (k < H) ? __ldg(twN + k) : make_float2(-1.f, 0.f);
+    float2 od = cmul(d, w);  // e^{-2 pi i k/N} d
+    X[k] = make_float2(e.x + od.y, e.y - od.x);  // e - i od
+  }
+}
+
+// Generic row kernel.  For each row (blockIdx.x = x*N + y): c2r of `nin`
+// input fields (slots in_slot[]), a per-position combine step Op, r2c of
+// `nout` output lines into slots out_slot[].  One warp per line at a time.
+template <int N, class Op>
+__global__ void __launch_bounds__(256) k_rows(Op op, float2* work, int64_t fs, int HP,
+                                              const float2* __restrict__ twN, const float2* __restrict__ twH) {
+  using C = RowCfg<N>;
+  constexpr int H = C::H;
+  extern __shared__ float2 sm[];
+  int64_t row = blockIdx.x;
+  int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int nwarps = blockDim.x >> 5;
+  int sub = lane / C::T, t = lane % C::T;
+  // phase 1: inverse transforms
+  for (int l0 = warp * C::LPW; l0 < op.nin(); l0 += nwarps * C::LPW) {
+    int l = l0 + sub;
+    bool act = l < op.nin() && sub < C::LPW;
+    float2* line = sm + (act ? l : 0) * C::LS;
+    if (act) row_c2r_pre<N>(work + (int64_t)op.in_slot(l) * fs + row * HP, line, t, C::T, twN);
+    __syncwarp();
+    line_fft_smem<H, C::T, +1>(line, t, twH, act);
+  }
+  __syncthreads();
+  // phase 2: per position combine (in place in the line buffers)
+  for (int n = threadIdx.x; n < H; n += blockDim.x) op.combine(sm, n, C::LS);
+  __syncthreads();
+  // phase 3: forward transforms of the output lines
+  for (int l0 = warp * C::LPW; l0 < op.nout(); l0 += nwarps * C::LPW) {
+    int l = l0 + sub;
+    bool act = l < op.nout() && sub < C::LPW;
+    float2* line = sm + (act ? op.out_line(l) : 0) * C::LS;
+    line_fft_smem<H, C::T, -1>(line, t, twH, act);
+    if (act) row_r2c_post<N>(line, work + (int64_t)op.out_slot(l) * fs + row * HP, t, C::T, twN);
+    __syncwarp();
+  }
+}
+
+// modal products: lines 0..M-1 hold f_p; line r is overwritten by g_r
+struct ModalRowOp {
+  int M;
+  const DevTerms* dt;
+  __device__ int nin() const { return M; }
+  __device__ int in_slot(int l) const { return l; }
+  __device__ int nout() const { return dt->tl.nr; }
+  __device__ int out_line(int l) const { return dt->tl.r_of_slot[l]; }
+  __device__ int out_slot(int l) const { return dt->tl.r_of_slot[l]; }
+  __device__ void combine(float2* sm, int n, int LS) const {
+    float2 g[kMaxModes];
+    const int nr = dt->tl.nr;
+#pragma unroll
+    for (int s = 0; s < kMaxModes; ++s) {
+      if (s < nr) {
+        float2 acc = make_float2(0.f, 0.f);
+        const int tb = dt->tl.begin[s], te = dt->tl.begin[s + 1];
+        for (int t = tb; t < te; ++t) {
+          Term tm = dt->t[t];
+          float2 fp = sm[tm.p * LS + spad(n)], fq = sm[tm.q * LS + spad(n)];
+          acc.x += tm.c * fp.x * fq.x;
+          acc.y += tm.c * fp.y * fq.y;
+        }
+        g[s] = acc;
+      }
+    }
+#pragma unroll
+    for (int s = 0; s < kMaxModes; ++s)
+      if (s < nr) sm[dt->tl.r_of_slot[s] * LS + spad(n)] = g[s];
+  }
+};
+
+// 2LPT source (main.c:1284-1294): lines 0..5 hold d00 d01 d02 d11 d12 d22;
+// the source goes to line 0, written to slot `out`.
+struct SourceRowOp {
+  int out;
+  __device__ int nin() const { return 6; }
+  __device__ int in_slot(int l) const { return l; }
+  __device__ int nout() const { return 1; }
+  __device__ int out_line(int) const { return 0; }
+  __device__ int out_slot(int) const { return out; }
+  __device__ void combine(float2* sm, int n, int LS) const {
+    float2 d[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) d[i] = sm[i * LS + spad(n)];
+    float2 s;
+    s.x = d[0].x * (d[3].x + d[5].x) + d[3].x * d[5].x - d[1].x * d[1].x - d[2].x * d[2].x - d[4].x * d[4].x;
+    s.y = d[0].y * (d[3].y + d[5].y) + d[3].y * d[5].y - d[1].y * d[1].y - d[2].y * d[2].y - d[4].y * d[4].y;
+    sm[spad(n)] = s;
+  }
+};
+
+// plain c2r of one field per blockIdx.y (slot = first + blockIdx.y)
+template <int N>
+__global__ void __launch_bounds__(256) k_rows_c2r(float2* work, int64_t fs, int HP, int first, int64_t nrows,
+                                                  const float2* __restrict__ twN, const float2* __restrict__ twH) {
+  using C = RowCfg<N>;
+  constexpr int H = C::H;
+  extern __shared__ float2 sm[];
+  int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int sub = lane / C::T, t = lane % C::T;
+  int lines_per_block = (blockDim.x >> 5) * C::LPW;
+  int64_t row = (int64_t)blockIdx.x * lines_per_block + warp * C::LPW + sub;
+  bool act = row < nrows && sub < C::LPW;
+  float2* line = sm + (warp * C::LPW + sub) * C::LS;
+  float2* f = work + (int64_t)(first + blockIdx.y) * fs + (act ? row : 0) * HP;
+  if (act) row_c2r_pre<N>(f, line, t, C::T, twN);
+  __syncwarp();
+  line_fft_smem<H, C::T, +1>(line, t, twH, act);
+  if (act)
+    for (int n = t; n < H; n += C::T) f[n] = line[spad(n)];
+}
+
+// ----------------------------------------------------------- 2LPT passes
+struct LptArgs {
+  ModalArgs m;      // grid and k helpers
+  float inv_Dbeta;  // 1 / (Dplus Beta)
+  const float* twb; // per n^2: T(k) / (Dplus Beta)
+  float box_over_2n;
+};
+
+__device__ __forceinline__ float sincf(float x) { return x == 0.f ? 1.f : sinf(x) / x; }
+
+// Hessian c = blockIdx.x % 6 of the ZA displacement (main.c:1238-1277):
+// d_ab = -k_a k_b T/(D Beta) phi, then the inverse x transform.
+template <int N, int W>
+__global__ void __launch_bounds__(AxisCfg<N, W>::THREADS) k_lpt_xinv_hess(LptArgs a, const float2* __restrict__ phi,
+                                                                           float2* work, int64_t fs, int HP,
+                                                                           const float2* __restrict__ tw) {
+  using C = AxisCfg<N, W>;
+  extern __shared__ float2 sm[];
+  const int pa[6] = {0, 0, 0, 1, 1, 2}, pb[6] = {0, 1, 2, 1, 2, 2};
+  int ncol = HP / W;
+  int tile = blockIdx.x / 6, comp = blockIdx.x % 6;
+  int o = tile / ncol, c0 = (tile % ncol) * W;
+  const int ky = sidx(o, N);
+  const float kF = a.m.g.kF;
+  for (int e = threadIdx.x; e < N * W; e += C::THREADS) {
+    int n = e / W, w = e % W;
+    int kz = c0 + w;
+    float2 v = make_float2(0.f, 0.f);
+    if (kz <= N / 2) {
+      int kv[3] = {sidx(n, N), ky, kz};
+      int n2 = kv[0] * kv[0] + kv[1] * kv[1] + kv[2] * kv[2];
+      float t = __ldg(a.twb + n2);
+      float f = -(kF * kv[pa[comp]]) * (kF * kv[pb[comp]]) * t;
+      float2 ph = phi[tile_elem<0>(N, HP, o, c0, n, w)];
+      v = make_float2(ph.x * f, ph.y * f);
+    }
+    sm[w * C::LS + spad(n)] = v;
+  }
+  __syncthreads();
+  tile_fft<N, W, +1>(sm, tw);
+  __syncthreads();
+  float2* f = work + (int64_t)comp * fs;
+  for (int e = threadIdx.x; e < N * W; e += C::THREADS) {
+    int n = e / W, w = e % W;
+    f[tile_elem<0>(N, HP, o, c0, n, w)] = sm[w * C::LS + spad(n)];
+  }
+}
+
+// Displacement spectra and the inverse x transform (main.c:1180-1216,
+// 1311-1368): comp 0..2 = ZA psi1_a = i k_a T/(D Beta) phi * smth; comp 3..5
+// = psi2_a = -i k_a / k^2 S * smth with S from the forward x transform of
+// the source slot.  Output slots 0..5.
+template <int N, int W>
+__global__ void __launch_bounds__(AxisCfg<N, W>::THREADS) k_lpt_xmid(LptArgs a, const float2* __restrict__ phi,
+                                                                      float2* work, int64_t fs, int HP, int src_slot,
+                                                                      const float2* __restrict__ tw) {
+  using C = AxisCfg<N, W>;
+  extern __shared__ float2 sm[];
+  int ncol = HP / W;
+  int tile = blockIdx.x / 6, comp = blockIdx.x % 6;
+  int o = tile / ncol, c0 = (tile % ncol) * W;
+  const int ky = sidx(o, N);
+  const float kF = a.m.g.kF;
+  const int ax = comp % 3;
+  if (comp >= 3) {
+    const float2* s = work + (int64_t)src_slot * fs;
+    for (int e = threadIdx.x; e < N * W; e += C::THREADS) {
+      int n = e / W, w = e % W;
+      sm[w * C::LS + spad(n)] = s[tile_elem<0>(N, HP, o, c0, n, w)];
+    }
+    __syncthreads();
+    tile_fft<N, W, -1>(sm, tw);
+    __syncthreads();
+  }
+  for (int e = threadIdx.x; e < N * W; e += C::THREADS) {
+    int n = e / W, w = e % W;
+    int kz = c0 + w;
+    float2 v = make_float2(0.f, 0.f);
+    if (kz <= N / 2) {
+      int kv[3] = {sidx(n, N), ky, kz};
+      int n2 = kv[0] * kv[0] + kv[1] * kv[1] + kv[2] * kv[2];
+      float fx = sincf(kF * kv[0] * a.box_over_2n), fy = sincf(kF * kv[1] * a.box_over_2n),
+            fz = sincf(kF * kv[2] * a.box_over_2n);
+      float ff = 1.f / (fx * fy * fz);
+      float smth = ff * ff;
+      float ka = kF * kv[ax];
+      if (comp < 3) {
+        float2 ph = phi[tile_elem<0>(N, HP, o, c0, n, w)];
+        float f = ka * __ldg(a.twb + n2) * smth;
+        v = make_float2(-f * ph.y, f * ph.x);
+      } else if (n2 > 0) {
+        float2 s = sm[w * C::LS + spad(n)];
+        float k2 = kF * kF * (float)n2;
+        float f = ka / k2 * smth;
+        v = make_float2(f * s.y, -f * s.x);
+      }
+    }
+    sm[w * C::LS + spad(n)] = v;
+  }
+  __syncthreads();
+  tile_fft<N, W, +1>(sm, tw);
+  __syncthreads();
+  float2* f = work + (int64_t)comp * fs;
+  for (int e = threadIdx.x; e < N * W; e += C::THREADS) {
+    int n = e / W, w = e % W;
+    f[tile_elem<0>(N, HP, o, c0, n, w)] = sm[w * C::LS + spad(n)];
+  }
+}
+
+// ----------------------------------------------------------- read-out
+// Trilinear read-out (main.c:1440-1516).  Fields: slots 0..5 of `work` as
+// real rows (float, row stride 2 HP); psi2 slots hold N^3 x the 2LPT field.
+struct ReadArgs {
+  int N, HP;
+  int64_t fs;           // field stride in floats
+  float box, inv_n3, vp1, vp2;
+  double n_over_box;
+};
+
+__device__ __forceinline__ void readout_one(const ReadArgs& a, const float* __restrict__ F, float px, float py,
+                                            float pz, float* op, float* ov) {
+  const int N = a.N;
+  float p[3] = {px, py, pz};
+  int ii[3], jj[3];
+  float fr[3];
+  for (int d = 0; d < 3; ++d) {
+    double u = (double)p[d] * a.n_over_box;
+    if (!(u >= 0.0)) u = 0.0;  // also catches NaN: the cell index stays inside the grid
+    if (u > (double)N) u = (double)N;
+    int i = (int)u;
+    if (i >= N) i = N - 1;
+    if (i < 0) i = 0;
+    fr[d] = (float)(u - (double)i);
+    ii[d] = i;
+    jj[d] = (i + 1 == N) ? 0 : i + 1;
+  }
+  const int64_t rs = 2 * (int64_t)a.HP;
+  int64_t o000 = ((int64_t)ii[0] * N + ii[1]) * rs, o010 = ((int64_t)ii[0] * N + jj[1]) * rs;
+  int64_t o100 = ((int64_t)jj[0] * N + ii[1]) * rs, o110 = ((int64_t)jj[0] * N + jj[1]) * rs;
+  float u = fr[0], v = fr[1], w = fr[2];
+  float f1 = (1 - u) * (1 - v) * (1 - w), f2 = (1 - u) * (1 - v) * w, f3 = (1 - u) * v * (1 - w),
+        f4 = (1 - u) * v * w, f5 = u * (1 - v) * (1 - w), f6 = u * (1 - v) * w, f7 = u * v * (1 - w),
+        f8 = u * v * w;
+  int k0 = ii[2], k1 = jj[2];
+  for (int ax = 0; ax < 3; ++ax) {
+    const float* d1 = F + ax * a.fs;
+    const float* d2 = F + (3 + ax) * a.fs;
+    float dis = d1[o000 + k0] * f1 + d1[o000 + k1] * f2 + d1[o010 + k0] * f3 + d1[o010 + k1] * f4 +
+                d1[o100 + k0] * f5 + d1[o100 + k1] * f6 + d1[o110 + k0] * f7 + d1[o110 + k1] * f8;
+    float dis2 = d2[o000 + k0] * f1 + d2[o000 + k1] * f2 + d2[o010 + k0] * f3 + d2[o010 + k1] * f4 +
+                 d2[o100 + k0] * f5 + d2[o100 + k1] * f6 + d2[o110 + k0] * f7 + d2[o110 + k1] * f8;
+    dis2 *= a.inv_n3;
+    float d = dis - (3.f / 7.f) * dis2;
+    float x = p[ax] + d;
+    if (x < 0.f) x += a.box;
+    if (x >= a.box) x -= a.box;
+    op[ax] = x;
+    ov[ax] = dis * a.vp1 - (3.f / 7.f) * dis2 * a.vp2;
+  }
+}
+
+__global__ void k_readout(ReadArgs a, const float* __restrict__ F, const float* __restrict__ lagr, int64_t np,
+                          float* pos, float* vel) {
+  int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= np) return;
+  float op[3], ov[3];
+  readout_one(a, F, lagr[3 * n], lagr[3 * n + 1], lagr[3 * n + 2], op, ov);
+  for (int d = 0; d < 3; ++d) {
+    pos[3 * n + d] = op[d];
+    vel[3 * n + d] = ov[d];
+  }
+}
+
+// Lagrangian position of particle n from a glass tiled tile^3 times
+// (read_glass.c:129-214): FP64 with unfused operations, rounded to float.
+__global__ void k_readout_glass(ReadArgs a, const float* __restrict__ F, const float* __restrict__ glass,
+                                int64_t nglass, double glass_box, int tile, double box_over_tile, float* pos,
+                                float* vel, int* ids) {
+  int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t np = nglass * tile * tile * tile;
+  if (n >= np) return;
+  int64_t gi = n % nglass, t = n / nglass;
+  int ti = (int)(t / ((int64_t)tile * tile)), tj = (int)((t / tile) % tile), tk = (int)(t % tile);
+  int tt[3] = {ti, tj, tk};
+  float lp[3];
+  for (int d = 0; d < 3; ++d) {
+    double x = __dadd_rn(__dmul_rn(__ddiv_rn((double)glass[3 * gi + d], glass_box), box_over_tile),
+                         __dmul_rn((double)tt[d], box_over_tile));
+    lp[d] = (float)x;
+  }
+  float op[3], ov[3];
+  readout_one(a, F, lp[0], lp[1], lp[2], op, ov);
+  for (int d = 0; d < 3; ++d) {
+    pos[3 * n + d] = op[d];
+    vel[3 * n + d] = ov[d];
+  }
+  if (ids) ids[n] = (int)(n + 1);
+}
+
+// ----------------------------------------------------------- host side
+template <int N>
+struct Launch {
+  static constexpr int W = 8;
+  static int configure(Plan* p) {
+    using A = AxisCfg<N, W>;
+    size_t sm_axis = A::SMEM, sm_acc = 3 * A::SMEM;
+    AAR_CUDA_TRY(p, cudaFuncSetAttribute(k_axis_inplace<N, W, 0, +1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_axis));
+    AAR_CUDA_TRY(p, cudaFuncSetAttribute(k_axis_inplace<N, W, 1, +1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_axis));
+    AAR_CUDA_TRY(p, cudaFuncSetAttribute(k_axis_inplace<N, W, 0, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_axis));
+    AAR_CUDA_TRY(p, cudaFuncSetAttribute(k_axis_inplace<N, W, 1, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_axis));
+    AAR_CUDA_TRY(p, cudaFuncSetAttribute(k_modal_xinv<N, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_axis));
+    AAR_CUDA_TRY(p, cudaFuncSetAttribute(k_axis_slots<N, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_axis));
+    AAR_CUDA_TRY(p, cudaFuncSetAttribute(k_modal_xacc<N, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_acc));
+    AAR_CUDA_TRY(p, cudaFuncSetAttribute(k_lpt_xinv_hess<N, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_axis));
+    AAR_CUDA_TRY(p, cudaFuncSetAttribute(k_lpt_xmid<N, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_axis));
+    size_t sm_rows = sizeof(float2) * (size_t)(kMaxModes + 1) * RowCfg<N>::LS;
+    AAR_CUDA_TRY(p, cudaFuncSetAttribute(k_rows<N, ModalRowOp>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_rows));
+    AAR_CUDA_TRY(p, cudaFuncSetAttribute(k_rows<N, SourceRowOp>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_rows));
+    return AAR_OK;
+  }
+  static int ypass(Plan* p, int nf, int sign, cudaStream_t st, const char* name) {
+    using A = AxisCfg<N, W>;
+    dim3 grid((unsigned)(N * (p->HP / W)), (unsigned)nf);
+    int64_t fs = (int64_t)N * N * p->HP;
+    if (sign > 0)
+      { ProfScope ps_(p, name, st);
+      k_axis_inplace<N, W, 1, +1><<<grid, A::THREADS, A::SMEM, st>>>(p->d_work, fs, p->HP, p->d_twN);
+      }
+    else
+      { ProfScope ps_(p, name, st);
+      k_axis_inplace<N, W, 1, -1><<<grid, A::THREADS, A::SMEM, st>>>(p->d_work, fs, p->HP, p->d_twN);
+      }
+    AAR_CUDA_TRY(p, cudaGetLastError());
+    p->last_launches += 1;
+    return AAR_OK;
+  }
+  static int modal(Plan* p, const ModalArgs& a, cudaStream_t st) {
+    using A = AxisCfg<N, W>;
+    int64_t fs = (int64_t)N * N * p->HP;
+    unsigned tiles = (unsigned)(N * (p->HP / W));
+    { ProfScope ps_(p, "modal_xinv", st);
+    k_modal_xinv<N, W><<<tiles * a.M, A::THREADS, A::SMEM, st>>>(a, p->d_phik, p->d_work, fs, p->HP, p->d_twN);
+    }
+    AAR_CUDA_TRY(p, cudaGetLastError());
+    p->last_launches += 1;
+    int rc = ypass(p, a.M, +1, st, "modal_ypass_inv");
+    if (rc) return rc;
+    size_t sm_rows = sizeof(float2) * (size_t)(a.M + 1) * RowCfg<N>::LS;
+    ModalRowOp op{a.M, (const DevTerms*)p->d_terms};
+    { ProfScope ps_(p, "modal_rows", st);
+    k_rows<N, ModalRowOp><<<(unsigned)((int64_t)N * N), 256, sm_rows, st>>>(op, p->d_work, fs, p->HP, p->d_twN, p->d_twH);
+    }
+    AAR_CUDA_TRY(p, cudaGetLastError());
+    p->last_launches += 1;
+    // forward y on the active slots only
+    {
+      dim3 grid((unsigned)(N * (p->HP / W)), (unsigned)p->nr_active);
+      { ProfScope ps_(p, "modal_ypass_fwd", st);
+      k_axis_slots<N, W><<<grid, A::THREADS, A::SMEM, st>>>(p->d_work, fs, p->HP, p->d_twN,
+                                                             (const DevTerms*)p->d_terms);
+      }
+      AAR_CUDA_TRY(p, cudaGetLastError());
+      p->last_launches += 1;
+    }
+    float fnl_n3 = (float)(p->prm.fnl / ((double)N * N * N));
+    { ProfScope ps_(p, "modal_xacc", st);
+    k_modal_xacc<N, W><<<tiles, A::THREADS, 3 * A::SMEM, st>>>(a, p->d_phik, p->d_work, fs, p->HP, fnl_n3, p->d_twN,
+                                                                  (const DevTerms*)p->d_terms);
+    }
+    AAR_CUDA_TRY(p, cudaGetLastError());
+    p->last_launches += 1;
+    return AAR_OK;
+  }
+  static int lpt(Plan* p, const LptArgs& a, cudaStream_t st) {
+    using A = AxisCfg<N, W>;
+    int64_t fs = (int64_t)N * N * p->HP;
+    unsigned tiles = (unsigned)(N * (p->HP / W));
+    { ProfScope ps_(p, "lpt_xinv_hess", st);
+    k_lpt_xinv_hess<N, W><<<tiles * 6, A::THREADS, A::SMEM, st>>>(a, p->d_phik, p->d_work, fs, p->HP, p->d_twN);
+    }
+    AAR_CUDA_TRY(p, cudaGetLastError());
+    p->last_launches += 1;
+    int rc = ypass(p, 6, +1, st, "lpt_ypass_inv_hess");
+    if (rc) return rc;
+    size_t sm_rows = sizeof(float2) * (size_t)7 * RowCfg<N>::LS;
+    SourceRowOp op{6};
+    { ProfScope ps_(p, "lpt_rows_source", st);
+    k_rows<N, SourceRowOp><<<(unsigned)((int64_t)N * N), 256, sm_rows, st>>>(op, p->d_work, fs, p->HP, p->d_twN, p->d_twH);
+    }
+    AAR_CUDA_TRY(p, cudaGetLastError());
+    p->last_launches += 1;
+    // forward y of the source slot only
+    {
+      dim3 grid((unsigned)(N * (p->HP / W)), 1);
+      { ProfScope ps_(p, "lpt_ypass_fwd_source", st);
+      k_axis_inplace<N, W, 1, -1><<<grid, A::THREADS, A::SMEM, st>>>(p->d_work + 6 * fs, fs, p->HP, p->d_twN);
+      }
+      AAR_CUDA_TRY(p, cudaGetLastError());
+      p->last_launches += 1;
+    }
+    { ProfScope ps_(p, "lpt_xmid", st);
+    k_lpt_xmid<N, W><<<tiles * 6, A::THREADS, A::SMEM, st>>>(a, p->d_phik, p->d_work, fs, p->HP, 6, p->d_twN);
+    }
+    AAR_CUDA_TRY(p, cudaGetLastError());
+    p->last_launches += 1;
+    rc = ypass(p, 6, +1, st, "lpt_ypass_inv_disp");
+    if (rc) return rc;
+    using R = RowCfg<N>;
+    int lines_per_block = 8 * R::LPW;
+    int64_t nrows = (int64_t)N * N;
+    dim3 grid((unsigned)((nrows + lines_per_block - 1) / lines_per_block), 6);
+    { ProfScope ps_(p, "lpt_rows_c2r", st);
+    k_rows_c2r<N><<<grid, 256, sizeof(float2) * lines_per_block * R::LS, st>>>(p->d_work, fs, p->HP, 0, nrows,
+                                                                              p->d_twN, p->d_twH);
+    }
+    AAR_CUDA_TRY(p, cudaGetLastError());
+    p->last_launches += 1;
+    return AAR_OK;
+  }
+};
+
+template <class F>
+static int dispatch_n(int N, F&& f) {
+  switch (N) {
+    case 16: return f(std::integral_constant<int, 16>{});
+    case 32: return f(std::integral_constant<int, 32>{});
+    case 64: return f(std::integral_constant<int, 64>{});
+    case 128: return f(std::integral_constant<int, 128>{});
+    case 256: return f(std::integral_constant<int, 256>{});
+    case 512: return f(std::integral_constant<int, 512>{});
+    case 1024: return f(std::integral_constant<int, 1024>{});
+    default: return AAR_ERR_ARG;
+  }
+}
+
+static ModalArgs modal_args(Plan* p) {
+  ModalArgs a;
+  a.g = p->grid;
+  double ns = p->prm.primordial_index;
+  double s = (4 - ns) / 3;
+  double kmin = 2 * kPi / p->prm.box, kmax = 2 * kPi / p->prm.box * p->prm.nmax;
+  a.s = (float)s;
+  a.ns = (float)ns;
+  a.kmin_s = (float)pow(kmin, s);
+  a.inv_dks = (float)(1.0 / (pow(kmax, s) - pow(kmin, s)));
+  a.ln_kF = (float)log(2 * kPi / p->prm.box);
+  a.M = p->M;
+  for (int i = 0; i < 32; ++i) a.x0[i] = i < p->M ? (float)p->x0[i] : 0.f;
+  return a;
+}
+
+// Build the regrouped term list: sorted triples p <= q <= r with alpha != 0
+// contribute a f_p f_q to g_r (main.c:833-867); the counter-terms of
+// main.c:1045-1050 add -a012 t012 f_0 f_1 to g_2 and +a012 t012 f_0 f_2 to g_1.
+static int build_terms(Plan* p) {
+  int M = p->M;
+  auto A = [&](int i, int j, int k) { return p->alpha[((size_t)i * M + j) * M + k]; };
+  std::vector<std::vector<Term>> by_r(M);
+  for (int i = 0; i < M; ++i)
+    for (int j = i; j < M; ++j)
+      for (int k = j; k < M; ++k)
+        if (A(i, j, k) != 0) by_r[k].push_back(Term{i, j, k, (float)A(i, j, k)});
+  if (M > 2 && A(0, 1, 2) != 0) {
+    double t012 = -A(1, 1, 1) / A(0, 1, 2);
+    double c = A(0, 1, 2) * t012;
+    by_r[2].push_back(Term{0, 1, 2, (float)(-c)});
+    by_r[1].push_back(Term{0, 2, 1, (float)(c)});
+  }
+  TermList tl{};
+  std::vector<Term> flat;
+  int nr = 0;
+  for (int r = 0; r < M; ++r) {
+    if (by_r[r].empty()) continue;
+    tl.r_of_slot[nr] = r;
+    tl.begin[nr] = (int)flat.size();
+    for (auto& t : by_r[r]) flat.push_back(t);
+    ++nr;
+  }
+  tl.begin[nr] = (int)flat.size();
+  tl.nr = nr;
+  tl.nterms = (int)flat.size();
+  if (tl.nterms > kMaxTerms) return set_err(p, "too many alpha terms"), AAR_ERR_ARG;
+  DevTerms* dt = (DevTerms*)p->d_terms;
+  AAR_CUDA_TRY(p, cudaMemcpy(&dt->tl, &tl, sizeof(tl), cudaMemcpyHostToDevice));
+  if (!flat.empty()) AAR_CUDA_TRY(p, cudaMemcpy(dt->t, flat.data(), sizeof(Term) * flat.size(), cudaMemcpyHostToDevice));
+  p->nterms = tl.nterms;
+  p->nr_active = nr;
+  return AAR_OK;
+}
+
+int fused_prepare(Plan* p) {
+  if (p->M > kMaxModes) return set_err(p, "N_modes above 32 is not supported"), AAR_ERR_ARG;
+  int rc = build_terms(p);
+  if (rc) return rc;
+  return dispatch_n(p->N, [&](auto nc) { return Launch<decltype(nc)::value>::configure(p); });
+}
+
+int fused_modal(Plan* p, cudaStream_t st) {
+  ModalArgs a = modal_args(p);
+  if (p->nr_active == 0 || p->prm.fnl == 0) return AAR_OK;  // no non-Gaussian term at all
+  return dispatch_n(p->N, [&](auto nc) { return Launch<decltype(nc)::value>::modal(p, a, st); });
+}
+
+int fused_lpt(Plan* p, cudaStream_t st) {
+  LptArgs a;
+  a.m = modal_args(p);
+  a.inv_Dbeta = (float)(1.0 / (p->Dplus * p->Beta));
+  a.twb = p->d_twb;
+  a.box_over_2n = (float)(p->prm.box / 2 / p->N);
+  return dispatch_n(p->N, [&](auto nc) { return Launch<decltype(nc)::value>::lpt(p, a, st); });
+}
+
+static ReadArgs read_args(Plan* p) {
+  ReadArgs a;
+  a.N = p->N;
+  a.HP = p->HP;
+  a.fs = 2 * (int64_t)p->N * p->N * p->HP;
+  a.box = (float)p->prm.box;
+  unsigned int n3 = (unsigned int)p->N * (unsigned int)p->N * (unsigned int)p->N;
+  a.inv_n3 = (float)(1.0 / (double)(float)n3);
+  a.vp1 = (float)p->vel_prefac;
+  a.vp2 = (float)p->vel_prefac2;
+  a.n_over_box = (double)p->N / p->prm.box;
+  return a;
+}
+
+int fused_readout(Plan* p, const float* d_lagr, int64_t npart, float* d_pos, float* d_vel, cudaStream_t st) {
+  if (npart == 0) return AAR_OK;
+  int bs = 256;
+  { ProfScope ps_(p, "readout", st);
+  k_readout<<<(unsigned)((npart + bs - 1) / bs), bs, 0, st>>>(read_args(p), (const float*)p->d_work, d_lagr, npart,
+                                                               d_pos, d_vel);
+  }
+  AAR_CUDA_TRY(p, cudaGetLastError());
+  p->last_launches += 1;
+  return AAR_OK;
+}
+
+int fused_readout_glass(Plan* p, const float* d_glass, int64_t nglass, double glass_box, int tile, float* d_pos,
+                        float* d_vel, int* d_ids, cudaStream_t st) {
+  int64_t np = nglass * tile * tile * tile;
+  if (np == 0) return AAR_OK;
+  int bs = 256;
+  { ProfScope ps_(p, "readout_glass", st);
+  k_readout_glass<<<(unsigned)((np + bs - 1) / bs), bs, 0, st>>>(read_args(p), (const float*)p->d_work, d_glass,
+                                                                  nglass, glass_box, tile, p->prm.box / tile, d_pos,
+                                                                  d_vel, d_ids);
+  }
+  AAR_CUDA_TRY(p, cudaGetLastError());
+  p->last_launches += 1;
+  return AAR_OK;
+}
+
+}  // namespace aar
+
+// ----------------------------------------------------------- standalone 3-D transforms
+namespace aar {
+
+template <int N>
+__global__ void __launch_bounds__(256) k_rows_r2c(float2* f, int HP, int64_t nrows, const float2* __restrict__ twN,
+                                                  const float2* __restrict__ twH) {
+  using C = RowCfg<N>;
+  constexpr int H = C::H;
+  extern __shared__ float2 sm[];
+  int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int sub = lane / C::T, t = lane % C::T;
+  int lines_per_block = (blockDim.x >> 5) * C::LPW;
+  int64_t row = (int64_t)blockIdx.x * lines_per_block + warp * C::LPW + sub;
+  bool act = row < nrows && sub < C::LPW;
+  float2* line = sm + (warp * C::LPW + sub) * C::LS;
+  float2* r = f + (act ? row : 0) * HP;
+  if (act)
+    for (int n = t; n < H; n += C::T) line[spad(n)] = r[n];
+  __syncwarp();
+  line_fft_smem<H, C::T, -1>(line, t, twH, act);
+  if (act) row_r2c_post<N>(line, r, t, C::T, twN);
+}
+
+template <int N>
+struct Xform {
+  static constexpr int W = 8;
+  static int c2r(Plan* p, float2* slot, cudaStream_t st) {
+    using A = AxisCfg<N, W>;
+    using R = RowCfg<N>;
+    dim3 grid((unsigned)(N * (p->HP / W)), 1);
+    { ProfScope ps_(p, "xform_axis", st);
+    k_axis_inplace<N, W, 0, +1><<<grid, A::THREADS, A::SMEM, st>>>(slot, 0, p->HP, p->d_twN);
+    }
+    { ProfScope ps_(p, "xform_axis", st);
+    k_axis_inplace<N, W, 1, +1><<<grid, A::THREADS, A::SMEM, st>>>(slot, 0, p->HP, p->d_twN);
+    }
+    int lpb = 8 * R::LPW;
+    int64_t nrows = (int64_t)N * N;
+    dim3 g2((unsigned)((nrows + lpb - 1) / lpb), 1);
+    { ProfScope ps_(p, "xform_rows", st);
+    k_rows_c2r<N><<<g2, 256, sizeof(float2) * lpb * R::LS, st>>>(slot, 0, p->HP, 0, nrows, p->d_twN, p->d_twH);
+    }
+    AAR_CUDA_TRY(p, cudaGetLastError());
+    p->last_launches += 3;
+    return AAR_OK;
+  }
+  static int r2c(Plan* p, float2* slot, cudaStream_t st) {
+    using A = AxisCfg<N, W>;
+    using R = RowCfg<N>;
+    int lpb = 8 * R::LPW;
+    int64_t nrows = (int64_t)N * N;
+    dim3 g2((unsigned)((nrows + lpb - 1) / lpb), 1);
+    { ProfScope ps_(p, "xform_rows", st);
+    k_rows_r2c<N><<<g2, 256, sizeof(float2) * lpb * R::LS, st>>>(slot, p->HP, nrows, p->d_twN, p->d_twH);
+    }
+    dim3 grid((unsigned)(N * (p->HP / W)), 1);
+    { ProfScope ps_(p, "xform_axis", st);
+    k_axis_inplace<N, W, 1, -1><<<grid, A::THREADS, A::SMEM, st>>>(slot, 0, p->HP, p->d_twN);
+    }
+    { ProfScope ps_(p, "xform_axis", st);
+    k_axis_inplace<N, W, 0, -1><<<grid, A::THREADS, A::SMEM, st>>>(slot, 0, p->HP, p->d_twN);
+    }
+    AAR_CUDA_TRY(p, cudaGetLastError());
+    p->last_launches += 3;
+    return AAR_OK;
+  }
+};
+
+// unnormalised FFTW-convention transforms through work slot 0
+int fused_c2r(Plan* p, const float2* in, float* out, cudaStream_t st) {
+  int N = p->N, H = N / 2 + 1;
+  float2* slot = p->d_work;
+  AAR_CUDA_TRY(p, cudaMemcpy2DAsync(slot, sizeof(float2) * p->HP, in, sizeof(float2) * H, sizeof(float2) * H,
+                                    (size_t)N * N, cudaMemcpyDeviceToDevice, st));
+  int rc = dispatch_n(N, [&](auto nc) { return Xform<decltype(nc)::value>::c2r(p, slot, st); });
+  if (rc) return rc;
+  AAR_CUDA_TRY(p, cudaMemcpy2DAsync(out, sizeof(float) * N, slot, sizeof(float) * 2 * p->HP, sizeof(float) * N,
+                                    (size_t)N * N, cudaMemcpyDeviceToDevice, st));
+  return AAR_OK;
+}
+
+int fused_r2c(Plan* p, const float* in, float2* out, cudaStream_t st) {
+  int N = p->N, H = N / 2 + 1;
+  float2* slot = p->d_work;
+  AAR_CUDA_TRY(p, cudaMemcpy2DAsync(slot, sizeof(float) * 2 * p->HP, in, sizeof(float) * N, sizeof(float) * N,
+                                    (size_t)N * N, cudaMemcpyDeviceToDevice, st));
+  int rc = dispatch_n(N, [&](auto nc) { return Xform<decltype(nc)::value>::r2c(p, slot, st); });
+  if (rc) return rc;
+  AAR_CUDA_TRY(p, cudaMemcpy2DAsync(out, sizeof(float2) * H, slot, sizeof(float2) * p->HP, sizeof(float2) * H,
+                                    (size_t)N * N, cudaMemcpyDeviceToDevice, st));
+  return AAR_OK;
+}
+
+int fused_configure_xform(Plan* p) {
+  return dispatch_n(p->N, [&](auto nc) {
+    constexpr int N = decltype(nc)::value;
+    using R = RowCfg<N>;
+    int lpb = 8 * R::LPW;
+    AAR_CUDA_TRY(p, cudaFuncSetAttribute(k_rows_c2r<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)(sizeof(float2) * lpb * R::LS)));
+    AAR_CUDA_TRY(p, cudaFuncSetAttribute(k_rows_r2c<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)(sizeof(float2) * lpb * R::LS)));
+    return Launch<N>::configure(p);
+  });
+}
+
+}  // namespace aar

@@ -1,0 +1,229 @@
+// Seed table and Gaussian potential (white noise) kernels.
+//
+// Seed table (Aarambam/LPT/Basis/main.c:317-349): one ranlxd1 stream seeded
+// with Seed delivers N^2 uniforms, stored as (unsigned)(0x7fffffff * u) in
+// eight "shell" segments per i < N/2.  The stream is split into segments of
+// rlx_seg refills; each thread rebuilds its segment's starting state with the
+// exact skip-ahead of ranlux.cuh and scatters its draws (the shell order is a
+// permutation of the table, so the scatter has no write conflicts).
+//
+// Noise (main.c:382-524): one thread per (i, j) column reseeds ranlxd1 with
+// seedtable[i][j] and draws (phase, amplitude) pairs for k < N/2, skipping the
+// Nyquist indices and DC after the draws, keeping the cube/sphere cut, and
+// writing the k = 0 plane with its Hermitian partner.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "aar_internal.cuh"
+#include "ranlux.cuh"
+
+namespace aar {
+
+__device__ __forceinline__ int64_t shell_pos(int64_t d, int N) {
+  // draws before shell i: 4 i^2; segment lengths i, i+1, i, i+1, ...
+  int64_t i = (int64_t)sqrt((double)d) / 2;
+  while (4 * (i + 1) * (i + 1) <= d) ++i;
+  while (4 * i * i > d) --i;
+  int64_t o = d - 4 * i * i;
+  int64_t n = N;
+  if (o < i) return i * n + o;
+  o -= i;
+  if (o < i + 1) return o * n + i;
+  o -= i + 1;
+  if (o < i) return (n - 1 - i) * n + o;
+  o -= i;
+  if (o < i + 1) return (n - 1 - o) * n + i;
+  o -= i + 1;
+  if (o < i) return i * n + (n - 1 - o);
+  o -= i;
+  if (o < i + 1) return o * n + (n - 1 - i);
+  o -= i + 1;
+  if (o < i) return (n - 1 - i) * n + (n - 1 - o);
+  o -= i;
+  return (n - 1 - o) * n + (n - 1 - i);
+}
+
+__global__ void k_seedtable(uint32_t seed, int N, int seg, const U576* __restrict__ pw, int npw,
+                            uint32_t* __restrict__ table) {
+  int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t total = (int64_t)N * N;
+  int64_t d0 = g * 12 * seg;
+  if (d0 >= total) return;
+  Rlx s;
+  rlx_seed(s, seed);
+  if (g > 0) {
+    U576 r = rlx_window_residue(s);
+    for (int b = 0; b < npw; ++b)
+      if ((g >> b) & 1) r = modmul576(r, pw[b]);
+    rlx_from_residue(r, s);
+  }
+  int64_t d1 = d0 + 12 * (int64_t)seg;
+  if (d1 > total) d1 = total;
+  for (int64_t d = d0; d < d1; ++d) {
+    double u = (double)rlx_next48(s) * 3.5527136788005009e-15;  // 2^-48
+    table[shell_pos(d, N)] = __double2uint_rz(__dmul_rn(2147483647.0, u));
+  }
+}
+
+int launch_seedtable(Plan* p, uint32_t seed, uint32_t* d_out, cudaStream_t st) {
+  int64_t total = (int64_t)p->N * p->N;
+  int64_t draws_per = 12 * (int64_t)p->rlx_seg;
+  int64_t nthr = (total + draws_per - 1) / draws_per;
+  int bs = 64;
+  { ProfScope ps_(p, "seedtable", st);
+  k_seedtable<<<(unsigned)((nthr + bs - 1) / bs), bs, 0, st>>>(seed, p->N, p->rlx_seg, (const U576*)p->d_rlxpow,
+                                                                 32, d_out);
+  }
+  AAR_CUDA_TRY(p, cudaGetLastError());
+  p->last_launches += 1;
+  return AAR_OK;
+}
+
+// ------------------------------------------------------------ noise
+struct NoiseArgs {
+  Grid g;
+  int phase_flip, fixed_amp;
+  // FP64 form: the reference's own formula
+  double anorm, ns, fac, beta;
+  // FP32 form: amplitude per n^2 = sqrt(Anorm k^ns) fac Beta / k^2
+  const float* amp;
+};
+
+// -ln(u) for u = U 2^-48 in (0, 1), FP32 with the small-(1-u) branch exact
+__device__ __forceinline__ float neg_log_u48(uint64_t U) {
+  if (U < (uint64_t(1) << 47)) return -logf((float)U * 3.5527136788005009e-15f);  // u < 1/2
+  float oneminus = (float)((uint64_t(1) << 48) - U) * 3.5527137e-15f;
+  return -log1pf(-oneminus);
+}
+
+// cos / sin of 2 pi u (+ pi when flipped) for u = U 2^-48, FP32: the exact
+// split U = H 2^24 + L gives sincospi(H 2^-23) plus a first-order correction.
+__device__ __forceinline__ void sincos_u48(uint64_t U, bool flip, float& c, float& s) {
+  uint32_t H = (uint32_t)(U >> 24), L = (uint32_t)(U & 0xFFFFFFu);
+  float a = (float)H * 1.1920928955078125e-07f;  // H 2^-23 (exact)
+  float s0, c0;
+  sincospif(a, &s0, &c0);
+  float d = (float)L * (float)(3.14159265358979323846 / 140737488355328.0);
+  c = c0 - d * s0;
+  s = s0 + d * c0;
+  if (flip) {
+    c = -c;
+    s = -s;
+  }
+}
+
+template <bool FP64>
+__global__ void k_noise(NoiseArgs a, const uint32_t* __restrict__ seedtable, void* __restrict__ out, int HP) {
+  const int N = a.g.N;
+  int64_t col = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= (int64_t)N * N) return;
+  int i = (int)(col / N), j = (int)(col % N);
+  Rlx s;
+  rlx_seed(s, seedtable[col]);
+  const int kx = sidx(i, N), ky = sidx(j, N);
+  const double box = a.g.box;
+  double fx = 0, fy = 0;
+  if (FP64) {
+    fx = __ddiv_rn(__dmul_rn((double)(2 * kx), kPi), box);
+    fy = __ddiv_rn(__dmul_rn((double)(2 * ky), kPi), box);
+  }
+  for (int k = 0; k < N / 2; ++k) {
+    uint64_t U1 = rlx_next48(s);
+    uint64_t U2;
+    do U2 = rlx_next48(s);
+    while (U2 == 0);
+    if (i == N / 2 || j == N / 2) continue;
+    if (i == 0 && j == 0 && k == 0) continue;
+    if (!keep_cell(a.g, kx, ky, k)) continue;
+    double re, im;
+    float rf = 0.f, imf = 0.f;
+    if (FP64) {
+      double fz = __ddiv_rn(__dmul_rn((double)(2 * k), kPi), box);
+      double k2 = __dadd_rn(__dadd_rn(__dmul_rn(fx, fx), __dmul_rn(fy, fy)), __dmul_rn(fz, fz));
+      double km = sqrt(k2);
+      double phase = __dmul_rn(__dmul_rn((double)U1 * 3.5527136788005009e-15, 2.0), kPi);
+      if (a.phase_flip) phase = __dadd_rn(phase, kPi);
+      double ampl = (double)U2 * 3.5527136788005009e-15;
+      double phig = a.anorm * exp(a.ns * log(km));
+      if (!a.fixed_amp) phig *= -log(ampl);
+      phig = sqrt(phig) * a.fac * a.beta / k2;
+      double sn, cs;
+      sincos(phase, &sn, &cs);
+      re = phig * cs;
+      im = phig * sn;
+    } else {
+      int n2 = kx * kx + ky * ky + k * k;
+      float amp = __ldg(a.amp + n2);
+      if (!a.fixed_amp) amp *= sqrtf(neg_log_u48(U2));
+      float c, sn;
+      sincos_u48(U1, a.phase_flip != 0, c, sn);
+      rf = amp * c;
+      imf = amp * sn;
+      re = rf;
+      im = imf;
+    }
+    int64_t c1 = -1, c2 = -1;
+    if (k > 0) {
+      c1 = ((int64_t)i * N + j) * HP + k;
+    } else if (i == 0) {
+      if (j >= N / 2) continue;
+      c1 = ((int64_t)0 * N + j) * HP;
+      c2 = ((int64_t)0 * N + (N - j)) * HP;
+    } else {
+      if (i >= N / 2) continue;
+      int ii = N - i, jj = (N - j) % N;
+      c1 = ((int64_t)i * N + j) * HP;
+      c2 = ((int64_t)ii * N + jj) * HP;
+    }
+    if (FP64) {
+      double2* o = (double2*)out;
+      o[c1] = make_double2(re, im);
+      if (c2 >= 0) o[c2] = make_double2(re, -im);
+    } else {
+      float2* o = (float2*)out;
+      o[c1] = make_float2(rf, imf);
+      if (c2 >= 0) o[c2] = make_float2(rf, -imf);
+    }
+  }
+}
+
+static NoiseArgs noise_args(Plan* p) {
+  NoiseArgs a;
+  a.g = p->grid;
+  a.phase_flip = p->prm.phase_flip == 1;
+  a.fixed_amp = p->prm.fixed_amplitude != 0;
+  a.anorm = p->Anorm;
+  a.ns = p->prm.primordial_index;
+  a.fac = pow(2 * kPi / p->prm.box, 1.5);
+  a.beta = p->Beta;
+  a.amp = p->d_amp;
+  return a;
+}
+
+int launch_noise_fp32(Plan* p, const uint32_t* d_seed, float2* d_phik, cudaStream_t st) {
+  size_t bytes = sizeof(float2) * (size_t)p->N * p->N * p->HP;
+  AAR_CUDA_TRY(p, cudaMemsetAsync(d_phik, 0, bytes, st));
+  int64_t cols = (int64_t)p->N * p->N;
+  int bs = 128;
+  { ProfScope ps_(p, "noise", st);
+  k_noise<false><<<(unsigned)((cols + bs - 1) / bs), bs, 0, st>>>(noise_args(p), d_seed, d_phik, p->HP);
+  }
+  AAR_CUDA_TRY(p, cudaGetLastError());
+  p->last_launches += 1;
+  return AAR_OK;
+}
+
+int launch_noise_fp64(Plan* p, const uint32_t* d_seed, double2* d_phik, int hp, cudaStream_t st) {
+  size_t bytes = sizeof(double2) * (size_t)p->N * p->N * hp;
+  AAR_CUDA_TRY(p, cudaMemsetAsync(d_phik, 0, bytes, st));
+  int64_t cols = (int64_t)p->N * p->N;
+  int bs = 128;
+  { ProfScope ps_(p, "noise", st);
+  k_noise<true><<<(unsigned)((cols + bs - 1) / bs), bs, 0, st>>>(noise_args(p), d_seed, d_phik, hp);
+  }
+  AAR_CUDA_TRY(p, cudaGetLastError());
+  p->last_launches += 1;
+  return AAR_OK;
+}
+
+}  // namespace aar

@@ -1,0 +1,165 @@
+"""Host API of the GPU initial-condition generator (PyTorch owns the device
+buffers and streams; the work runs in libaarambam_gpu.so).
+
+`ICGenerator(cfg, alpha, x0, k, T)` mirrors one run of the reference
+executable for a parameter-file dict `cfg` (keys as in
+Aarambam/LPT/Basis/read_param.c:25-184): `run(lagr_pos)` performs
+displacement_fields() (main.c:149-1532) on float32 [n, 3] Lagrangian
+positions resident on the GPU and returns (pos, vel).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import AarError, check
+
+
+def params_from_config(cfg: dict, precision: int = _lib.AAR_FUSED_FP32, mem_limit_bytes: int = 0) -> _lib.Params:
+    return _lib.Params(
+        nmesh=cfg["Nmesh"], nsample=cfg["Nsample"], nmax=cfg["Nmax"], seed=cfg["Seed"], box=cfg["Box"],
+        omega=cfg["Omega"], omega_lambda=cfg["OmegaLambda"], hubble_param=cfg["HubbleParam"],
+        sigma8=cfg["Sigma8"], primordial_index=cfg["PrimordialIndex"], redshift=cfg["Redshift"], fnl=cfg["Fnl"],
+        unit_length_in_cm=cfg["UnitLength_in_cm"], unit_mass_in_g=cfg["UnitMass_in_g"],
+        unit_velocity_in_cm_per_s=cfg["UnitVelocity_in_cm_per_s"],
+        input_spectrum_unit_length_in_cm=cfg["InputSpectrum_UnitLength_in_cm"],
+        fixed_amplitude=cfg["FixedAmplitude"], phase_flip=cfg["PhaseFlip"], sphere_mode=cfg["SphereMode"],
+        precision=precision, mem_limit_bytes=mem_limit_bytes)
+
+
+def _ptr(t: torch.Tensor) -> int:
+    if not t.is_cuda or not t.is_contiguous():
+        raise ValueError("expected a contiguous CUDA tensor")
+    return t.data_ptr()
+
+
+def _dptr(a: np.ndarray):
+    return np.ascontiguousarray(a, dtype=np.float64).ctypes.data_as(C.POINTER(C.c_double))
+
+
+class ICGenerator:
+    """One plan: grid, cosmology, coefficient tables and transfer function."""
+
+    def __init__(self, cfg: dict, alpha: np.ndarray, x0: np.ndarray, k: np.ndarray, T: np.ndarray,
+                 precision: str = "fp32", device=None, mem_limit_bytes: int = 0):
+        self.L = _lib.load()
+        self.cfg = dict(cfg)
+        self.N = int(cfg["Nmesh"])
+        self.device = torch.device(device if device is not None else "cuda", torch.cuda.current_device()
+                                   if device is None else torch.device(device).index or 0)
+        self.precision = _lib.AAR_FUSED_FP32 if precision == "fp32" else _lib.AAR_PLAIN_FP64
+        prm = params_from_config(cfg, self.precision, mem_limit_bytes)
+        h = C.c_void_p()
+        with torch.cuda.device(self.device):
+            rc = self.L.aar_plan_create(C.byref(prm), C.byref(h))
+        self.h = h
+        if rc != _lib.AAR_OK:
+            msg = self.L.aar_last_error(h) if h else b"plan creation failed"
+            self.close()
+            raise AarError(rc, msg.decode() if msg else "")
+        self._alpha = np.ascontiguousarray(alpha, dtype=np.float64)
+        self._x0 = np.ascontiguousarray(x0, dtype=np.float64)
+        M = self._alpha.shape[0]
+        check(self.L, self.h, self.L.aar_set_tables(self.h, _dptr(self._alpha), _dptr(self._x0), M))
+        kk = np.ascontiguousarray(k, dtype=np.float64)
+        tt = np.ascontiguousarray(T, dtype=np.float64)
+        check(self.L, self.h, self.L.aar_set_transfer(self.h, _dptr(kk), _dptr(tt), len(kk)))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.aar_plan_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def scalars(self) -> dict:
+        s = _lib.Scalars()
+        check(self.L, self.h, self.L.aar_get_scalars(self.h, C.byref(s)))
+        return {n: getattr(s, n) for n, _ in _lib.Scalars._fields_}
+
+    @property
+    def launches(self) -> int:
+        return self.L.aar_last_launch_count(self.h)
+
+    def set_seed(self, seed: int) -> None:
+        check(self.L, self.h, self.L.aar_set_seed(self.h, int(seed)))
+        self.cfg["Seed"] = int(seed)
+
+    def _stream(self):
+        return C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
+
+    def seedtable(self) -> torch.Tensor:
+        out = torch.empty((self.N, self.N), dtype=torch.int32, device=self.device)
+        check(self.L, self.h, self.L.aar_seedtable(self.h, _ptr(out), self._stream()))
+        return out
+
+    def stage(self, name: str) -> None:
+        fn = getattr(self.L, f"aar_stage_{name}")
+        check(self.L, self.h, fn(self.h, self._stream()))
+
+    def spectrum(self) -> torch.Tensor:
+        """The plan's current potential spectrum, complex64 [N, N, N/2+1]."""
+        out = torch.empty((self.N, self.N, self.N // 2 + 1), dtype=torch.complex64, device=self.device)
+        check(self.L, self.h, self.L.aar_copy_spectrum(self.h, _ptr(out), self._stream()))
+        return out
+
+    def field(self, which: int) -> torch.Tensor:
+        out = torch.empty((self.N, self.N, self.N), dtype=torch.float32, device=self.device)
+        check(self.L, self.h, self.L.aar_copy_field(self.h, which, _ptr(out), self._stream()))
+        return out
+
+    def c2r(self, spec: torch.Tensor) -> torch.Tensor:
+        spec = spec.to(torch.complex64).contiguous()
+        out = torch.empty((self.N, self.N, self.N), dtype=torch.float32, device=self.device)
+        check(self.L, self.h, self.L.aar_c2r(self.h, _ptr(spec), _ptr(out), self._stream()))
+        return out
+
+    def r2c(self, real: torch.Tensor) -> torch.Tensor:
+        real = real.to(torch.float32).contiguous()
+        out = torch.empty((self.N, self.N, self.N // 2 + 1), dtype=torch.complex64, device=self.device)
+        check(self.L, self.h, self.L.aar_r2c(self.h, _ptr(real), _ptr(out), self._stream()))
+        return out
+
+    def readout(self, lagr: torch.Tensor):
+        lagr = lagr.contiguous()
+        pos = torch.empty_like(lagr)
+        vel = torch.empty_like(lagr)
+        check(self.L, self.h, self.L.aar_stage_readout(self.h, _ptr(lagr), lagr.shape[0], _ptr(pos), _ptr(vel),
+                                                       self._stream()))
+        return pos, vel
+
+    def run(self, lagr: torch.Tensor, pos: torch.Tensor = None, vel: torch.Tensor = None):
+        """Whole path on device-resident Lagrangian positions float32 [n, 3]."""
+        lagr = lagr.contiguous()
+        pos = torch.empty_like(lagr) if pos is None else pos
+        vel = torch.empty_like(lagr) if vel is None else vel
+        check(self.L, self.h, self.L.aar_run(self.h, _ptr(lagr), lagr.shape[0], _ptr(pos), _ptr(vel),
+                                             self._stream()))
+        return pos, vel
+
+    def run_glass(self, glass: torch.Tensor, glass_box: float, tile: int):
+        glass = glass.contiguous()
+        n = glass.shape[0] * tile ** 3
+        pos = torch.empty((n, 3), dtype=torch.float32, device=self.device)
+        vel = torch.empty_like(pos)
+        ids = torch.empty((n,), dtype=torch.int32, device=self.device)
+        check(self.L, self.h, self.L.aar_run_glass(self.h, _ptr(glass), glass.shape[0], float(glass_box), tile,
+                                                   _ptr(pos), _ptr(vel), _ptr(ids), self._stream()))
+        return pos, vel, ids
+
+    def run_host(self, lagr: np.ndarray):
+        """The C-ABI host-buffer path: numpy in, numpy out (copies included)."""
+        lagr = np.ascontiguousarray(lagr, dtype=np.float32)
+        pos = np.empty_like(lagr)
+        vel = np.empty_like(lagr)
+        check(self.L, self.h, self.L.aar_run_host(self.h, lagr.ctypes.data, lagr.shape[0], pos.ctypes.data,
+                                                  vel.ctypes.data, self._stream()))
+        return pos, vel

@@ -1,0 +1,368 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 IC path: IC particles/s at 1024^3 (ScalarI template,
+20 modes, Box 1000 Mpc/h), fused FP32 form.
+
+One "step" = one whole pass of the path (seed table -> white noise -> modal
+non-Gaussian potential -> ZA + 2LPT -> particle positions and velocities) for
+one realisation, with the Lagrangian positions and all fields resident in HBM.
+Inputs are synthetic (BBKS transfer table, regular particle lattice,
+coefficient table from the reference Decomposer); the working set (~130 GB)
+is far above L2, so no flush is needed between steps.
+
+  python bench.py [--gpus N --steps K --warmup W]           (GPU arm)
+  python bench.py --impl reference [...]                    (CPU reference arm)
+
+Under torchrun (N > 1) every rank runs its own realisation (replicas: the
+path has no exchange step), timing is the max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+TABLES = os.path.join(ROOT, "tests", "golden", "tables")
+METRIC = "IC particles/s at 1024^3 (fused FP32 form)"
+UNIT = "particles/s"
+
+WORKLOADS = {
+    # name: (Nmesh, Box, table, N_modes, Nmax, Fnl)
+    "scalarI_m20_n1024": (1024, 1000.0, "scalarI_m20_L1000_n1024", 20, 1024, 100.0),
+    "scalarI_m12_n512": (512, 1000.0, "scalarI_m12_L1000_n512", 12, 512, 100.0),
+    "local_m8_n128": (128, 500.0, "local_m8_L500_n128", 8, 128, 10.0),
+}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
+    ap.add_argument("--workload", default="scalarI_m20_n1024", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-sample-n", type=int, default=128)
+    return ap.parse_args()
+
+
+def make_cfg(wl: str, seed: int) -> dict:
+    N, box, tab, M, nmax, fnl = WORKLOADS[wl]
+    return dict(Nmesh=N, Nsample=N, Nmax=nmax, Box=box, Seed=seed, Fnl=fnl, N_modes=M, table=tab, Omega=0.3,
+                OmegaLambda=0.7, HubbleParam=0.7, Sigma8=0.8, PrimordialIndex=0.965, Redshift=49.0,
+                FixedAmplitude=0, PhaseFlip=0, SphereMode=0, UnitLength_in_cm=3.085678e24, UnitMass_in_g=1.989e43,
+                UnitVelocity_in_cm_per_s=1e5, InputSpectrum_UnitLength_in_cm=3.085678e24)
+
+
+def load_tables(tab: str, M: int):
+    from aarambam_gb300 import tables
+    d = os.path.join(TABLES, tab)
+    alpha = tables.load_alpha(os.path.join(d, "AlphaTable.dat"), M)
+    x0 = tables.load_x0(os.path.join(d, "AiTable.dat"), M)
+    k, t = tables.bbks_transfer()
+    return alpha, x0, k, t
+
+
+def active_r(alpha: np.ndarray) -> int:
+    M = alpha.shape[0]
+    rs = {r for p in range(M) for q in range(p, M) for r in range(q, M) if alpha[p, q, r] != 0}
+    if M > 2 and alpha[0, 1, 2] != 0:
+        rs |= {1, 2}
+    return len(rs)
+
+
+def lattice_positions(N: int, box: float, device):
+    """Lagrangian positions of an N^3 lattice in the reference's particle
+    order (read_glass.c:181-214 with a 64^3 lattice glass tiled N/64 times
+    when N >= 64), float32 [N^3, 3] on the device."""
+    import torch
+    g = min(N, 64)
+    tile = N // g
+    glass = (torch.arange(g, dtype=torch.float64) * (100.0 / g)).float().double()
+    bt = box / tile
+    n = torch.arange(N, device=device)
+    # index of a particle: ((ti*tile + tj)*tile + tk) * g^3 + (gi*g + gj)*g + gk
+    ti, gi = n // g, n % g
+    coord = (glass.to(device)[gi] / 100.0 * bt + ti.double() * bt).float()  # per-axis value of lattice index
+    # assemble in particle order
+    idx = torch.arange(N ** 3, device=device, dtype=torch.int64)
+    gl, t = idx % (g ** 3), idx // (g ** 3)
+    gx, gy, gz = gl // (g * g), (gl // g) % g, gl % g
+    tx, ty, tz = t // (tile * tile), (t // tile) % tile, t % tile
+    pos = torch.stack([coord[tx * g + gx], coord[ty * g + gy], coord[tz * g + gz]], dim=1).contiguous()
+    return pos
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(gpu_index), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self) -> dict:
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        self.p.wait()
+        self.f.flush()
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+                for nm, v in zip(names, r[5:9]):
+                    if v.strip().lower() == "active":
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                continue
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def alg_bytes(name: str, N: int, M: int, R: int, npart: int) -> float:
+    """Algorithmic HBM bytes of one launch of each kernel: every field it must
+    read and write once (complex half spectrum, F = 8 N^2 (N/2+1) bytes)."""
+    F = 8.0 * N * N * (N // 2 + 1)
+    table = {
+        "seedtable": 4.0 * N * N, "noise": F + 4.0 * N * N,
+        "modal_xinv": (1 + M) * F, "modal_ypass_inv": 2 * M * F, "modal_rows": (M + R) * F,
+        "modal_ypass_fwd": 2 * R * F, "modal_xacc": (R + 2) * F,
+        "lpt_xinv_hess": 7 * F, "lpt_ypass_inv_hess": 12 * F, "lpt_rows_source": 7 * F,
+        "lpt_ypass_fwd_source": 2 * F, "lpt_xmid": 8 * F, "lpt_ypass_inv_disp": 12 * F,
+        "lpt_rows_c2r": 12 * F, "readout": 6 * 4.0 * N ** 3 + 36.0 * npart,
+    }
+    return table.get(name, float("nan"))
+
+
+def peaks() -> dict:
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    except (OSError, KeyError, ValueError):
+        return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def traffic_for(kernel: str, N: int):
+    """dram bytes per launch from a committed ncu summary, scaled to N."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        e = d[kernel]
+        return e["bytes_per_launch"] * (N / e["N"]) ** 3
+    except (OSError, KeyError, ValueError):
+        return None
+
+
+def cpu_baseline(wl: str, n_sample: int, steps: int = 1) -> dict:
+    """The FP64 oracle (the reference algorithm restated in C, OpenMP over all
+    host cores) on a bounded sample of the workload: the same coefficient
+    table and path at n_sample^3."""
+    from oracle import oracle as O
+    O.build()
+    cfg = make_cfg(wl, 1234)
+    cfg.update(Nmesh=n_sample, Nsample=n_sample)
+    alpha, x0, k, t = load_tables(cfg["table"], cfg["N_modes"])
+    o = O.Oracle(cfg, k, t)
+    g = np.arange(n_sample, dtype=np.float64) * (cfg["Box"] / n_sample)
+    x, y, z = np.meshgrid(g, g, g, indexing="ij")
+    lagr = np.stack([x.ravel(), y.ravel(), z.ravel()], 1).astype(np.float32)
+    ts = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        o.run(alpha, x0, lagr)
+        ts.append(time.perf_counter() - t0)
+    t = min(ts)
+    cores = os.cpu_count()
+    return {"value": n_sample ** 3 / t, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"oracle FP64 C restatement of the reference path (same {cfg['N_modes']}-mode table, "
+                      f"reference loop structure, OpenMP) on {n_sample}^3 particles/grid, {t:.2f} s/step, "
+                      f"{os.uname().machine}"}
+
+
+def gpu_arm(args):
+    import torch
+    import torch.distributed as dist
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    from aarambam_gb300 import _lib
+    from aarambam_gb300.ic import ICGenerator
+    _lib.load(build_if_missing=True)
+
+    cfg = make_cfg(args.workload, 1234 + rank)
+    N, M = cfg["Nmesh"], cfg["N_modes"]
+    alpha, x0, k, t = load_tables(cfg["table"], M)
+    R = active_r(alpha)
+    gen = ICGenerator(cfg, alpha, x0, k, t)
+    lagr = lattice_positions(N, cfg["Box"], dev)
+    npart = lagr.shape[0]
+    pos = torch.empty_like(lagr)
+    vel = torch.empty_like(lagr)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        gen.run(lagr, pos, vel)
+    barrier()
+    clk = Clocks(local)
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    launches = 0
+    for _ in range(args.steps):
+        gen.run(lagr, pos, vel)
+        launches += gen.launches
+    e1.record(stream)
+    barrier()
+    clocks = clk.stop()
+    elapsed = e0.elapsed_time(e1) / 1e3
+    if world > 1:
+        tt = torch.tensor([elapsed], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        elapsed = float(tt.item())
+    value = world * args.steps * npart / elapsed
+
+    # per-kernel times of one profiled step (events on the launching stream)
+    buf = __import__("ctypes").create_string_buffer(1 << 16)
+    gen.L.aar_profile_enable(gen.h, 1)
+    for _ in range(max(1, min(args.steps, 2))):
+        gen.run(lagr, pos, vel)
+    gen.L.aar_profile_report(gen.h, buf, len(buf))
+    gen.L.aar_profile_enable(gen.h, 0)
+    kernels = {}
+    for line in buf.value.decode().strip().splitlines():
+        nm, cnt, ms = line.split(",")
+        kernels[nm] = {"launches": int(cnt), "ms": float(ms)}
+    tot = sum(v["ms"] for v in kernels.values())
+    pk = peaks()
+    dom = max(kernels, key=lambda n: kernels[n]["ms"])
+    for nm, v in kernels.items():
+        per = v["ms"] / v["launches"] / 1e3
+        v["share"] = round(v["ms"] / tot, 4)
+        v["gbs"] = round(alg_bytes(nm, N, M, R, npart) / per / 1e9, 1)
+    d_per = kernels[dom]["ms"] / kernels[dom]["launches"] / 1e3
+    achieved = alg_bytes(dom, N, M, R, npart) / d_per / 1e9
+    roofline = {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": pk["hbm_gbs"],
+                "unit": "GB/s", "frac": round(achieved / pk["hbm_gbs"], 4),
+                "traffic": traffic_for(dom, N), "peak_source": pk["source"]}
+    # whole path against the algorithmic byte count 4 N^3 (46 + 9 M)
+    b_path = 4.0 * N ** 3 * (46 + 9 * M)
+    path_roof = {"bytes_per_step": b_path, "achieved": round(b_path / (elapsed / args.steps) / 1e9, 1),
+                 "frac": round(b_path / (elapsed / args.steps) / 1e9 / pk["hbm_gbs"], 4)}
+
+    e2e = None
+    if not args.no_e2e:
+        h_in = torch.empty((npart, 3), dtype=torch.float32, pin_memory=True)
+        h_in.copy_(lagr.cpu())
+        h_pos = torch.empty_like(h_in).pin_memory()
+        h_vel = torch.empty_like(h_in).pin_memory()
+        import ctypes
+        st = ctypes.c_void_p(stream.cuda_stream)
+
+        def host_step():
+            rc = gen.L.aar_run_host(gen.h, h_in.data_ptr(), npart, h_pos.data_ptr(), h_vel.data_ptr(), st)
+            _lib.check(gen.L, gen.h, rc)
+        host_step()
+        barrier()
+        t0 = time.perf_counter()
+        ks = max(1, min(args.steps, 3))
+        for _ in range(ks):
+            host_step()
+        barrier()
+        te = time.perf_counter() - t0
+        if world > 1:
+            tt = torch.tensor([te], device=dev)
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            te = float(tt.item())
+        e2e = {"value": world * ks * npart / te, "unit": UNIT, "h2d_bytes_per_step": 12 * npart,
+               "d2h_bytes_per_step": 24 * npart, "steps": ks, "api": "aar_run_host (C ABI, pinned host buffers)"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(args.workload, args.cpu_sample_n)
+
+    if rank == 0:
+        out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+               "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
+               "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+               "config": {"workload": f"{args.workload}: Nmesh={N}^3 particles, Box={cfg['Box']} Mpc/h, "
+                                      f"{cfg['table']} ({M} modes, {R} active r), Fnl={cfg['Fnl']}, BBKS T(k), "
+                                      f"z=49", "nmesh": N, "n_modes": M, "l2": "working set >> L2 (no flush)",
+                          "parallelism": "replicas" if world > 1 else "single GPU"},
+               "roofline": roofline, "path_roofline": path_roof, "cpu_baseline": cpu, "e2e": e2e,
+               "gpu_launches": launches, "clocks": clocks, "kernels": kernels}
+        print(json.dumps(out))
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    cfg = make_cfg(args.workload, 1234)
+    n = args.cpu_sample_n
+    # size the sample so the whole run stays within a few minutes
+    first = cpu_baseline(args.workload, n, 1)
+    per = n ** 3 / first["value"]
+    while n > 32 and per * (args.steps + args.warmup) > 240:
+        n //= 2
+        first = cpu_baseline(args.workload, n, 1)
+        per = n ** 3 / first["value"]
+    for _ in range(max(0, args.warmup - 1)):
+        cpu_baseline(args.workload, n, 1)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        cpu_baseline(args.workload, n, 1)
+    el = time.perf_counter() - t0
+    value = args.steps * n ** 3 / el
+    base = dict(first, value=value)
+    print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": 0,
+                      "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+                      "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                      "data": "synthetic", "config": {"workload": f"{args.workload} sampled at {n}^3",
+                                                      "nmesh": cfg["Nmesh"]},
+                      "cpu_baseline": base,
+                      "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+
+
+if __name__ == "__main__":
+    a = parse()
+    if a.impl == "reference":
+        reference_arm(a)
+    else:
+        gpu_arm(a)

@@ -1,0 +1,145 @@
+/*
+ * aarambam.h -- C ABI of libaarambam_gpu.so, the GB300 (sm_103a) implementation
+ * of Aarambam's initial-condition path: seed-table white noise -> modal
+ * non-Gaussian potential -> ZA + 2LPT displacements -> particles.
+ *
+ * The reference exposes this path as a process: `Aarambam-2LPT-Basis
+ * <paramfile>` (Aarambam/LPT/Basis/cli.py:5-10) runs the C/MPI executable
+ * whose work happens in main() (Aarambam/LPT/Basis/main.c:53-102) and
+ * displacement_fields() (main.c:149-1532).  Each entry point below replaces
+ * one piece of that executable; the comment names the piece.  The reference
+ * has no in-process library interface, so the binding a maintainer adds is
+ * the ctypes layer of the Python package (aarambam_gb300/_lib.py) behind the
+ * same CLI name.
+ *
+ * Conventions: every call returns AAR_OK (0) or an error code (never exits);
+ * aar_last_error() gives the message.  Device pointers are caller-owned CUDA
+ * allocations on the plan's device; `stream` is a cudaStream_t (NULL = the
+ * legacy default stream).  A plan owns its scratch and is not thread-safe;
+ * distinct plans may run concurrently on distinct streams.
+ */
+#ifndef AARAMBAM_H
+#define AARAMBAM_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define AAR_OK 0
+#define AAR_ERR_ARG 1           /* invalid argument or unsupported size */
+#define AAR_ERR_CUDA 2          /* a CUDA call failed */
+#define AAR_ERR_OOM 3           /* device allocation refused (or over mem_limit_bytes) */
+#define AAR_ERR_STATE 4         /* tables / transfer function not set */
+#define AAR_ERR_NMAX 200        /* Nmax < Nsample (main.c:200 assert) */
+#define AAR_ERR_TRANSFER 1111   /* first log10 k of the transfer table >= -4.6 (power.c:117-122) */
+#define AAR_ERR_TRANSFER_DUP 777 /* two transfer rows with equal k (power.c:205-206) */
+
+/* Arithmetic of the run. */
+#define AAR_FUSED_FP32 0  /* own FFTs, fused filters/products/accumulation, FP32 */
+#define AAR_PLAIN_FP64 1  /* cuFFT Z2D/D2Z + separate pointwise kernels, FP64 */
+
+/* The parameter-file values the path uses (read_param.c:25-184). */
+typedef struct aar_params {
+  int32_t nmesh, nsample, nmax, seed;
+  double box;
+  double omega, omega_lambda, hubble_param, sigma8, primordial_index, redshift, fnl;
+  double unit_length_in_cm, unit_mass_in_g, unit_velocity_in_cm_per_s;
+  double input_spectrum_unit_length_in_cm;
+  int32_t fixed_amplitude, phase_flip, sphere_mode;
+  int32_t precision;        /* AAR_FUSED_FP32 or AAR_PLAIN_FP64 */
+  int64_t mem_limit_bytes;  /* refuse plan allocations beyond this (0 = no cap) */
+} aar_params;
+
+/* Host scalars of the set-up: power.c:391-448 (Norm = sigma8 normalisation,
+   Anorm, D0, Dplus), set_units main.c:1547-1552 (Hubble), main.c:305-307
+   (velocity prefactors), main.c:372 (Beta). */
+typedef struct aar_scalars {
+  double norm, anorm, d0, dplus, init_time, hubble, beta, vel_prefac, vel_prefac2;
+} aar_scalars;
+
+typedef struct aar_plan aar_plan;
+
+/* Create a plan for one grid size on the current CUDA device
+   (replaces initialize_ffts main.c:1556-1599 and the parameter broadcast). */
+int aar_plan_create(const aar_params* prm, aar_plan** out);
+
+/* Coefficient tables: alpha as a symmetric [M][M][M] array (as the reference
+   stores it after reading AlphaTable.dat, main.c:213-247), X0 as [M] (first
+   value column of AiTable.dat, main.c:249-289). */
+int aar_set_tables(aar_plan* plan, const double* alpha_sym, const double* x0, int32_t n_modes);
+
+/* Tabulated transfer function, raw (k, T) rows in h/Mpc (read_transfer_table
+   power.c:66-153 plus initialize_powerspectrum power.c:391-448, which needs
+   the table for the sigma8 normalisation).  Computes the host scalars. */
+int aar_set_transfer(aar_plan* plan, const double* k, const double* t, int32_t n);
+
+int aar_get_scalars(const aar_plan* plan, aar_scalars* out);
+
+/* Change the realisation seed (the parameter-file Seed). */
+int aar_set_seed(aar_plan* plan, int32_t seed);
+
+/* The whole of displacement_fields() (main.c:149-1532): particles at the
+   Lagrangian positions d_lagr_pos (float32 [npart][3]) are moved; positions
+   and velocities (float32 [npart][3]) are written to d_pos / d_vel, which may
+   alias d_lagr_pos. */
+int aar_run(aar_plan* plan, const float* d_lagr_pos, int64_t npart, float* d_pos, float* d_vel, void* stream);
+
+/* As aar_run, with the Lagrangian positions made on the device from a glass
+   tiled tile^3 times (read_glass.c:129-214); also writes the particle IDs
+   (int32, 1-based, read_glass.c:183-211).  npart = nglass * tile^3. */
+int aar_run_glass(aar_plan* plan, const float* d_glass_pos, int64_t nglass, double glass_box, int32_t tile,
+                  float* d_pos, float* d_vel, int32_t* d_ids, void* stream);
+
+/* aar_run with HOST buffers: copies in, runs on `stream`, copies out and
+   synchronises.  The device staging buffers are owned by the plan (allocated
+   on first use, grown when npart grows, freed with the plan). */
+int aar_run_host(aar_plan* plan, const float* h_lagr_pos, int64_t npart, float* h_pos, float* h_vel, void* stream);
+
+/* ---- stage entry points (the same work as aar_run, split; used by tests) ---- */
+
+/* Seed table of main.c:317-349 (uint32 [N][N]) for the plan's seed. */
+int aar_seedtable(aar_plan* plan, uint32_t* d_out, void* stream);
+/* Gaussian potential spectrum (main.c:354-524) into the plan's spectrum. */
+int aar_stage_noise(aar_plan* plan, void* stream);
+/* Modal non-Gaussian potential and combination (main.c:564-1151). */
+int aar_stage_modal(aar_plan* plan, void* stream);
+/* ZA + 2LPT displacement fields (main.c:1156-1381). */
+int aar_stage_lpt(aar_plan* plan, void* stream);
+/* Particle read-out (main.c:1436-1516). */
+int aar_stage_readout(aar_plan* plan, const float* d_lagr_pos, int64_t npart, float* d_pos, float* d_vel,
+                      void* stream);
+/* Copy the plan's current potential spectrum to d_out as complex
+   [N][N][N/2+1] (interleaved re, im; float32 for AAR_FUSED_FP32, float64
+   for AAR_PLAIN_FP64). */
+int aar_copy_spectrum(aar_plan* plan, void* d_out, void* stream);
+/* Copy displacement field `which` (0..2: ZA x,y,z; 3..5: 2LPT x,y,z as the
+   reference holds them before its 1/N^3) to d_out, float32 [N][N][N]. */
+int aar_copy_field(aar_plan* plan, int32_t which, float* d_out, void* stream);
+
+/* The plan's own 3-D transforms with FFTW's rfftwnd conventions
+   (unnormalised; c2r drops the imaginary parts that the kz = 0 and kz = N/2
+   planes would need to be Hermitian), as used on every rfftwnd_mpi call site
+   of main.c.  Fused form only; complex data as in aar_copy_spectrum, real
+   data float32 [N][N][N].  The plan's first work field is used as scratch. */
+int aar_c2r(aar_plan* plan, const void* d_in, float* d_out, void* stream);
+int aar_r2c(aar_plan* plan, const float* d_in, void* d_out, void* stream);
+
+/* Per-kernel timing: when enabled, CUDA events are recorded on the launching
+   stream around every kernel; aar_profile_report synchronises the device and
+   writes "kernel,launches,total_ms" lines for everything recorded since the
+   last report into buf (NUL-terminated). */
+int aar_profile_enable(aar_plan* plan, int32_t on);
+int aar_profile_report(aar_plan* plan, char* buf, int32_t len);
+
+/* Number of kernels the last aar_run* / stage call launched. */
+int aar_last_launch_count(const aar_plan* plan);
+const char* aar_last_error(const aar_plan* plan);
+void aar_plan_destroy(aar_plan* plan);
+int aar_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,210 @@
+"""Parity of the CUDA path (through the C ABI) with the FP64 oracle and with
+the reference's own outputs.  Bit-exact: seed table, the zero pattern of the
+Gaussian spectrum (Nyquist / DC / cut / Hermitian fill).  Tolerances (FP32
+arithmetic against FP64): stated per test."""
+import functools
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import oracle as O
+from tests.common import (CASES, bbks, lattice_lagrangian, load_case, make_cfg, periodic_delta, rel_rms, table)
+
+pytestmark = pytest.mark.gpu
+
+
+def gen_for(cfg, precision="fp32", **kw):
+    from aarambam_gb300.ic import ICGenerator
+    alpha, x0 = table(cfg["table"], cfg["N_modes"])
+    k, t = bbks()
+    return ICGenerator(cfg, alpha, x0, k, t, precision=precision, **kw)
+
+
+@functools.lru_cache(maxsize=None)
+def oracle_run(key):
+    cfg = dict(key)
+    k, t = bbks()
+    o = O.Oracle(cfg, k, t)
+    alpha, x0 = table(cfg["table"], cfg["N_modes"])
+    gn, tile = cfg.get("glass_n", cfg["Nmesh"]), cfg.get("GlassTileFac", 1)
+    lagr = lattice_lagrangian(o, gn, tile)
+    r = o.run(alpha, x0, lagr)
+    r["lagr"] = lagr
+    return r
+
+
+def key(cfg):
+    return tuple(sorted(cfg.items()))
+
+
+SMALL = [
+    make_cfg(16, 500.0, 1234, 10.0, 8, "local_m8_L500_n128", 128),
+    make_cfg(32, 500.0, 4321, 100.0, 10, "scalarI_m10_L500_n256", 256, Nsample=24, PhaseFlip=1),
+    make_cfg(32, 1000.0, 7, 100.0, 12, "scalarI_m12_L1000_n512", 512, SphereMode=1, Nsample=28),
+    make_cfg(64, 500.0, 99, -50.0, 8, "local_m8_L500_n128", 128, FixedAmplitude=1),
+    make_cfg(128, 500.0, 1234, 10.0, 8, "local_m8_L500_n128", 128),
+]
+
+
+@pytest.mark.parametrize("N,seed", [(16, 1234), (32, 4321), (64, 7), (128, 1), (256, 99), (512, 2024)])
+def test_seedtable_bit_exact(cuda, N, seed):
+    cfg = make_cfg(N, 500.0, seed, 10.0, 8, "local_m8_L500_n128", max(N, 128))
+    g = gen_for(cfg)
+    got = g.seedtable().cpu().numpy().view(np.uint32)
+    k, t = bbks()
+    want = O.Oracle(cfg, k, t).seedtable()
+    assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("cfg", SMALL[:4], ids=lambda c: f"N{c['Nmesh']}_s{c['Seed']}")
+def test_gaussian_spectrum(cuda, cfg):
+    g = gen_for(cfg)
+    g.stage("noise")
+    got = g.spectrum().cpu().numpy()
+    k, t = bbks()
+    ref = O.Oracle(cfg, k, t).gauss()
+    ref = ref[..., 0] + 1j * ref[..., 1]
+    # exactly the same cells are set (skips after the draws, cut, Hermitian k=0 plane)
+    assert np.array_equal(got != 0, ref != 0)
+    # FP32 amplitude / phase from the bit-exact uniforms: per-cell relative error
+    nz = ref != 0
+    relerr = np.abs(got[nz] - ref[nz]) / np.abs(ref[nz])
+    assert relerr.max() < 2e-6
+    assert rel_rms(got, ref) < 3e-7
+
+
+@pytest.mark.parametrize("N", [16, 32, 64, 128])
+def test_transforms_match_numpy(cuda, N):
+    cfg = make_cfg(N, 500.0, 1, 10.0, 8, "local_m8_L500_n128", 128)
+    g = gen_for(cfg)
+    rng = np.random.default_rng(N)
+    X = (rng.standard_normal((N, N, N // 2 + 1)) + 1j * rng.standard_normal((N, N, N // 2 + 1))).astype(np.complex64)
+    y = g.c2r(torch.from_numpy(X).cuda()).cpu().numpy()
+    yr = np.fft.irfftn(X.astype(np.complex128), s=(N, N, N), axes=(0, 1, 2)) * N**3
+    assert rel_rms(y, yr) < 1e-6
+    x = rng.standard_normal((N, N, N)).astype(np.float32)
+    c = g.r2c(torch.from_numpy(x).cuda()).cpu().numpy()
+    cr = np.fft.rfftn(x.astype(np.float64))
+    assert rel_rms(c, cr) < 1e-6
+    assert g.launches == 3
+
+
+@pytest.mark.parametrize("cfg", SMALL, ids=lambda c: f"N{c['Nmesh']}_s{c['Seed']}")
+def test_nongaussian_potential(cuda, cfg):
+    r = oracle_run(key(cfg))
+    g = gen_for(cfg)
+    g.stage("noise")
+    gauss = g.spectrum().cpu().numpy().astype(np.complex128)
+    g.stage("modal")
+    tot = g.spectrum().cpu().numpy().astype(np.complex128)
+    ref_tot = r["total"][..., 0] + 1j * r["total"][..., 1]
+    ref_g = r["gauss"][..., 0] + 1j * r["gauss"][..., 1]
+    N = cfg["Nmesh"]
+    # the non-Gaussian part on its own: (total - gauss) N^3 / Fnl = acc
+    ng = (tot - gauss) * N**3 / cfg["Fnl"]
+    ref_ng = (ref_tot - ref_g) * N**3 / cfg["Fnl"]
+    assert rel_rms(ng, ref_ng) < 2e-4
+    assert rel_rms(tot, ref_tot) < 1e-6
+
+
+@pytest.mark.parametrize("cfg", SMALL, ids=lambda c: f"N{c['Nmesh']}_s{c['Seed']}")
+def test_displacement_fields(cuda, cfg):
+    r = oracle_run(key(cfg))
+    g = gen_for(cfg)
+    g.stage("noise")
+    g.stage("modal")
+    g.stage("lpt")
+    # ZA fields to 1e-5; the 2LPT fields carry the FP32 rounding of the
+    # Hessians through the cancelling source S = d00 (d11 + d22) + ... (their
+    # weight in the displacement is 3/7 psi2 / N^3, about 1% at z = 49)
+    for which in range(6):
+        got = g.field(which).cpu().numpy()
+        tol = 1e-5 if which < 3 else 2e-4
+        assert rel_rms(got, r["disp"][which]) < tol, which
+
+
+@pytest.mark.parametrize("cfg", SMALL, ids=lambda c: f"N{c['Nmesh']}_s{c['Seed']}")
+def test_particles_vs_oracle(cuda, cfg):
+    r = oracle_run(key(cfg))
+    g = gen_for(cfg)
+    lagr = torch.from_numpy(r["lagr"]).cuda()
+    pos, vel = g.run(lagr)
+    pos, vel = pos.cpu().numpy(), vel.cpu().numpy()
+    d_gpu = periodic_delta(pos, r["lagr"], cfg["Box"])
+    d_ref = periodic_delta(r["pos"], r["lagr"], cfg["Box"])
+    assert rel_rms(d_gpu, d_ref) < 1e-5
+    assert rel_rms(vel, r["vel"]) < 1e-5
+    assert g.launches > 5
+
+
+@pytest.mark.parametrize("name", [c for c in CASES if c != "local_n24"])
+def test_particles_vs_reference_outputs(cuda, name):
+    """Against the reference executable's own snapshot (tests/golden/ref)."""
+    cfg, z = load_case(name)
+    g = gen_for(cfg)
+    k, t = bbks()
+    o = O.Oracle(cfg, k, t)
+    lagr = lattice_lagrangian(o, cfg["glass_n"], cfg["GlassTileFac"])
+    pos, vel = g.run(torch.from_numpy(lagr).cuda())
+    d_gpu = periodic_delta(pos.cpu().numpy(), lagr, cfg["Box"])
+    d_ref = periodic_delta(z["pos"], lagr, cfg["Box"])
+    assert rel_rms(d_gpu, d_ref) < 1e-5
+    assert rel_rms(vel.cpu().numpy(), z["vel"]) < 1e-5
+
+
+def test_run_glass_matches_run(cuda):
+    from aarambam_gb300 import gadget
+    cfg, z = load_case("local_n32")
+    g = gen_for(cfg)
+    glass = gadget.lattice_glass(cfg["glass_n"], 100.0)
+    pos_g, vel_g, ids = g.run_glass(torch.from_numpy(glass).cuda(), 100.0, cfg["GlassTileFac"])
+    k, t = bbks()
+    lagr = lattice_lagrangian(O.Oracle(cfg, k, t), cfg["glass_n"], cfg["GlassTileFac"])
+    pos, vel = g.run(torch.from_numpy(lagr).cuda())
+    assert torch.equal(pos_g, pos) and torch.equal(vel_g, vel)
+    assert np.array_equal(ids.cpu().numpy(), z["ids"])
+
+
+def test_run_host_matches_device(cuda):
+    cfg = SMALL[1]
+    r = oracle_run(key(cfg))
+    g = gen_for(cfg)
+    pos_d, vel_d = g.run(torch.from_numpy(r["lagr"]).cuda())
+    torch.cuda.synchronize()
+    pos_h, vel_h = g.run_host(r["lagr"])
+    assert np.array_equal(pos_h, pos_d.cpu().numpy()) and np.array_equal(vel_h, vel_d.cpu().numpy())
+
+
+def test_seed_changes_realisation(cuda):
+    cfg = SMALL[0]
+    g = gen_for(cfg)
+    a = g.seedtable().cpu()
+    g.set_seed(cfg["Seed"] + 1)
+    b = g.seedtable().cpu()
+    assert not torch.equal(a, b)
+
+
+def test_error_codes_without_faults(cuda):
+    from aarambam_gb300._lib import AAR_ERR_ARG, AAR_ERR_NMAX, AAR_ERR_OOM, AAR_ERR_TRANSFER, AarError
+    from aarambam_gb300.ic import ICGenerator
+    alpha, x0 = table("local_m8_L500_n128", 8)
+    k, t = bbks()
+    with pytest.raises(AarError) as e:
+        ICGenerator(make_cfg(32, 500.0, 1, 10.0, 8, "x", Nmax=16), alpha, x0, k, t)
+    assert e.value.code == AAR_ERR_NMAX
+    with pytest.raises(AarError) as e:
+        ICGenerator(make_cfg(48, 500.0, 1, 10.0, 8, "x", Nmax=128), alpha, x0, k, t)
+    assert e.value.code == AAR_ERR_ARG
+    kk = np.logspace(-3, 2, 100)
+    with pytest.raises(AarError) as e:
+        ICGenerator(make_cfg(32, 500.0, 1, 10.0, 8, "x", Nmax=128), alpha, x0, kk, np.ones_like(kk))
+    assert e.value.code == AAR_ERR_TRANSFER
+    with pytest.raises(AarError) as e:
+        ICGenerator(make_cfg(64, 500.0, 1, 10.0, 8, "x", Nmax=128), alpha, x0, k, t, mem_limit_bytes=1 << 16)
+    assert e.value.code == AAR_ERR_OOM
+    bad = alpha.copy()
+    bad[1, 1, 1] = np.nan
+    with pytest.raises(AarError) as e:
+        ICGenerator(make_cfg(32, 500.0, 1, 10.0, 8, "x", Nmax=128), bad, x0, k, t)
+    assert e.value.code == AAR_ERR_ARG

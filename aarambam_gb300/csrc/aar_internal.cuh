@@ -70,6 +70,10 @@ struct Plan {
   float2* d_twH = nullptr;    // exp(-2 pi i m / (N/2)), m < N/2
   float* d_amp = nullptr;     // per n^2 noise amplitude
   float* d_twb = nullptr;     // per n^2 T(k) / (Dplus Beta)
+  float* d_qtab = nullptr;    // [M][nsq] field filters q_p per n^2
+  float* d_rtab = nullptr;    // [M][nsq] radial parts rho_r per n^2
+  int64_t nsq = 0;            // 3 (N/2)^2 + 1
+  int qtab_m = 0;             // modes the tables were allocated for
   void* d_rlxpow = nullptr;   // skip-ahead powers (U576[32])
   int rlx_seg = 0;            // refills per seed-table thread
   // modal term list (device)

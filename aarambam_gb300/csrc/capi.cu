@@ -83,6 +83,11 @@ struct Cosmo {
   }
 };
 
+double plain_transfer(const Plan* p, double k) {
+  Cosmo c{p, 1.0};
+  return c.transfer(k);
+}
+
 // Romberg quadrature: trapezoid refinements extrapolated to zero step with
 // Neville's algorithm over the last five estimates, relative tolerance 1e-8.
 template <class F>
@@ -227,7 +232,7 @@ static void plan_release(Plan* p) {
   p->prof.clear();
   for (auto e : p->event_pool) cudaEventDestroy(e);
   p->event_pool.clear();
-  void* ptrs[] = {p->d_phik, p->d_work, p->d_seed, p->d_twN, p->d_twH, p->d_amp, p->d_twb, p->d_rlxpow, p->d_terms, p->d_io};
+  void* ptrs[] = {p->d_phik, p->d_work, p->d_seed, p->d_twN, p->d_twH, p->d_amp, p->d_twb, p->d_rlxpow, p->d_terms, p->d_io, p->d_qtab, p->d_rtab};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   p->d_phik = p->d_work = nullptr;
@@ -235,6 +240,7 @@ static void plan_release(Plan* p) {
   p->d_twN = p->d_twH = nullptr;
   p->d_amp = p->d_twb = nullptr;
   p->d_rlxpow = p->d_terms = nullptr;
+  p->d_qtab = p->d_rtab = nullptr;
   p->d_io = nullptr;
   p->io_cap = 0;
   plain_free(p);
@@ -255,6 +261,61 @@ static int alloc_fused(Plan* p, int M) {
   int rc = plan_alloc(p, (void**)&p->d_work, fbytes * nwork);
   if (rc) return rc;
   p->nwork = nwork;
+  return AAR_OK;
+}
+
+// Per-|k|^2 tables of the mode functions, FP64 on the host with the
+// reference's formulas, stored as float:
+//   q_n (field filter, main.c:580-637):   k^{s(n-3)} k^{4-ns}           (n <= 3)
+//                                         (P_{n-1}(kbar) - X0[n-1]) k^{2-ns}
+//   rho_n (radial part, main.c:833-860):  k^{s(n-3)} (n <= 3),  (P_{n-1}(kbar) - X0[n-1]) / k^2
+// with s = (4-ns)/3, kbar = -1 + 2 (k^s - kmin^s)/(kmax^s - kmin^s).
+static int mode_tables(Plan* p) {
+  int N = p->N, M = p->M;
+  int64_t nsq = 3LL * (N / 2) * (N / 2) + 1;
+  if (p->d_qtab && p->nsq == nsq && p->qtab_m >= M) {
+    // reuse the allocation
+  } else {
+    if (p->d_qtab) cudaFree(p->d_qtab), p->used_bytes -= sizeof(float) * p->nsq * p->qtab_m;
+    if (p->d_rtab) cudaFree(p->d_rtab), p->used_bytes -= sizeof(float) * p->nsq * p->qtab_m;
+    p->d_qtab = p->d_rtab = nullptr;
+    int rc;
+    if ((rc = plan_alloc(p, (void**)&p->d_qtab, sizeof(float) * nsq * M))) return rc;
+    if ((rc = plan_alloc(p, (void**)&p->d_rtab, sizeof(float) * nsq * M))) return rc;
+    p->qtab_m = M;
+  }
+  p->nsq = nsq;
+  const double ns = p->prm.primordial_index, box = p->prm.box;
+  const double kmin = 2 * kPi / box, kmax = 2 * kPi / box * p->prm.nmax;
+  const double sx = (4 - ns) / 3, kmin_ns = pow(kmin, sx), kmax_ns = pow(kmax, sx);
+  const double kF = 2 * kPi / box;
+  std::vector<float> qt((size_t)nsq * M), rt((size_t)nsq * M);
+  std::vector<double> P(std::max(M, 2));
+  for (int64_t n2 = 1; n2 < nsq; ++n2) {
+    double k1 = kF * sqrt((double)n2), k2 = k1 * k1;
+    double kbar = -1 + 2 * (pow(k1, sx) - kmin_ns) / (kmax_ns - kmin_ns);
+    double pin = pow(k1, 4 - ns), p2n = pow(k1, 2 - ns);
+    // P_l(kbar), l < M, by the Bonnet recurrence
+    P[0] = 1;
+    if (M > 1) P[1] = kbar;
+    for (int l = 2; l < M; ++l) P[l] = ((2 * l - 1) * kbar * P[l - 1] - (l - 1) * P[l - 2]) / l;
+    for (int n = 0; n < M; ++n) {
+      double in, out;
+      if (n <= 3) {
+        out = pow(k1, sx * (n - 3.));
+        in = out * pin;
+      } else {
+        double d = P[n - 1] - p->x0[n - 1];
+        out = d / k2;
+        in = d * p2n;
+      }
+      qt[(size_t)n * nsq + n2] = (float)in;
+      rt[(size_t)n * nsq + n2] = (float)out;
+    }
+  }
+  for (int n = 0; n < M; ++n) qt[(size_t)n * nsq] = rt[(size_t)n * nsq] = 0.f;
+  AAR_CUDA_TRY(p, cudaMemcpy(p->d_qtab, qt.data(), sizeof(float) * qt.size(), cudaMemcpyHostToDevice));
+  AAR_CUDA_TRY(p, cudaMemcpy(p->d_rtab, rt.data(), sizeof(float) * rt.size(), cudaMemcpyHostToDevice));
   return AAR_OK;
 }
 
@@ -378,9 +439,11 @@ int aar_set_tables(aar_plan* h, const double* alpha, const double* x0, int32_t M
   p->alpha.assign(alpha, alpha + n3);
   p->x0.assign(x0, x0 + M);
   p->M = M;
+  plain_free(p);  // plain-form tables are rebuilt on the next run
   int rc;
   if (p->prm.precision == AAR_FUSED_FP32) {
     if ((rc = alloc_fused(p, M))) return rc;
+    if ((rc = mode_tables(p))) return rc;
     if (!p->d_terms && (rc = plan_alloc(p, &p->d_terms, terms_bytes()))) return rc;
     if ((rc = fused_prepare(p))) return rc;
     if ((rc = fused_configure_xform(p))) return rc;
@@ -391,6 +454,7 @@ int aar_set_tables(aar_plan* h, const double* alpha, const double* x0, int32_t M
 
 int aar_set_transfer(aar_plan* h, const double* k, const double* t, int32_t n) {
   if (!h) return AAR_ERR_ARG;
+  plain_free(&h->p);
   return set_transfer(&h->p, k, t, n);
 }
 

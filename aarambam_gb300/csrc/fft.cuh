@@ -195,13 +195,25 @@ __device__ __forceinline__ void stage_load(float2* v, const float2* s, int t) {
   }
 }
 
+// Barrier among the T lanes that share a line: a warp barrier when the line
+// lives in one warp, else the named barrier `bar_id` (1..15) over T threads.
+template <int T>
+__device__ __forceinline__ void line_sync(int bar_id) {
+  if constexpr (T <= 32) {
+    __syncwarp();
+  } else {
+    asm volatile("bar.sync %0, %1;\n" ::"r"(bar_id), "n"(T) : "memory");
+  }
+}
+
 // Full line FFT.  On entry the line (natural order) is in the buffer s; on
 // exit the transform is in s (natural order).  All T lanes of the line call
-// this together; `sync` is the barrier among the lanes sharing s.
-// Lanes with act == false (no line of their own) only take part in the
-// warp barriers.
+// this together; lanes with act == false (no line of their own) only take
+// part in the barriers.  bar_id names the barrier of a line spread over
+// several warps.
 template <int N, int T, int SIGN, int S = 0>
-__device__ __forceinline__ void line_fft_smem(float2* s, int t, const float2* __restrict__ tw, bool act) {
+__device__ __forceinline__ void line_fft_smem(float2* s, int t, const float2* __restrict__ tw, bool act,
+                                              int bar_id = 1) {
   constexpr int E = N / T;
   constexpr int NS = num_stages(N, E);
   if constexpr (S < NS) {
@@ -209,17 +221,19 @@ __device__ __forceinline__ void line_fft_smem(float2* s, int t, const float2* __
     constexpr int Ns = stage_span(N, E, S);
     float2 v[E];
     if (act) stage_load<N, T, R>(v, s, t);
-    __syncwarp();
+    line_sync<T>(bar_id);
     if (act) {
       stage_compute<N, T, R, Ns, SIGN>(v, t, tw);
       stage_store<N, T, R, Ns>(v, s, t);
     }
-    __syncwarp();
-    line_fft_smem<N, T, SIGN, S + 1>(s, t, tw, act);
+    line_sync<T>(bar_id);
+    line_fft_smem<N, T, SIGN, S + 1>(s, t, tw, act, bar_id);
   }
 }
 
-// lanes per line and values per lane for a line of length N
-__host__ __device__ constexpr int lanes_for(int N) { return N >= 256 ? 32 : (N / 8 >= 1 ? (N / 8 < 32 ? N / 8 : 32) : 1); }
+// lanes per line: 16 values per lane for N >= 512, 8 below
+__host__ __device__ constexpr int lanes_for(int N) {
+  return N >= 512 ? N / 16 : (N / 8 >= 1 ? (N / 8 < 32 ? N / 8 : 32) : 1);
+}
 
 }  // namespace aar

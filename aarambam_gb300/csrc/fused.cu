@@ -110,26 +110,72 @@ __device__ __forceinline__ float mode_in(const ModalArgs& a, int n, const KCell&
 }
 
 // ----------------------------------------------------------- tile passes
+// Line stride of a tile in shared memory: at least the padded line length,
+// and = 2 (mod 16) float2 so that the 8 lines x 2 rows a half-warp touches
+// while moving a tile between global and shared memory fall in 32 distinct
+// banks.
+__host__ __device__ constexpr int tile_ls(int N) {
+  int base = N + N / 32;
+  return base + ((2 - base % 16) + 16) % 16;
+}
+
 template <int N, int W>
 struct AxisCfg {
-  static constexpr int T = lanes_for(N);
+  static constexpr int T = lanes_for(N);  // lanes per line (may span two warps)
   static constexpr int E = N / T;
-  static constexpr int LPW = 32 / T;  // lines per warp
-  static constexpr int WARPS = (W + LPW - 1) / LPW;
-  static constexpr int THREADS = WARPS * 32;
-  static constexpr int LS = spad_len(N);  // smem line stride (float2)
+  static constexpr int THREADS = ((W * T + 31) / 32) * 32;
+  static constexpr int WARPS = THREADS / 32;
+  static constexpr int LS = tile_ls(N);  // smem line stride (float2)
   static constexpr size_t SMEM = sizeof(float2) * (size_t)W * LS;
+  static constexpr int PER = N * W / THREADS;  // tile elements per thread
+  static constexpr int MINB = THREADS >= 512 ? 2 : 3;  // resident blocks per SM aimed at
 };
+
+// asynchronous global -> shared copies (sm_80+ cp.async), 8 bytes each
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+  unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int K>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(K) : "memory");
+}
+
+template <int AXIS>
+__device__ __forceinline__ int64_t tile_elem(int N, int HP, int o, int c0, int n, int w);
+
+// issue the asynchronous copy of a tile (rows along AXIS) into shared memory
+template <int N, int W, int AXIS>
+__device__ __forceinline__ void tile_load_async(float2* sm, const float2* __restrict__ f, int HP, int o, int c0) {
+  using C = AxisCfg<N, W>;
+#pragma unroll 4
+  for (int q = 0; q < C::PER; ++q) {
+    int e = threadIdx.x + C::THREADS * q;
+    int n = e / W, w = e % W;
+    cp_async8(sm + w * C::LS + spad(n), f + tile_elem<AXIS>(N, HP, o, c0, n, w));
+  }
+}
+
+template <int N, int W, int AXIS>
+__device__ __forceinline__ void tile_store(const float2* sm, float2* __restrict__ f, int HP, int o, int c0) {
+  using C = AxisCfg<N, W>;
+#pragma unroll 4
+  for (int q = 0; q < C::PER; ++q) {
+    int e = threadIdx.x + C::THREADS * q;
+    int n = e / W, w = e % W;
+    f[tile_elem<AXIS>(N, HP, o, c0, n, w)] = sm[w * C::LS + spad(n)];
+  }
+}
 
 // run the W line FFTs of a tile held in shared memory
 template <int N, int W, int SIGN>
 __device__ __forceinline__ void tile_fft(float2* sm, const float2* __restrict__ tw) {
   using C = AxisCfg<N, W>;
-  int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  int line = warp * C::LPW + lane / C::T;
-  int t = lane % C::T;
+  int line = threadIdx.x / C::T;
+  int t = threadIdx.x % C::T;
   bool act = line < W;
-  line_fft_smem<N, C::T, SIGN>(sm + (act ? line : 0) * C::LS, t, tw, act);
+  line_fft_smem<N, C::T, SIGN>(sm + (act ? line : 0) * C::LS, t, tw, act, 1 + (act ? line : 0));
 }
 
 // Tile indexing.  Axis 0 (x): rows n = x, other index o = y.  Axis 1 (y):
@@ -143,134 +189,118 @@ __device__ __forceinline__ int64_t tile_elem(int N, int HP, int o, int c0, int n
 // In-place complex pass along AXIS over fields [0, nf) of `base` (field
 // stride fs).  blockIdx.x = tile, blockIdx.y = field.
 template <int N, int W, int AXIS, int SIGN>
-__global__ void __launch_bounds__(AxisCfg<N, W>::THREADS) k_axis_inplace(float2* base, int64_t fs, int HP,
+__global__ void __launch_bounds__(AxisCfg<N, W>::THREADS, AxisCfg<N, W>::MINB) k_axis_inplace(float2* base, int64_t fs, int HP,
                                                                           const float2* __restrict__ tw) {
-  using C = AxisCfg<N, W>;
   extern __shared__ float2 sm[];
   int ncol = HP / W;
   int o = blockIdx.x / ncol, c0 = (blockIdx.x % ncol) * W;
   float2* f = base + (int64_t)blockIdx.y * fs;
-  for (int e = threadIdx.x; e < N * W; e += C::THREADS) {
-    int n = e / W, w = e % W;
-    sm[w * C::LS + spad(n)] = f[tile_elem<AXIS>(N, HP, o, c0, n, w)];
-  }
+  tile_load_async<N, W, AXIS>(sm, f, HP, o, c0);
+  cp_async_commit();
+  cp_async_wait<0>();
   __syncthreads();
   tile_fft<N, W, SIGN>(sm, tw);
   __syncthreads();
-  for (int e = threadIdx.x; e < N * W; e += C::THREADS) {
-    int n = e / W, w = e % W;
-    f[tile_elem<AXIS>(N, HP, o, c0, n, w)] = sm[w * C::LS + spad(n)];
-  }
+  tile_store<N, W, AXIS>(sm, f, HP, o, c0);
 }
 
 // In-place forward y pass over the active slots r = r_of_slot[blockIdx.y].
 template <int N, int W>
-__global__ void __launch_bounds__(AxisCfg<N, W>::THREADS) k_axis_slots(float2* base, int64_t fs, int HP,
+__global__ void __launch_bounds__(AxisCfg<N, W>::THREADS, AxisCfg<N, W>::MINB) k_axis_slots(float2* base, int64_t fs, int HP,
                                                                         const float2* __restrict__ tw,
                                                                         const DevTerms* __restrict__ dt) {
-  using C = AxisCfg<N, W>;
   extern __shared__ float2 sm[];
   int ncol = HP / W;
   int o = blockIdx.x / ncol, c0 = (blockIdx.x % ncol) * W;
   float2* f = base + (int64_t)dt->tl.r_of_slot[blockIdx.y] * fs;
-  for (int e = threadIdx.x; e < N * W; e += C::THREADS) {
-    int n = e / W, w = e % W;
-    sm[w * C::LS + spad(n)] = f[tile_elem<1>(N, HP, o, c0, n, w)];
-  }
+  tile_load_async<N, W, 1>(sm, f, HP, o, c0);
+  cp_async_commit();
+  cp_async_wait<0>();
   __syncthreads();
   tile_fft<N, W, -1>(sm, tw);
   __syncthreads();
-  for (int e = threadIdx.x; e < N * W; e += C::THREADS) {
-    int n = e / W, w = e % W;
-    f[tile_elem<1>(N, HP, o, c0, n, w)] = sm[w * C::LS + spad(n)];
-  }
+  tile_store<N, W, 1>(sm, f, HP, o, c0);
 }
 
-// First modal pass: field p = blockIdx.y gets the inverse x transform of
-// q_p(k) phi(k).  phi is read once per tile per p (the M reads of one tile
-// follow each other and hit L2).
+// First modal pass: field p gets the inverse x transform of q_p(k) phi(k),
+// q_p from the per-|k|^2 table (FP64 host evaluation of main.c:606-637).
+// The M blocks of one tile follow each other, so phi is read from HBM once.
 template <int N, int W>
-__global__ void __launch_bounds__(AxisCfg<N, W>::THREADS) k_modal_xinv(ModalArgs a, const float2* __restrict__ phi,
+__global__ void __launch_bounds__(AxisCfg<N, W>::THREADS, AxisCfg<N, W>::MINB) k_modal_xinv(ModalArgs a, const float2* __restrict__ phi,
                                                                         float2* work, int64_t fs, int HP,
-                                                                        const float2* __restrict__ tw) {
+                                                                        const float2* __restrict__ tw,
+                                                                        const float* __restrict__ qtab, int64_t nsq) {
   using C = AxisCfg<N, W>;
   extern __shared__ float2 sm[];
   int ncol = HP / W;
   int tile = blockIdx.x / a.M, p = blockIdx.x % a.M;
   int o = tile / ncol, c0 = (tile % ncol) * W;
   const int ky = sidx(o, N);
-  for (int e = threadIdx.x; e < N * W; e += C::THREADS) {
+  const float* q = qtab + (int64_t)p * nsq;
+#pragma unroll 4
+  for (int i = 0; i < C::PER; ++i) {
+    int e = threadIdx.x + C::THREADS * i;
     int n = e / W, w = e % W;
-    int kz = c0 + w;
+    int kz = c0 + w, kx = sidx(n, N);
     float2 v = make_float2(0.f, 0.f);
-    if (kz <= N / 2) {
-      KCell c = kcell(a, sidx(n, N), ky, kz);
-      if (c.keep) {
-        float q = mode_in(a, p, c);
-        float2 ph = phi[tile_elem<0>(N, HP, o, c0, n, w)];
-        v = make_float2(ph.x * q, ph.y * q);
-      }
+    int n2 = kx * kx + ky * ky + kz * kz;
+    if (kz <= N / 2 && n2 != 0 && keep_cell(a.g, kx, ky, kz)) {
+      float qq = __ldg(q + n2);
+      float2 ph = __ldg(phi + tile_elem<0>(N, HP, o, c0, n, w));
+      v = make_float2(ph.x * qq, ph.y * qq);
     }
     sm[w * C::LS + spad(n)] = v;
   }
   __syncthreads();
   tile_fft<N, W, +1>(sm, tw);
   __syncthreads();
-  float2* f = work + (int64_t)p * fs;
-  for (int e = threadIdx.x; e < N * W; e += C::THREADS) {
-    int n = e / W, w = e % W;
-    f[tile_elem<0>(N, HP, o, c0, n, w)] = sm[w * C::LS + spad(n)];
-  }
+  tile_store<N, W, 0>(sm, work + (int64_t)p * fs, HP, o, c0);
 }
 
 // Last modal pass: for each active r, forward x transform of slot r, times
-// rho_r(k), summed (Neumaier-compensated) over r; then
-// phi <- phi + fnl_n3 * acc, DC = 0 (main.c:1101-1126).
+// rho_r(k) (per-|k|^2 table), summed over r with Neumaier compensation (sum
+// and compensation interleaved in shared memory, one float4 per element);
+// then phi <- phi + fnl_n3 * acc, DC = 0 (main.c:1101-1126).
 template <int N, int W>
-__global__ void __launch_bounds__(AxisCfg<N, W>::THREADS) k_modal_xacc(ModalArgs a, float2* phi, const float2* work,
-                                                                        int64_t fs, int HP, float fnl_n3,
-                                                                        const float2* __restrict__ tw,
-                                                                        const DevTerms* __restrict__ dt) {
+__global__ void __launch_bounds__(AxisCfg<N, W>::THREADS, AxisCfg<N, W>::THREADS >= 512 ? 1 : 2) k_modal_xacc(ModalArgs a, float2* phi,
+                                                                           const float2* work, int64_t fs, int HP,
+                                                                           float fnl_n3, const float2* __restrict__ tw,
+                                                                           const DevTerms* __restrict__ dt,
+                                                                           const float* __restrict__ rtab,
+                                                                           int64_t nsq) {
   using C = AxisCfg<N, W>;
   extern __shared__ float2 sm[];
-  float2* acc = sm + W * C::LS;
-  float2* cmp = acc + W * C::LS;
+  float4* acc = (float4*)(sm + W * C::LS);  // (sum.x, sum.y, comp.x, comp.y) per tile element
   int ncol = HP / W;
   int o = blockIdx.x / ncol, c0 = (blockIdx.x % ncol) * W;
   const int ky = sidx(o, N);
-  for (int e = threadIdx.x; e < N * W; e += C::THREADS) {
-    int n = e / W, w = e % W;
-    acc[w * C::LS + spad(n)] = make_float2(0.f, 0.f);
-    cmp[w * C::LS + spad(n)] = make_float2(0.f, 0.f);
-  }
+  for (int e = threadIdx.x; e < N * W; e += C::THREADS) acc[e] = make_float4(0.f, 0.f, 0.f, 0.f);
   const int nr = dt->tl.nr;
   for (int sl = 0; sl < nr; ++sl) {
-    int r = dt->tl.r_of_slot[sl];
-    const float2* f = work + (int64_t)r * fs;
+    const int r = dt->tl.r_of_slot[sl];
     __syncthreads();
-    for (int e = threadIdx.x; e < N * W; e += C::THREADS) {
-      int n = e / W, w = e % W;
-      sm[w * C::LS + spad(n)] = f[tile_elem<0>(N, HP, o, c0, n, w)];
-    }
+    tile_load_async<N, W, 0>(sm, work + (int64_t)r * fs, HP, o, c0);
+    cp_async_commit();
+    cp_async_wait<0>();
     __syncthreads();
     tile_fft<N, W, -1>(sm, tw);
     __syncthreads();
+    const float* rt = rtab + (int64_t)r * nsq;
     for (int e = threadIdx.x; e < N * W; e += C::THREADS) {
       int n = e / W, w = e % W;
-      int kz = c0 + w;
-      if (kz > N / 2) continue;
-      KCell c = kcell(a, sidx(n, N), ky, kz);
-      if (!c.keep) continue;
-      float rho = mode_out(a, r, c);
+      int kz = c0 + w, kx = sidx(n, N);
+      int n2 = kx * kx + ky * ky + kz * kz;
+      if (kz > N / 2 || n2 == 0 || !keep_cell(a.g, kx, ky, kz)) continue;
+      float rho = __ldg(rt + n2);
       float2 v = sm[w * C::LS + spad(n)];
-      int idx = w * C::LS + spad(n);
-      float2 s0 = acc[idx], cc = cmp[idx];
+      float4 s4 = acc[e];
       float tx = v.x * rho, ty = v.y * rho;
-      float sx = s0.x + tx, sy = s0.y + ty;
-      cc.x += (fabsf(s0.x) >= fabsf(tx)) ? (s0.x - sx) + tx : (tx - sx) + s0.x;
-      cc.y += (fabsf(s0.y) >= fabsf(ty)) ? (s0.y - sy) + ty : (ty - sy) + s0.y;
-      acc[idx] = make_float2(sx, sy);
-      cmp[idx] = cc;
+      float sx = s4.x + tx, sy = s4.y + ty;
+      s4.z += (fabsf(s4.x) >= fabsf(tx)) ? (s4.x - sx) + tx : (tx - sx) + s4.x;
+      s4.w += (fabsf(s4.y) >= fabsf(ty)) ? (s4.y - sy) + ty : (ty - sy) + s4.y;
+      s4.x = sx;
+      s4.y = sy;
+      acc[e] = s4;
     }
   }
   __syncthreads();
@@ -279,11 +309,10 @@ __global__ void __launch_bounds__(AxisCfg<N, W>::THREADS) k_modal_xacc(ModalArgs
     int kz = c0 + w;
     if (kz > N / 2) continue;
     int64_t gi = tile_elem<0>(N, HP, o, c0, n, w);
-    int idx = w * C::LS + spad(n);
-    float2 s0 = acc[idx], cc = cmp[idx];
     float2 ph = phi[gi];
-    ph.x += fnl_n3 * (s0.x + cc.x);
-    ph.y += fnl_n3 * (s0.y + cc.y);
+    float4 s4 = acc[e];
+    ph.x += fnl_n3 * (s4.x + s4.z);
+    ph.y += fnl_n3 * (s4.y + s4.w);
     if (n == 0 && o == 0 && kz == 0) ph = make_float2(0.f, 0.f);
     phi[gi] = ph;
   }
@@ -353,7 +382,7 @@ __device__ __forceinline__ void row_r2c_post(const float2* line, float2* __restr
 // input fields (slots in_slot[]), a per-position combine step Op, r2c of
 // `nout` output lines into slots out_slot[].  One warp per line at a time.
 template <int N, class Op>
-__global__ void __launch_bounds__(256) k_rows(Op op, float2* work, int64_t fs, int HP,
+__global__ void __launch_bounds__(512, 1) k_rows(Op op, float2* work, int64_t fs, int HP,
                                               const float2* __restrict__ twN, const float2* __restrict__ twH) {
   using C = RowCfg<N>;
   constexpr int H = C::H;
@@ -395,26 +424,35 @@ struct ModalRowOp {
   __device__ int nout() const { return dt->tl.nr; }
   __device__ int out_line(int l) const { return dt->tl.r_of_slot[l]; }
   __device__ int out_slot(int l) const { return dt->tl.r_of_slot[l]; }
+  // Slots in descending r: g_r only needs f_p f_q with p <= q <= r, so once
+  // g_r is formed nothing later reads f_r and it is stored over it at once.
+  // (The counter-term f_0 f_2 -> g_1 reads f_2 after g_2 has replaced it;
+  // that term is evaluated first, in the pass for r = 2, into a register.)
   __device__ void combine(float2* sm, int n, int LS) const {
-    float2 g[kMaxModes];
     const int nr = dt->tl.nr;
-#pragma unroll
-    for (int s = 0; s < kMaxModes; ++s) {
-      if (s < nr) {
-        float2 acc = make_float2(0.f, 0.f);
-        const int tb = dt->tl.begin[s], te = dt->tl.begin[s + 1];
-        for (int t = tb; t < te; ++t) {
-          Term tm = dt->t[t];
-          float2 fp = sm[tm.p * LS + spad(n)], fq = sm[tm.q * LS + spad(n)];
-          acc.x += tm.c * fp.x * fq.x;
-          acc.y += tm.c * fp.y * fq.y;
+    float2 g1_extra = make_float2(0.f, 0.f);
+    for (int s = nr - 1; s >= 0; --s) {
+      const int r = dt->tl.r_of_slot[s];
+      float2 acc = make_float2(0.f, 0.f);
+      const int tb = dt->tl.begin[s], te = dt->tl.begin[s + 1];
+      for (int t = tb; t < te; ++t) {
+        Term tm = dt->t[t];
+        float2 fp = sm[tm.p * LS + spad(n)], fq = sm[tm.q * LS + spad(n)];
+        float2 v = make_float2(tm.c * fp.x * fq.x, tm.c * fp.y * fq.y);
+        if (tm.r == r) {
+          acc.x += v.x;
+          acc.y += v.y;
+        } else {  // a term stored early (its r is below this slot's)
+          g1_extra.x += v.x;
+          g1_extra.y += v.y;
         }
-        g[s] = acc;
       }
+      if (r == 1) {
+        acc.x += g1_extra.x;
+        acc.y += g1_extra.y;
+      }
+      sm[r * LS + spad(n)] = acc;
     }
-#pragma unroll
-    for (int s = 0; s < kMaxModes; ++s)
-      if (s < nr) sm[dt->tl.r_of_slot[s] * LS + spad(n)] = g[s];
   }
 };
 
@@ -664,7 +702,7 @@ struct Launch {
   static constexpr int W = 8;
   static int configure(Plan* p) {
     using A = AxisCfg<N, W>;
-    size_t sm_axis = A::SMEM, sm_acc = 3 * A::SMEM;
+    size_t sm_axis = A::SMEM, sm_acc = A::SMEM + sizeof(float4) * N * W;
     AAR_CUDA_TRY(p, cudaFuncSetAttribute(k_axis_inplace<N, W, 0, +1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_axis));
     AAR_CUDA_TRY(p, cudaFuncSetAttribute(k_axis_inplace<N, W, 1, +1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_axis));
     AAR_CUDA_TRY(p, cudaFuncSetAttribute(k_axis_inplace<N, W, 0, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_axis));
@@ -700,7 +738,8 @@ struct Launch {
     int64_t fs = (int64_t)N * N * p->HP;
     unsigned tiles = (unsigned)(N * (p->HP / W));
     { ProfScope ps_(p, "modal_xinv", st);
-    k_modal_xinv<N, W><<<tiles * a.M, A::THREADS, A::SMEM, st>>>(a, p->d_phik, p->d_work, fs, p->HP, p->d_twN);
+    k_modal_xinv<N, W><<<tiles * a.M, A::THREADS, A::SMEM, st>>>(a, p->d_phik, p->d_work, fs, p->HP, p->d_twN,
+                                                                  p->d_qtab, p->nsq);
     }
     AAR_CUDA_TRY(p, cudaGetLastError());
     p->last_launches += 1;
@@ -709,7 +748,7 @@ struct Launch {
     size_t sm_rows = sizeof(float2) * (size_t)(a.M + 1) * RowCfg<N>::LS;
     ModalRowOp op{a.M, (const DevTerms*)p->d_terms};
     { ProfScope ps_(p, "modal_rows", st);
-    k_rows<N, ModalRowOp><<<(unsigned)((int64_t)N * N), 256, sm_rows, st>>>(op, p->d_work, fs, p->HP, p->d_twN, p->d_twH);
+    k_rows<N, ModalRowOp><<<(unsigned)((int64_t)N * N), 512, sm_rows, st>>>(op, p->d_work, fs, p->HP, p->d_twN, p->d_twH);
     }
     AAR_CUDA_TRY(p, cudaGetLastError());
     p->last_launches += 1;
@@ -725,8 +764,8 @@ struct Launch {
     }
     float fnl_n3 = (float)(p->prm.fnl / ((double)N * N * N));
     { ProfScope ps_(p, "modal_xacc", st);
-    k_modal_xacc<N, W><<<tiles, A::THREADS, 3 * A::SMEM, st>>>(a, p->d_phik, p->d_work, fs, p->HP, fnl_n3, p->d_twN,
-                                                                  (const DevTerms*)p->d_terms);
+    k_modal_xacc<N, W><<<tiles, A::THREADS, A::SMEM + sizeof(float4) * N * W, st>>>(a, p->d_phik, p->d_work, fs, p->HP, fnl_n3, p->d_twN,
+                                                                  (const DevTerms*)p->d_terms, p->d_rtab, p->nsq);
     }
     AAR_CUDA_TRY(p, cudaGetLastError());
     p->last_launches += 1;
@@ -825,7 +864,9 @@ static int build_terms(Plan* p) {
     double t012 = -A(1, 1, 1) / A(0, 1, 2);
     double c = A(0, 1, 2) * t012;
     by_r[2].push_back(Term{0, 1, 2, (float)(-c)});
-    by_r[1].push_back(Term{0, 2, 1, (float)(c)});
+    // f_0 f_2 -> g_1 is evaluated in the r = 2 pass (before g_2 replaces f_2)
+    by_r[2].push_back(Term{0, 2, 1, (float)(c)});
+    if (by_r[1].empty()) by_r[1].push_back(Term{0, 0, 1, 0.f});  // keep a slot for r = 1
   }
   TermList tl{};
   std::vector<Term> flat;

@@ -39,6 +39,7 @@ WORKLOADS = {
     # name: (Nmesh, Box, table, N_modes, Nmax, Fnl)
     "scalarI_m20_n1024": (1024, 1000.0, "scalarI_m20_L1000_n1024", 20, 1024, 100.0),
     "scalarI_m12_n512": (512, 1000.0, "scalarI_m12_L1000_n512", 12, 512, 100.0),
+    "scalarI_m12_n256": (256, 1000.0, "scalarI_m12_L1000_n512", 12, 512, 100.0),
     "local_m8_n128": (128, 500.0, "local_m8_L500_n128", 8, 128, 10.0),
 }
 
@@ -53,6 +54,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-n", type=int, default=128)
+    ap.add_argument("--plain", action="store_true", help="also time the plain FP64 cuFFT form (1 step)")
     return ap.parse_args()
 
 
@@ -311,6 +313,25 @@ def gpu_arm(args):
         e2e = {"value": world * ks * npart / te, "unit": UNIT, "h2d_bytes_per_step": 12 * npart,
                "d2h_bytes_per_step": 24 * npart, "steps": ks, "api": "aar_run_host (C ABI, pinned host buffers)"}
 
+    plain = None
+    if args.plain:
+        del gen
+        torch.cuda.empty_cache()
+        gp = ICGenerator(cfg, alpha, x0, k, t, precision="fp64")
+        gp.run(lagr, pos, vel)  # warm-up (plans, tables)
+        barrier()
+        p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        p0.record(stream)
+        gp.run(lagr, pos, vel)
+        p1.record(stream)
+        barrier()
+        tp = p0.elapsed_time(p1) / 1e3
+        plain = {"value": npart / tp, "unit": UNIT, "ms_per_step": 1e3 * tp, "steps": 1,
+                 "fused_speedup": round(tp / (elapsed / args.steps), 2),
+                 "form": "cuFFT Z2D/D2Z FP64 + separate pointwise kernels, reference loop structure"}
+        del gp
+        torch.cuda.empty_cache()
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(args.workload, args.cpu_sample_n)
@@ -323,7 +344,7 @@ def gpu_arm(args):
                                       f"{cfg['table']} ({M} modes, {R} active r), Fnl={cfg['Fnl']}, BBKS T(k), "
                                       f"z=49", "nmesh": N, "n_modes": M, "l2": "working set >> L2 (no flush)",
                           "parallelism": "replicas" if world > 1 else "single GPU"},
-               "roofline": roofline, "path_roofline": path_roof, "cpu_baseline": cpu, "e2e": e2e,
+               "roofline": roofline, "path_roofline": path_roof, "cpu_baseline": cpu, "e2e": e2e, "plain_fp64": plain,
                "gpu_launches": launches, "clocks": clocks, "kernels": kernels}
         print(json.dumps(out))
     if world > 1:

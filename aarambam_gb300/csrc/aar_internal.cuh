@@ -62,6 +62,7 @@ struct Plan {
   bool have_tables = false, have_transfer = false;
   // device resources (fused FP32 form)
   int dev = -1;
+  int num_sms = 0;            // multiprocessors of the plan's device
   float2* d_phik = nullptr;   // Gaussian / total potential spectrum [N][N][HP]
   float2* d_work = nullptr;   // nwork fields [N][N][HP]
   int nwork = 0;
@@ -70,6 +71,7 @@ struct Plan {
   float2* d_twH = nullptr;    // exp(-2 pi i m / (N/2)), m < N/2
   float* d_amp = nullptr;     // per n^2 noise amplitude
   float* d_twb = nullptr;     // per n^2 T(k) / (Dplus Beta)
+  float* d_sinc = nullptr;    // per grid index: CIC window sin(x)/x
   float* d_qtab = nullptr;    // [M][nsq] field filters q_p per n^2
   float* d_rtab = nullptr;    // [M][nsq] radial parts rho_r per n^2
   int64_t nsq = 0;            // 3 (N/2)^2 + 1

@@ -232,7 +232,7 @@ static void plan_release(Plan* p) {
   p->prof.clear();
   for (auto e : p->event_pool) cudaEventDestroy(e);
   p->event_pool.clear();
-  void* ptrs[] = {p->d_phik, p->d_work, p->d_seed, p->d_twN, p->d_twH, p->d_amp, p->d_twb, p->d_rlxpow, p->d_terms, p->d_io, p->d_qtab, p->d_rtab};
+  void* ptrs[] = {p->d_phik, p->d_work, p->d_seed, p->d_twN, p->d_twH, p->d_amp, p->d_twb, p->d_rlxpow, p->d_terms, p->d_io, p->d_qtab, p->d_rtab, p->d_sinc};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   p->d_phik = p->d_work = nullptr;
@@ -332,6 +332,7 @@ static int create(Plan* p) {
   if (!(q.box > 0) || q.nsample <= 0) return set_err(p, "Box and Nsample must be positive"), AAR_ERR_ARG;
   if (q.seed < 0) return set_err(p, "Seed must be >= 0"), AAR_ERR_ARG;
   AAR_CUDA_TRY(p, cudaGetDevice(&p->dev));
+  AAR_CUDA_TRY(p, cudaDeviceGetAttribute(&p->num_sms, cudaDevAttrMultiProcessorCount, p->dev));
   p->N = N;
   p->HP = ((N / 2 + 1) + 7) / 8 * 8;
   p->grid.N = N;
@@ -374,6 +375,18 @@ static int create(Plan* p) {
     int64_t nsq = 3LL * (N / 2) * (N / 2) + 1;
     if ((rc = plan_alloc(p, (void**)&p->d_amp, sizeof(float) * nsq))) return rc;
     if ((rc = plan_alloc(p, (void**)&p->d_twb, sizeof(float) * nsq))) return rc;
+    // CIC window per grid index, the reference's expression (main.c:1334-1349)
+    std::vector<float> sinc(N);
+    for (int i = 0; i < N; ++i) {
+      double kv = sidx(i, N) * 2 * kPi / q.box, f = 1;
+      if (kv != 0) {
+        f = (kv * q.box / 2) / N;
+        f = sin(f) / f;
+      }
+      sinc[i] = (float)f;
+    }
+    if ((rc = plan_alloc(p, (void**)&p->d_sinc, sizeof(float) * N))) return rc;
+    AAR_CUDA_TRY(p, cudaMemcpy(p->d_sinc, sinc.data(), sizeof(float) * N, cudaMemcpyHostToDevice));
   }
   return AAR_OK;
 }
@@ -514,6 +527,15 @@ int aar_stage_readout(aar_plan* h, const float* d_lagr, int64_t npart, float* d_
   p->last_launches = 0;
   if (p->prm.precision != AAR_FUSED_FP32) return set_err(p, "stage calls are for the fused form"), AAR_ERR_ARG;
   return fused_readout(p, d_lagr, npart, d_pos, d_vel, S(stream));
+}
+
+int aar_stage_readout_glass(aar_plan* h, const float* d_glass, int64_t nglass, double glass_box, int32_t tile,
+                            float* d_pos, float* d_vel, int32_t* d_ids, void* stream) {
+  if (!h || nglass < 0 || tile < 1 || !(glass_box > 0)) return AAR_ERR_ARG;
+  Plan* p = &h->p;
+  if (p->prm.precision != AAR_FUSED_FP32) return set_err(p, "stage calls are for the fused form"), AAR_ERR_ARG;
+  p->last_launches = 0;
+  return fused_readout_glass(p, d_glass, nglass, glass_box, tile, d_pos, d_vel, d_ids, S(stream));
 }
 
 int aar_run(aar_plan* h, const float* d_lagr, int64_t npart, float* d_pos, float* d_vel, void* stream) {

@@ -24,6 +24,8 @@
 #include <math.h>
 #include <stdint.h>
 
+#include <stddef.h>
+
 #include <algorithm>
 #include <vector>
 
@@ -184,77 +186,6 @@ template <int AXIS>
 __device__ __forceinline__ int64_t tile_elem(int N, int HP, int o, int c0, int n, int w) {
   if (AXIS == 0) return ((int64_t)n * N + o) * HP + c0 + w;
   return ((int64_t)o * N + n) * HP + c0 + w;
-}
-
-// In-place complex pass along AXIS over fields [0, nf) of `base` (field
-// stride fs).  blockIdx.x = tile, blockIdx.y = field.
-template <int N, int W, int AXIS, int SIGN>
-__global__ void __launch_bounds__(AxisCfg<N, W>::THREADS, AxisCfg<N, W>::MINB) k_axis_inplace(float2* base, int64_t fs, int HP,
-                                                                          const float2* __restrict__ tw) {
-  extern __shared__ float2 sm[];
-  int ncol = HP / W;
-  int o = blockIdx.x / ncol, c0 = (blockIdx.x % ncol) * W;
-  float2* f = base + (int64_t)blockIdx.y * fs;
-  tile_load_async<N, W, AXIS>(sm, f, HP, o, c0);
-  cp_async_commit();
-  cp_async_wait<0>();
-  __syncthreads();
-  tile_fft<N, W, SIGN>(sm, tw);
-  __syncthreads();
-  tile_store<N, W, AXIS>(sm, f, HP, o, c0);
-}
-
-// In-place forward y pass over the active slots r = r_of_slot[blockIdx.y].
-template <int N, int W>
-__global__ void __launch_bounds__(AxisCfg<N, W>::THREADS, AxisCfg<N, W>::MINB) k_axis_slots(float2* base, int64_t fs, int HP,
-                                                                        const float2* __restrict__ tw,
-                                                                        const DevTerms* __restrict__ dt) {
-  extern __shared__ float2 sm[];
-  int ncol = HP / W;
-  int o = blockIdx.x / ncol, c0 = (blockIdx.x % ncol) * W;
-  float2* f = base + (int64_t)dt->tl.r_of_slot[blockIdx.y] * fs;
-  tile_load_async<N, W, 1>(sm, f, HP, o, c0);
-  cp_async_commit();
-  cp_async_wait<0>();
-  __syncthreads();
-  tile_fft<N, W, -1>(sm, tw);
-  __syncthreads();
-  tile_store<N, W, 1>(sm, f, HP, o, c0);
-}
-
-// First modal pass: field p gets the inverse x transform of q_p(k) phi(k),
-// q_p from the per-|k|^2 table (FP64 host evaluation of main.c:606-637).
-// The M blocks of one tile follow each other, so phi is read from HBM once.
-template <int N, int W>
-__global__ void __launch_bounds__(AxisCfg<N, W>::THREADS, AxisCfg<N, W>::MINB) k_modal_xinv(ModalArgs a, const float2* __restrict__ phi,
-                                                                        float2* work, int64_t fs, int HP,
-                                                                        const float2* __restrict__ tw,
-                                                                        const float* __restrict__ qtab, int64_t nsq) {
-  using C = AxisCfg<N, W>;
-  extern __shared__ float2 sm[];
-  int ncol = HP / W;
-  int tile = blockIdx.x / a.M, p = blockIdx.x % a.M;
-  int o = tile / ncol, c0 = (tile % ncol) * W;
-  const int ky = sidx(o, N);
-  const float* q = qtab + (int64_t)p * nsq;
-#pragma unroll 4
-  for (int i = 0; i < C::PER; ++i) {
-    int e = threadIdx.x + C::THREADS * i;
-    int n = e / W, w = e % W;
-    int kz = c0 + w, kx = sidx(n, N);
-    float2 v = make_float2(0.f, 0.f);
-    int n2 = kx * kx + ky * ky + kz * kz;
-    if (kz <= N / 2 && n2 != 0 && keep_cell(a.g, kx, ky, kz)) {
-      float qq = __ldg(q + n2);
-      float2 ph = __ldg(phi + tile_elem<0>(N, HP, o, c0, n, w));
-      v = make_float2(ph.x * qq, ph.y * qq);
-    }
-    sm[w * C::LS + spad(n)] = v;
-  }
-  __syncthreads();
-  tile_fft<N, W, +1>(sm, tw);
-  __syncthreads();
-  tile_store<N, W, 0>(sm, work + (int64_t)p * fs, HP, o, c0);
 }
 
 // Last modal pass: for each active r, forward x transform of slot r, times
@@ -499,112 +430,16 @@ __global__ void __launch_bounds__(256) k_rows_c2r(float2* work, int64_t fs, int 
 
 // ----------------------------------------------------------- 2LPT passes
 struct LptArgs {
-  ModalArgs m;      // grid and k helpers
-  float inv_Dbeta;  // 1 / (Dplus Beta)
-  const float* twb; // per n^2: T(k) / (Dplus Beta)
+  ModalArgs m;       // grid and k helpers
+  float inv_Dbeta;   // 1 / (Dplus Beta)
+  const float* twb;  // per n^2: T(k) / (Dplus Beta)
+  const float* sinc; // per grid index: sin(x)/x, x = k Box / 2N (1 at k = 0)
   float box_over_2n;
 };
 
 __device__ __forceinline__ float sincf(float x) { return x == 0.f ? 1.f : sinf(x) / x; }
 
-// Hessian c = blockIdx.x % 6 of the ZA displacement (main.c:1238-1277):
-// d_ab = -k_a k_b T/(D Beta) phi, then the inverse x transform.
-template <int N, int W>
-__global__ void __launch_bounds__(AxisCfg<N, W>::THREADS) k_lpt_xinv_hess(LptArgs a, const float2* __restrict__ phi,
-                                                                           float2* work, int64_t fs, int HP,
-                                                                           const float2* __restrict__ tw) {
-  using C = AxisCfg<N, W>;
-  extern __shared__ float2 sm[];
-  const int pa[6] = {0, 0, 0, 1, 1, 2}, pb[6] = {0, 1, 2, 1, 2, 2};
-  int ncol = HP / W;
-  int tile = blockIdx.x / 6, comp = blockIdx.x % 6;
-  int o = tile / ncol, c0 = (tile % ncol) * W;
-  const int ky = sidx(o, N);
-  const float kF = a.m.g.kF;
-  for (int e = threadIdx.x; e < N * W; e += C::THREADS) {
-    int n = e / W, w = e % W;
-    int kz = c0 + w;
-    float2 v = make_float2(0.f, 0.f);
-    if (kz <= N / 2) {
-      int kv[3] = {sidx(n, N), ky, kz};
-      int n2 = kv[0] * kv[0] + kv[1] * kv[1] + kv[2] * kv[2];
-      float t = __ldg(a.twb + n2);
-      float f = -(kF * kv[pa[comp]]) * (kF * kv[pb[comp]]) * t;
-      float2 ph = phi[tile_elem<0>(N, HP, o, c0, n, w)];
-      v = make_float2(ph.x * f, ph.y * f);
-    }
-    sm[w * C::LS + spad(n)] = v;
-  }
-  __syncthreads();
-  tile_fft<N, W, +1>(sm, tw);
-  __syncthreads();
-  float2* f = work + (int64_t)comp * fs;
-  for (int e = threadIdx.x; e < N * W; e += C::THREADS) {
-    int n = e / W, w = e % W;
-    f[tile_elem<0>(N, HP, o, c0, n, w)] = sm[w * C::LS + spad(n)];
-  }
-}
-
-// Displacement spectra and the inverse x transform (main.c:1180-1216,
-// 1311-1368): comp 0..2 = ZA psi1_a = i k_a T/(D Beta) phi * smth; comp 3..5
-// = psi2_a = -i k_a / k^2 S * smth with S from the forward x transform of
-// the source slot.  Output slots 0..5.
-template <int N, int W>
-__global__ void __launch_bounds__(AxisCfg<N, W>::THREADS) k_lpt_xmid(LptArgs a, const float2* __restrict__ phi,
-                                                                      float2* work, int64_t fs, int HP, int src_slot,
-                                                                      const float2* __restrict__ tw) {
-  using C = AxisCfg<N, W>;
-  extern __shared__ float2 sm[];
-  int ncol = HP / W;
-  int tile = blockIdx.x / 6, comp = blockIdx.x % 6;
-  int o = tile / ncol, c0 = (tile % ncol) * W;
-  const int ky = sidx(o, N);
-  const float kF = a.m.g.kF;
-  const int ax = comp % 3;
-  if (comp >= 3) {
-    const float2* s = work + (int64_t)src_slot * fs;
-    for (int e = threadIdx.x; e < N * W; e += C::THREADS) {
-      int n = e / W, w = e % W;
-      sm[w * C::LS + spad(n)] = s[tile_elem<0>(N, HP, o, c0, n, w)];
-    }
-    __syncthreads();
-    tile_fft<N, W, -1>(sm, tw);
-    __syncthreads();
-  }
-  for (int e = threadIdx.x; e < N * W; e += C::THREADS) {
-    int n = e / W, w = e % W;
-    int kz = c0 + w;
-    float2 v = make_float2(0.f, 0.f);
-    if (kz <= N / 2) {
-      int kv[3] = {sidx(n, N), ky, kz};
-      int n2 = kv[0] * kv[0] + kv[1] * kv[1] + kv[2] * kv[2];
-      float fx = sincf(kF * kv[0] * a.box_over_2n), fy = sincf(kF * kv[1] * a.box_over_2n),
-            fz = sincf(kF * kv[2] * a.box_over_2n);
-      float ff = 1.f / (fx * fy * fz);
-      float smth = ff * ff;
-      float ka = kF * kv[ax];
-      if (comp < 3) {
-        float2 ph = phi[tile_elem<0>(N, HP, o, c0, n, w)];
-        float f = ka * __ldg(a.twb + n2) * smth;
-        v = make_float2(-f * ph.y, f * ph.x);
-      } else if (n2 > 0) {
-        float2 s = sm[w * C::LS + spad(n)];
-        float k2 = kF * kF * (float)n2;
-        float f = ka / k2 * smth;
-        v = make_float2(f * s.y, -f * s.x);
-      }
-    }
-    sm[w * C::LS + spad(n)] = v;
-  }
-  __syncthreads();
-  tile_fft<N, W, +1>(sm, tw);
-  __syncthreads();
-  float2* f = work + (int64_t)comp * fs;
-  for (int e = threadIdx.x; e < N * W; e += C::THREADS) {
-    int n = e / W, w = e % W;
-    f[tile_elem<0>(N, HP, o, c0, n, w)] = sm[w * C::LS + spad(n)];
-  }
-}
+#include "passes.cuh"
 
 // ----------------------------------------------------------- read-out
 // Trilinear read-out (main.c:1440-1516).  Fields: slots 0..5 of `work` as
@@ -697,121 +532,109 @@ __global__ void k_readout_glass(ReadArgs a, const float* __restrict__ F, const f
 }
 
 // ----------------------------------------------------------- host side
+// Launch a persistent pass: as many blocks as fit on the device at once.
+template <int N, class Op>
+static int run_pass(Plan* p, const Op& op, int64_t nitems, cudaStream_t st, const char* name) {
+  constexpr int W = 8;
+  using A = AxisCfg<N, W>;
+  auto kern = k_pass<N, W, Op>;
+  const size_t smem = A::SMEM;
+  AAR_CUDA_TRY(p, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  if (nitems < 1) return AAR_OK;
+  if (nitems > 0x7fffffff) return set_err(p, std::string(name) + ": too many work items"), AAR_ERR_ARG;
+  {
+    ProfScope ps_(p, name, st);
+    kern<<<(unsigned)nitems, A::THREADS, smem, st>>>(op, p->d_twN);
+  }
+  AAR_CUDA_TRY(p, cudaGetLastError());
+  p->last_launches += 1;
+  return AAR_OK;
+}
+
 template <int N>
 struct Launch {
   static constexpr int W = 8;
+  static int64_t tiles(Plan* p) { return (int64_t)N * (p->HP / W); }
+  static int64_t fstride(Plan* p) { return (int64_t)N * N * p->HP; }
+  static const int* slot_map(Plan* p) {
+    return (const int*)((const char*)p->d_terms + offsetof(DevTerms, tl) + offsetof(TermList, r_of_slot));
+  }
   static int configure(Plan* p) {
     using A = AxisCfg<N, W>;
-    size_t sm_axis = A::SMEM, sm_acc = A::SMEM + sizeof(float4) * N * W;
-    AAR_CUDA_TRY(p, cudaFuncSetAttribute(k_axis_inplace<N, W, 0, +1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_axis));
-    AAR_CUDA_TRY(p, cudaFuncSetAttribute(k_axis_inplace<N, W, 1, +1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_axis));
-    AAR_CUDA_TRY(p, cudaFuncSetAttribute(k_axis_inplace<N, W, 0, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_axis));
-    AAR_CUDA_TRY(p, cudaFuncSetAttribute(k_axis_inplace<N, W, 1, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_axis));
-    AAR_CUDA_TRY(p, cudaFuncSetAttribute(k_modal_xinv<N, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_axis));
-    AAR_CUDA_TRY(p, cudaFuncSetAttribute(k_axis_slots<N, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_axis));
+    size_t sm_acc = A::SMEM + sizeof(float4) * N * W;
     AAR_CUDA_TRY(p, cudaFuncSetAttribute(k_modal_xacc<N, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_acc));
-    AAR_CUDA_TRY(p, cudaFuncSetAttribute(k_lpt_xinv_hess<N, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_axis));
-    AAR_CUDA_TRY(p, cudaFuncSetAttribute(k_lpt_xmid<N, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_axis));
     size_t sm_rows = sizeof(float2) * (size_t)(kMaxModes + 1) * RowCfg<N>::LS;
     AAR_CUDA_TRY(p, cudaFuncSetAttribute(k_rows<N, ModalRowOp>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_rows));
     AAR_CUDA_TRY(p, cudaFuncSetAttribute(k_rows<N, SourceRowOp>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_rows));
     return AAR_OK;
   }
-  static int ypass(Plan* p, int nf, int sign, cudaStream_t st, const char* name) {
-    using A = AxisCfg<N, W>;
-    dim3 grid((unsigned)(N * (p->HP / W)), (unsigned)nf);
-    int64_t fs = (int64_t)N * N * p->HP;
-    if (sign > 0)
-      { ProfScope ps_(p, name, st);
-      k_axis_inplace<N, W, 1, +1><<<grid, A::THREADS, A::SMEM, st>>>(p->d_work, fs, p->HP, p->d_twN);
-      }
-    else
-      { ProfScope ps_(p, name, st);
-      k_axis_inplace<N, W, 1, -1><<<grid, A::THREADS, A::SMEM, st>>>(p->d_work, fs, p->HP, p->d_twN);
-      }
-    AAR_CUDA_TRY(p, cudaGetLastError());
-    p->last_launches += 1;
-    return AAR_OK;
+  // y transform of fields [first, first + nf) (or the active modal slots)
+  template <int SIGN>
+  static int ypass(Plan* p, float2* base, int nf, const int* map, cudaStream_t st, const char* name) {
+    AxisOp<N, W, 1, SIGN> op{base, fstride(p), tiles(p), p->HP, map};
+    return run_pass<N>(p, op, nf * tiles(p), st, name);
   }
   static int modal(Plan* p, const ModalArgs& a, cudaStream_t st) {
-    using A = AxisCfg<N, W>;
-    int64_t fs = (int64_t)N * N * p->HP;
-    unsigned tiles = (unsigned)(N * (p->HP / W));
-    { ProfScope ps_(p, "modal_xinv", st);
-    k_modal_xinv<N, W><<<tiles * a.M, A::THREADS, A::SMEM, st>>>(a, p->d_phik, p->d_work, fs, p->HP, p->d_twN,
-                                                                  p->d_qtab, p->nsq);
-    }
-    AAR_CUDA_TRY(p, cudaGetLastError());
-    p->last_launches += 1;
-    int rc = ypass(p, a.M, +1, st, "modal_ypass_inv");
+    int64_t fs = fstride(p);
+    XinvOp<N, W> xo{a, p->d_phik, p->d_work, fs, tiles(p), p->nsq, p->HP, p->d_qtab};
+    int rc = run_pass<N>(p, xo, tiles(p) * a.M, st, "modal_xinv");
     if (rc) return rc;
+    if ((rc = ypass<+1>(p, p->d_work, a.M, nullptr, st, "modal_ypass_inv"))) return rc;
     size_t sm_rows = sizeof(float2) * (size_t)(a.M + 1) * RowCfg<N>::LS;
     ModalRowOp op{a.M, (const DevTerms*)p->d_terms};
-    { ProfScope ps_(p, "modal_rows", st);
-    k_rows<N, ModalRowOp><<<(unsigned)((int64_t)N * N), 512, sm_rows, st>>>(op, p->d_work, fs, p->HP, p->d_twN, p->d_twH);
+    {
+      ProfScope ps_(p, "modal_rows", st);
+      k_rows<N, ModalRowOp><<<(unsigned)((int64_t)N * N), 512, sm_rows, st>>>(op, p->d_work, fs, p->HP, p->d_twN,
+                                                                               p->d_twH);
     }
     AAR_CUDA_TRY(p, cudaGetLastError());
     p->last_launches += 1;
-    // forward y on the active slots only
-    {
-      dim3 grid((unsigned)(N * (p->HP / W)), (unsigned)p->nr_active);
-      { ProfScope ps_(p, "modal_ypass_fwd", st);
-      k_axis_slots<N, W><<<grid, A::THREADS, A::SMEM, st>>>(p->d_work, fs, p->HP, p->d_twN,
-                                                             (const DevTerms*)p->d_terms);
-      }
-      AAR_CUDA_TRY(p, cudaGetLastError());
-      p->last_launches += 1;
-    }
+    if ((rc = ypass<-1>(p, p->d_work, p->nr_active, slot_map(p), st, "modal_ypass_fwd"))) return rc;
+    using A = AxisCfg<N, W>;
     float fnl_n3 = (float)(p->prm.fnl / ((double)N * N * N));
-    { ProfScope ps_(p, "modal_xacc", st);
-    k_modal_xacc<N, W><<<tiles, A::THREADS, A::SMEM + sizeof(float4) * N * W, st>>>(a, p->d_phik, p->d_work, fs, p->HP, fnl_n3, p->d_twN,
-                                                                  (const DevTerms*)p->d_terms, p->d_rtab, p->nsq);
+    {
+      ProfScope ps_(p, "modal_xacc", st);
+      k_modal_xacc<N, W><<<(unsigned)tiles(p), A::THREADS, A::SMEM + sizeof(float4) * N * W, st>>>(
+          a, p->d_phik, p->d_work, fs, p->HP, fnl_n3, p->d_twN, (const DevTerms*)p->d_terms, p->d_rtab, p->nsq);
     }
     AAR_CUDA_TRY(p, cudaGetLastError());
     p->last_launches += 1;
     return AAR_OK;
   }
   static int lpt(Plan* p, const LptArgs& a, cudaStream_t st) {
-    using A = AxisCfg<N, W>;
-    int64_t fs = (int64_t)N * N * p->HP;
-    unsigned tiles = (unsigned)(N * (p->HP / W));
-    { ProfScope ps_(p, "lpt_xinv_hess", st);
-    k_lpt_xinv_hess<N, W><<<tiles * 6, A::THREADS, A::SMEM, st>>>(a, p->d_phik, p->d_work, fs, p->HP, p->d_twN);
-    }
-    AAR_CUDA_TRY(p, cudaGetLastError());
-    p->last_launches += 1;
-    int rc = ypass(p, 6, +1, st, "lpt_ypass_inv_hess");
+    int64_t fs = fstride(p);
+    LptOp<N, W, 0> ho{a, p->d_phik, p->d_work, fs, tiles(p), p->HP, 6};
+    int rc = run_pass<N>(p, ho, tiles(p) * 6, st, "lpt_xinv_hess");
     if (rc) return rc;
+    if ((rc = ypass<+1>(p, p->d_work, 6, nullptr, st, "lpt_ypass_inv_hess"))) return rc;
     size_t sm_rows = sizeof(float2) * (size_t)7 * RowCfg<N>::LS;
     SourceRowOp op{6};
-    { ProfScope ps_(p, "lpt_rows_source", st);
-    k_rows<N, SourceRowOp><<<(unsigned)((int64_t)N * N), 256, sm_rows, st>>>(op, p->d_work, fs, p->HP, p->d_twN, p->d_twH);
-    }
-    AAR_CUDA_TRY(p, cudaGetLastError());
-    p->last_launches += 1;
-    // forward y of the source slot only
     {
-      dim3 grid((unsigned)(N * (p->HP / W)), 1);
-      { ProfScope ps_(p, "lpt_ypass_fwd_source", st);
-      k_axis_inplace<N, W, 1, -1><<<grid, A::THREADS, A::SMEM, st>>>(p->d_work + 6 * fs, fs, p->HP, p->d_twN);
-      }
-      AAR_CUDA_TRY(p, cudaGetLastError());
-      p->last_launches += 1;
-    }
-    { ProfScope ps_(p, "lpt_xmid", st);
-    k_lpt_xmid<N, W><<<tiles * 6, A::THREADS, A::SMEM, st>>>(a, p->d_phik, p->d_work, fs, p->HP, 6, p->d_twN);
+      ProfScope ps_(p, "lpt_rows_source", st);
+      k_rows<N, SourceRowOp><<<(unsigned)((int64_t)N * N), 256, sm_rows, st>>>(op, p->d_work, fs, p->HP, p->d_twN,
+                                                                                p->d_twH);
     }
     AAR_CUDA_TRY(p, cudaGetLastError());
     p->last_launches += 1;
-    rc = ypass(p, 6, +1, st, "lpt_ypass_inv_disp");
-    if (rc) return rc;
+    if ((rc = ypass<-1>(p, p->d_work + 6 * fs, 1, nullptr, st, "lpt_ypass_fwd_source"))) return rc;
+    // forward x of the source in place, psi2 from it, then psi1 from phi
+    {
+      AxisOp<N, W, 0, -1> xs{p->d_work + 6 * fs, 0, tiles(p), p->HP, nullptr};
+      if ((rc = run_pass<N>(p, xs, tiles(p), st, "lpt_xfwd_source"))) return rc;
+    }
+    LptOp<N, W, 2> m2{a, p->d_phik, p->d_work, fs, tiles(p), p->HP, 6};
+    if ((rc = run_pass<N>(p, m2, tiles(p) * 3, st, "lpt_xpsi2"))) return rc;
+    LptOp<N, W, 1> m1{a, p->d_phik, p->d_work, fs, tiles(p), p->HP, 6};
+    if ((rc = run_pass<N>(p, m1, tiles(p) * 3, st, "lpt_xpsi1"))) return rc;
+    if ((rc = ypass<+1>(p, p->d_work, 6, nullptr, st, "lpt_ypass_inv_disp"))) return rc;
     using R = RowCfg<N>;
     int lines_per_block = 8 * R::LPW;
     int64_t nrows = (int64_t)N * N;
     dim3 grid((unsigned)((nrows + lines_per_block - 1) / lines_per_block), 6);
-    { ProfScope ps_(p, "lpt_rows_c2r", st);
-    k_rows_c2r<N><<<grid, 256, sizeof(float2) * lines_per_block * R::LS, st>>>(p->d_work, fs, p->HP, 0, nrows,
-                                                                              p->d_twN, p->d_twH);
+    {
+      ProfScope ps_(p, "lpt_rows_c2r", st);
+      k_rows_c2r<N><<<grid, 256, sizeof(float2) * lines_per_block * R::LS, st>>>(p->d_work, fs, p->HP, 0, nrows,
+                                                                                p->d_twN, p->d_twH);
     }
     AAR_CUDA_TRY(p, cudaGetLastError());
     p->last_launches += 1;
@@ -908,6 +731,7 @@ int fused_lpt(Plan* p, cudaStream_t st) {
   a.m = modal_args(p);
   a.inv_Dbeta = (float)(1.0 / (p->Dplus * p->Beta));
   a.twb = p->d_twb;
+  a.sinc = p->d_sinc;
   a.box_over_2n = (float)(p->prm.box / 2 / p->N);
   return dispatch_n(p->N, [&](auto nc) { return Launch<decltype(nc)::value>::lpt(p, a, st); });
 }
@@ -982,44 +806,37 @@ template <int N>
 struct Xform {
   static constexpr int W = 8;
   static int c2r(Plan* p, float2* slot, cudaStream_t st) {
-    using A = AxisCfg<N, W>;
     using R = RowCfg<N>;
-    dim3 grid((unsigned)(N * (p->HP / W)), 1);
-    { ProfScope ps_(p, "xform_axis", st);
-    k_axis_inplace<N, W, 0, +1><<<grid, A::THREADS, A::SMEM, st>>>(slot, 0, p->HP, p->d_twN);
-    }
-    { ProfScope ps_(p, "xform_axis", st);
-    k_axis_inplace<N, W, 1, +1><<<grid, A::THREADS, A::SMEM, st>>>(slot, 0, p->HP, p->d_twN);
-    }
+    int64_t tiles = (int64_t)N * (p->HP / W);
+    int rc = run_pass<N>(p, AxisOp<N, W, 0, +1>{slot, 0, tiles, p->HP, nullptr}, tiles, st, "xform_x");
+    if (rc) return rc;
+    if ((rc = run_pass<N>(p, AxisOp<N, W, 1, +1>{slot, 0, tiles, p->HP, nullptr}, tiles, st, "xform_y"))) return rc;
     int lpb = 8 * R::LPW;
     int64_t nrows = (int64_t)N * N;
     dim3 g2((unsigned)((nrows + lpb - 1) / lpb), 1);
-    { ProfScope ps_(p, "xform_rows", st);
-    k_rows_c2r<N><<<g2, 256, sizeof(float2) * lpb * R::LS, st>>>(slot, 0, p->HP, 0, nrows, p->d_twN, p->d_twH);
+    {
+      ProfScope ps_(p, "xform_rows", st);
+      k_rows_c2r<N><<<g2, 256, sizeof(float2) * lpb * R::LS, st>>>(slot, 0, p->HP, 0, nrows, p->d_twN, p->d_twH);
     }
     AAR_CUDA_TRY(p, cudaGetLastError());
-    p->last_launches += 3;
+    p->last_launches += 1;
     return AAR_OK;
   }
   static int r2c(Plan* p, float2* slot, cudaStream_t st) {
-    using A = AxisCfg<N, W>;
     using R = RowCfg<N>;
     int lpb = 8 * R::LPW;
     int64_t nrows = (int64_t)N * N;
     dim3 g2((unsigned)((nrows + lpb - 1) / lpb), 1);
-    { ProfScope ps_(p, "xform_rows", st);
-    k_rows_r2c<N><<<g2, 256, sizeof(float2) * lpb * R::LS, st>>>(slot, p->HP, nrows, p->d_twN, p->d_twH);
-    }
-    dim3 grid((unsigned)(N * (p->HP / W)), 1);
-    { ProfScope ps_(p, "xform_axis", st);
-    k_axis_inplace<N, W, 1, -1><<<grid, A::THREADS, A::SMEM, st>>>(slot, 0, p->HP, p->d_twN);
-    }
-    { ProfScope ps_(p, "xform_axis", st);
-    k_axis_inplace<N, W, 0, -1><<<grid, A::THREADS, A::SMEM, st>>>(slot, 0, p->HP, p->d_twN);
+    {
+      ProfScope ps_(p, "xform_rows", st);
+      k_rows_r2c<N><<<g2, 256, sizeof(float2) * lpb * R::LS, st>>>(slot, p->HP, nrows, p->d_twN, p->d_twH);
     }
     AAR_CUDA_TRY(p, cudaGetLastError());
-    p->last_launches += 3;
-    return AAR_OK;
+    p->last_launches += 1;
+    int64_t tiles = (int64_t)N * (p->HP / W);
+    int rc = run_pass<N>(p, AxisOp<N, W, 1, -1>{slot, 0, tiles, p->HP, nullptr}, tiles, st, "xform_y");
+    if (rc) return rc;
+    return run_pass<N>(p, AxisOp<N, W, 0, -1>{slot, 0, tiles, p->HP, nullptr}, tiles, st, "xform_x");
   }
 };
 

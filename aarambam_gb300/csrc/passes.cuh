@@ -1,0 +1,211 @@
+// Strided FFT passes (included by fused.cu).
+//
+// A pass is a list of work items (tile x field / component), one block per
+// item; several blocks share an SM, so one block's cp.async tile load
+// overlaps the FFT work of the others.  (Measured at N = 512 and 1024: a
+// persistent loop over items lets the compiler keep loop-invariant twiddles
+// live across items and spill, and a second tile buffer for prefetching
+// halves the resident blocks; both were slower.)  An Op supplies
+//   load(buf, item)   issue the cp.async copy of the item's input tile
+//   pre(buf, item)    optional in-place prologue once the tile has landed
+//                     (returns true when it wrote shared memory)
+//   body(buf, item)   the FFT(s) and mid-stage work (ends with a barrier)
+//   store(buf, item)  epilogue + store to global memory
+// Consecutive items run at the same time on consecutive blocks, so items
+// that share an input tile (one phi tile for the M filters, the six 2LPT
+// components) are ordered next to each other and hit L2.
+#pragma once
+// (included inside namespace aar)
+
+template <int N, int W, class Op>
+__global__ void __launch_bounds__(AxisCfg<N, W>::THREADS, AxisCfg<N, W>::MINB) k_pass(Op op, const float2* __restrict__ tw) {
+  extern __shared__ float2 sm[];
+  const int64_t it = blockIdx.x;
+  op.load(sm, it);
+  cp_async_commit();
+  cp_async_wait<0>();
+  __syncthreads();
+  if (op.pre(sm, it)) __syncthreads();
+  op.body(sm, it, tw);
+  op.store(sm, it);
+}
+
+// element (n, w) of the e-th entry a thread owns in a tile
+template <int N, int W>
+__device__ __forceinline__ void tile_owned(int i, int& e, int& n, int& w) {
+  e = threadIdx.x + AxisCfg<N, W>::THREADS * i;
+  n = e / W;
+  w = e % W;
+}
+
+// In-place complex FFT along AXIS of fields (slot_map[f] or f), items
+// f * tiles + t.
+template <int N, int W, int AXIS, int SIGN>
+struct AxisOp {
+  float2* base;
+  int64_t fs, tiles;
+  int HP;
+  const int* slot_map;  // optional field indirection (active modal slots)
+  __device__ float2* field(int64_t item) const {
+    int64_t f = item / tiles;
+    return base + (slot_map ? (int64_t)slot_map[f] : f) * fs;
+  }
+  __device__ void coords(int64_t item, int& o, int& c0) const {
+    int64_t t = item % tiles;
+    int ncol = HP / W;
+    o = (int)(t / ncol);
+    c0 = (int)(t % ncol) * W;
+  }
+  __device__ void load(float2* b, int64_t item) const {
+    int o, c0;
+    coords(item, o, c0);
+    tile_load_async<N, W, AXIS>(b, field(item), HP, o, c0);
+  }
+  __device__ bool pre(float2*, int64_t) const { return false; }
+  __device__ void body(float2* b, int64_t, const float2* tw) const {
+    tile_fft<N, W, SIGN>(b, tw);
+    __syncthreads();
+  }
+  __device__ void store(const float2* b, int64_t item) const {
+    int o, c0;
+    coords(item, o, c0);
+    tile_store<N, W, AXIS>(b, field(item), HP, o, c0);
+  }
+};
+
+// First modal pass: item = tile * M + p; phi tile times q_p(n^2) (zero on
+// the cut, DC and padding columns), inverse x FFT, into field p.
+template <int N, int W>
+struct XinvOp {
+  ModalArgs a;
+  const float2* phi;
+  float2* work;
+  int64_t fs, tiles, nsq;
+  int HP;
+  const float* qtab;
+  __device__ void coords(int64_t item, int& o, int& c0, int& p) const {
+    int64_t t = item / a.M;
+    p = (int)(item % a.M);
+    int ncol = HP / W;
+    o = (int)(t / ncol);
+    c0 = (int)(t % ncol) * W;
+  }
+  __device__ void load(float2* b, int64_t item) const {
+    int o, c0, p;
+    coords(item, o, c0, p);
+    tile_load_async<N, W, 0>(b, phi, HP, o, c0);
+  }
+  __device__ bool pre(float2* b, int64_t item) const {
+    using C = AxisCfg<N, W>;
+    int o, c0, p;
+    coords(item, o, c0, p);
+    const int ky = sidx(o, N);
+    const float* q = qtab + (int64_t)p * nsq;
+#pragma unroll 4
+    for (int i = 0; i < C::PER; ++i) {
+      int e, n, w;
+      tile_owned<N, W>(i, e, n, w);
+      int kz = c0 + w, kx = sidx(n, N);
+      int n2 = kx * kx + ky * ky + kz * kz;
+      float f = 0.f;
+      if (kz <= N / 2 && n2 != 0 && keep_cell(a.g, kx, ky, kz)) f = __ldg(q + n2);
+      float2& v = b[w * C::LS + spad(n)];
+      v = make_float2(v.x * f, v.y * f);
+    }
+    return true;
+  }
+  __device__ void body(float2* b, int64_t, const float2* tw) const {
+    tile_fft<N, W, +1>(b, tw);
+    __syncthreads();
+  }
+  __device__ void store(const float2* b, int64_t item) const {
+    int o, c0, p;
+    coords(item, o, c0, p);
+    tile_store<N, W, 0>(b, work + (int64_t)p * fs, HP, o, c0);
+  }
+};
+
+// 2LPT passes (MODE 0: Hessians, items tile * 6 + comp; MODE 1: ZA
+// displacements, items tile * 3 + a; MODE 2: 2LPT displacements, items
+// tile * 3 + a).
+//  MODE 0: d_ab = -k_a k_b T/(D Beta) phi (main.c:1238-1277), inverse x FFT
+//  MODE 1: psi1_a = i k_a T/(D Beta) phi smth (main.c:1180-1216), inverse x
+//  MODE 2: psi2_a = -i k_a/k^2 S smth (main.c:1311-1368) from the source
+//          slot already transformed along x, inverse x
+// smth = [sinc(kx Box/2N) sinc(ky Box/2N) sinc(kz Box/2N)]^-2 (CORRECT_CIC),
+// from a per-index sinc table.  Outputs: Hessians to slots 0..5, psi1 to
+// slots 0..2, psi2 to slots 3..5.
+template <int N, int W, int MODE>
+struct LptOp {
+  LptArgs a;
+  const float2* phi;
+  float2* work;
+  int64_t fs, tiles;
+  int HP, src_slot;
+  static constexpr int NC = MODE == 0 ? 6 : 3;
+  __device__ void coords(int64_t item, int& o, int& c0, int& comp) const {
+    int64_t t = item / NC;
+    comp = (int)(item % NC);
+    int ncol = HP / W;
+    o = (int)(t / ncol);
+    c0 = (int)(t % ncol) * W;
+  }
+  __device__ void load(float2* b, int64_t item) const {
+    int o, c0, comp;
+    coords(item, o, c0, comp);
+    const float2* src = MODE == 2 ? work + (int64_t)src_slot * fs : phi;
+    tile_load_async<N, W, 0>(b, src, HP, o, c0);
+  }
+  // multiply the tile in place by the spectral factor of component comp
+  __device__ void apply(float2* b, int o, int c0, int comp) const {
+    using C = AxisCfg<N, W>;
+    const int ax = MODE == 0 ? (comp < 3 ? 0 : (comp < 5 ? 1 : 2)) : comp;
+    const int bx = MODE == 0 ? (comp == 0 ? 0 : comp == 1 ? 1 : comp == 2 ? 2 : comp == 3 ? 1 : 2) : comp;
+    const int ky = sidx(o, N);
+    const float kF = a.m.g.kF;
+    const float sy = MODE == 0 ? 1.f : __ldg(a.sinc + o);
+#pragma unroll 2
+    for (int i = 0; i < C::PER; ++i) {
+      int e, n, w;
+      tile_owned<N, W>(i, e, n, w);
+      const int kz = c0 + w, kx = sidx(n, N);
+      const int n2 = kx * kx + ky * ky + kz * kz;
+      const float ka = kF * (float)(ax == 0 ? kx : ax == 1 ? ky : kz);
+      float2& v = b[w * C::LS + spad(n)];
+      float2 r = make_float2(0.f, 0.f);
+      if (kz <= N / 2) {
+        if (MODE == 0) {
+          const float kb = kF * (float)(bx == 0 ? kx : bx == 1 ? ky : kz);
+          float f = -ka * kb * __ldg(a.twb + n2);
+          r = make_float2(v.x * f, v.y * f);
+        } else {
+          float ff = 1.f / (__ldg(a.sinc + n) * sy * __ldg(a.sinc + kz));
+          float smth = ff * ff;
+          if (MODE == 1) {
+            float f = ka * __ldg(a.twb + n2) * smth;
+            r = make_float2(-f * v.y, f * v.x);
+          } else if (n2 > 0) {
+            float f = ka / (kF * kF * (float)n2) * smth;
+            r = make_float2(f * v.y, -f * v.x);
+          }
+        }
+      }
+      v = r;
+    }
+  }
+  __device__ bool pre(float2* b, int64_t item) const {
+    int o, c0, comp;
+    coords(item, o, c0, comp);
+    apply(b, o, c0, comp);
+    return true;
+  }
+  __device__ void body(float2* b, int64_t item, const float2* tw) const {
+    tile_fft<N, W, +1>(b, tw);
+    __syncthreads();
+  }
+  __device__ void store(const float2* b, int64_t item) const {
+    int o, c0, comp;
+    coords(item, o, c0, comp);
+    tile_store<N, W, 0>(b, work + (int64_t)(MODE == 2 ? 3 + comp : comp) * fs, HP, o, c0);
+  }
+};

@@ -155,6 +155,17 @@ class ICGenerator:
                                                    _ptr(pos), _ptr(vel), _ptr(ids), self._stream()))
         return pos, vel, ids
 
+    def readout_glass(self, glass: torch.Tensor, glass_box: float, tile: int):
+        """Read-out stage alone, Lagrangian positions from the tiled glass."""
+        glass = glass.contiguous()
+        n = glass.shape[0] * tile ** 3
+        pos = torch.empty((n, 3), dtype=torch.float32, device=self.device)
+        vel = torch.empty_like(pos)
+        ids = torch.empty((n,), dtype=torch.int32, device=self.device)
+        check(self.L, self.h, self.L.aar_stage_readout_glass(self.h, _ptr(glass), glass.shape[0], float(glass_box),
+                                                             tile, _ptr(pos), _ptr(vel), _ptr(ids), self._stream()))
+        return pos, vel, ids
+
     def run_host(self, lagr: np.ndarray):
         """The C-ABI host-buffer path: numpy in, numpy out (copies included)."""
         lagr = np.ascontiguousarray(lagr, dtype=np.float32)

@@ -110,6 +110,10 @@ int aar_stage_lpt(aar_plan* plan, void* stream);
 /* Particle read-out (main.c:1436-1516). */
 int aar_stage_readout(aar_plan* plan, const float* d_lagr_pos, int64_t npart, float* d_pos, float* d_vel,
                       void* stream);
+/* Read-out with the Lagrangian positions made from a tiled glass, as in
+   aar_run_glass (read_glass.c:129-214, main.c:1436-1516). */
+int aar_stage_readout_glass(aar_plan* plan, const float* d_glass_pos, int64_t nglass, double glass_box, int32_t tile,
+                            float* d_pos, float* d_vel, int32_t* d_ids, void* stream);
 /* Copy the plan's current potential spectrum to d_out as complex
    [N][N][N/2+1] (interleaved re, im; float32 for AAR_FUSED_FP32, float64
    for AAR_PLAIN_FP64). */

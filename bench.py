@@ -39,6 +39,9 @@ WORKLOADS = {
     # name: (Nmesh, Box, table, N_modes, Nmax, Fnl)
     "scalarI_m20_n1024": (1024, 1000.0, "scalarI_m20_L1000_n1024", 20, 1024, 100.0),
     "scalarI_m12_n512": (512, 1000.0, "scalarI_m12_L1000_n512", 12, 512, 100.0),
+    # the 1024^3 workload's 20-mode table on a 512^3 grid (per-launch DRAM
+    # traffic of this case times 8 is the 1024^3 traffic: same term list)
+    "scalarI_m20_n512": (512, 1000.0, "scalarI_m20_L1000_n1024", 20, 1024, 100.0),
     "scalarI_m12_n256": (256, 1000.0, "scalarI_m12_L1000_n512", 12, 512, 100.0),
     "local_m8_n128": (128, 500.0, "local_m8_L500_n128", 8, 128, 10.0),
 }
@@ -208,6 +211,28 @@ def cpu_baseline(wl: str, n_sample: int, steps: int = 1) -> dict:
                       f"{os.uname().machine}"}
 
 
+def replica_seed(rank: int) -> int:
+    """Replicas run independent realisations: the seed of rank r is 1234 + r."""
+    return 1234 + rank
+
+
+def max_over_ranks(seconds: float, device=None) -> float:
+    """The slowest rank's time (the job ends when it does); the process
+    group's backend does the reduction (NCCL on GPUs, gloo in the CPU test)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return seconds
+    tt = torch.tensor([seconds], dtype=torch.float64, device=device)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return float(tt.item())
+
+
+def job_rate(world: int, steps: int, units_per_step: int, seconds: float) -> float:
+    """Whole-job throughput: units of all ranks over the slowest rank's time."""
+    return world * steps * units_per_step / seconds
+
+
 def gpu_arm(args):
     import torch
     import torch.distributed as dist
@@ -223,7 +248,7 @@ def gpu_arm(args):
     from aarambam_gb300.ic import ICGenerator
     _lib.load(build_if_missing=True)
 
-    cfg = make_cfg(args.workload, 1234 + rank)
+    cfg = make_cfg(args.workload, replica_seed(rank))
     N, M = cfg["Nmesh"], cfg["N_modes"]
     alpha, x0, k, t = load_tables(cfg["table"], M)
     R = active_r(alpha)
@@ -252,12 +277,8 @@ def gpu_arm(args):
     e1.record(stream)
     barrier()
     clocks = clk.stop()
-    elapsed = e0.elapsed_time(e1) / 1e3
-    if world > 1:
-        tt = torch.tensor([elapsed], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        elapsed = float(tt.item())
-    value = world * args.steps * npart / elapsed
+    elapsed = max_over_ranks(e0.elapsed_time(e1) / 1e3, dev)
+    value = job_rate(world, args.steps, npart, elapsed)
 
     # per-kernel times of one profiled step (events on the launching stream)
     buf = __import__("ctypes").create_string_buffer(1 << 16)
@@ -306,12 +327,8 @@ def gpu_arm(args):
         for _ in range(ks):
             host_step()
         barrier()
-        te = time.perf_counter() - t0
-        if world > 1:
-            tt = torch.tensor([te], device=dev)
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            te = float(tt.item())
-        e2e = {"value": world * ks * npart / te, "unit": UNIT, "h2d_bytes_per_step": 12 * npart,
+        te = max_over_ranks(time.perf_counter() - t0, dev)
+        e2e = {"value": job_rate(world, ks, npart, te), "unit": UNIT, "h2d_bytes_per_step": 12 * npart,
                "d2h_bytes_per_step": 24 * npart, "steps": ks, "api": "aar_run_host (C ABI, pinned host buffers)"}
 
     plain = None

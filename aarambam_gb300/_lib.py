@@ -25,7 +25,7 @@ AAR_PLAIN_FP64 = 1
 EXPORTS = [
     "aar_plan_create", "aar_set_tables", "aar_set_transfer", "aar_get_scalars", "aar_set_seed", "aar_run",
     "aar_run_glass", "aar_run_host", "aar_seedtable", "aar_stage_noise", "aar_stage_modal", "aar_stage_lpt",
-    "aar_stage_readout", "aar_stage_readout_glass", "aar_copy_spectrum", "aar_copy_field", "aar_c2r", "aar_r2c", "aar_last_launch_count", "aar_profile_enable", "aar_profile_report",
+    "aar_stage_readout", "aar_stage_readout_glass", "aar_copy_spectrum", "aar_copy_field", "aar_gaussian_spectrum_noalloc", "aar_c2r", "aar_r2c", "aar_last_launch_count", "aar_profile_enable", "aar_profile_report",
     "aar_last_error", "aar_plan_destroy", "aar_version",
 ]
 
@@ -87,6 +87,7 @@ def load(build_if_missing: bool = False):
     L.aar_stage_readout_glass.argtypes = [vp, vp, i64, C.c_double, i32, vp, vp, vp, vp]
     L.aar_copy_spectrum.argtypes = [vp, vp, vp]
     L.aar_copy_field.argtypes = [vp, i32, vp, vp]
+    L.aar_gaussian_spectrum_noalloc.argtypes = [vp, vp, vp]
     L.aar_c2r.argtypes = [vp, vp, vp, vp]
     L.aar_r2c.argtypes = [vp, vp, vp, vp]
     L.aar_last_launch_count.argtypes = [vp]

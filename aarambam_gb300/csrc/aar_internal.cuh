@@ -128,6 +128,7 @@ void plain_free(Plan* p);
 int fused_c2r(Plan* p, const float2* in, float* out, cudaStream_t st);
 int fused_r2c(Plan* p, const float* in, float2* out, cudaStream_t st);
 int fused_configure_xform(Plan* p);
+int noalloc_gaussian(Plan* p, void* d_out, cudaStream_t st);
 
 }  // namespace aar
 

@@ -607,6 +607,13 @@ int aar_copy_spectrum(aar_plan* h, void* d_out, void* stream) {
   return AAR_OK;
 }
 
+int aar_gaussian_spectrum_noalloc(aar_plan* h, void* d_out, void* stream) {
+  if (!h || !d_out) return AAR_ERR_ARG;
+  Plan* p = &h->p;
+  if (!p->have_transfer) return set_err(p, "transfer function not set"), AAR_ERR_STATE;
+  return noalloc_gaussian(p, d_out, S(stream));
+}
+
 static int need_work(Plan* p) {
   if (p->prm.precision != AAR_FUSED_FP32) return set_err(p, "transforms are for the fused form"), AAR_ERR_ARG;
   if (!p->d_work) {

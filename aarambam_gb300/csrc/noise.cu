@@ -14,6 +14,9 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <mutex>
+#include <string>
+
 #include "aar_internal.cuh"
 #include "ranlux.cuh"
 
@@ -223,6 +226,69 @@ int launch_noise_fp64(Plan* p, const uint32_t* d_seed, double2* d_phik, int hp, 
   }
   AAR_CUDA_TRY(p, cudaGetLastError());
   p->last_launches += 1;
+  return AAR_OK;
+}
+
+// ------------------------------------------- no-allocation Gaussian spectrum
+// Scratch of aar_gaussian_spectrum_noalloc: the seed table, one uint32 per
+// (x, y) column of an Nmesh <= kNoAllocMaxN grid (4 MiB).  It is static
+// device memory of this library, reserved when the CUDA module is loaded, so
+// the call itself allocates nothing.  k_seedtable writes every entry before
+// k_noise reads any, so nothing in it has to start at zero.  There is one
+// scratch per device: calls that overlap on one device race on it.
+constexpr int kNoAllocMaxN = 1024;
+static __device__ __align__(256) uint32_t g_noalloc_seed[kNoAllocMaxN * kNoAllocMaxN];
+
+// Address of the scratch on the plan's device, resolved once per device with
+// cudaGetSymbolAddress (the first call on a device does this set-up).
+static int noalloc_scratch(Plan* p, uint32_t** out) {
+  constexpr int kMaxDev = 64;
+  static std::mutex mu;
+  static uint32_t* addr[kMaxDev] = {};
+  int dev = -1;
+  AAR_CUDA_TRY(p, cudaGetDevice(&dev));
+  if (dev != p->dev) return set_err(p, "the current device is not the plan's device"), AAR_ERR_ARG;
+  if (dev < 0 || dev >= kMaxDev) return set_err(p, "device ordinal out of range"), AAR_ERR_ARG;
+  std::lock_guard<std::mutex> lock(mu);
+  if (!addr[dev]) {
+    void* a = nullptr;
+    AAR_CUDA_TRY(p, cudaGetSymbolAddress(&a, g_noalloc_seed));
+    addr[dev] = (uint32_t*)a;
+  }
+  *out = addr[dev];
+  return AAR_OK;
+}
+
+// The Gaussian potential spectrum of the plan's seed straight into the
+// caller's complex [N][N][N/2+1] buffer (float32 pairs for the fused form,
+// float64 for the plain form), with the seed table in the static scratch
+// instead of the plan's seed-table buffer.  Same kernels and arguments as
+// launch_seedtable + launch_noise_fp32 / _fp64.
+int noalloc_gaussian(Plan* p, void* d_out, cudaStream_t st) {
+  const int N = p->N;
+  if (N > kNoAllocMaxN)
+    return set_err(p, "Nmesh " + std::to_string(N) + " exceeds the no-allocation scratch (Nmesh <= " +
+                          std::to_string(kNoAllocMaxN) + ")"),
+           AAR_ERR_ARG;
+  uint32_t* seed = nullptr;
+  int rc = noalloc_scratch(p, &seed);
+  if (rc) return rc;
+  const int64_t total = (int64_t)N * N;
+  const int64_t draws_per = 12 * (int64_t)p->rlx_seg;
+  const int64_t nthr = (total + draws_per - 1) / draws_per;
+  k_seedtable<<<(unsigned)((nthr + 63) / 64), 64, 0, st>>>((uint32_t)p->prm.seed, N, p->rlx_seg,
+                                                           (const U576*)p->d_rlxpow, 32, seed);
+  AAR_CUDA_TRY(p, cudaGetLastError());
+  const int hp = N / 2 + 1;
+  const bool fp64 = p->prm.precision == AAR_PLAIN_FP64;
+  AAR_CUDA_TRY(p, cudaMemsetAsync(d_out, 0, (fp64 ? sizeof(double2) : sizeof(float2)) * (size_t)total * hp, st));
+  const unsigned nb = (unsigned)((total + 127) / 128);
+  if (fp64)
+    k_noise<true><<<nb, 128, 0, st>>>(noise_args(p), seed, d_out, hp);
+  else
+    k_noise<false><<<nb, 128, 0, st>>>(noise_args(p), seed, d_out, hp);
+  AAR_CUDA_TRY(p, cudaGetLastError());
+  p->last_launches = 2;
   return AAR_OK;
 }
 

@@ -122,6 +122,29 @@ int aar_copy_spectrum(aar_plan* plan, void* d_out, void* stream);
    reference holds them before its 1/N^3) to d_out, float32 [N][N][N]. */
 int aar_copy_field(aar_plan* plan, int32_t which, float* d_out, void* stream);
 
+/* No counterpart in the reference.  The Gaussian potential spectrum of the
+   plan's seed (what aar_stage_noise + aar_copy_spectrum give for the fused
+   form) written straight into the caller's buffer d_out, complex
+   [N][N][N/2+1]: float32 pairs for AAR_FUSED_FP32 plans, float64 pairs for
+   AAR_PLAIN_FP64 plans.  Needs the transfer function set (aar_set_transfer);
+   the coefficient tables are not used.
+   The call allocates nothing: no cudaMalloc / cudaFree and no allocating
+   library.  It is for callers that own the device-memory budget themselves,
+   such as a simulation code that reserved HBM for its particle and mesh
+   arrays up front, or a framework whose caching allocator holds the device
+   memory: there a library cudaMalloc can fail once the memory is reserved,
+   and a cudaFree synchronises the whole device and stalls the caller's other
+   streams.  The seed table it needs between its two kernels lives in a
+   static 4 MiB device array of the library (Nmesh <= 1024); larger Nmesh is
+   rejected with AAR_ERR_ARG and a message.  The plan's own spectrum and
+   seed-table buffers are not touched.  d_out need not be zeroed (the call
+   clears it on the stream) and nothing in the scratch has to start at zero.
+   The first call on a device resolves the scratch address
+   (cudaGetSymbolAddress); make that first call before any stream capture
+   begins.  There is one scratch per device, so calls that overlap on one
+   device (other streams or host threads) race on it: serialise them. */
+int aar_gaussian_spectrum_noalloc(aar_plan* plan, void* d_out, void* stream);
+
 /* The plan's own 3-D transforms with FFTW's rfftwnd conventions
    (unnormalised; c2r drops the imaginary parts that the kz = 0 and kz = N/2
    planes would need to be Hermitian), as used on every rfftwnd_mpi call site

@@ -27,6 +27,7 @@ EXPORTS = [
     "aar_run_glass", "aar_run_host", "aar_seedtable", "aar_stage_noise", "aar_stage_modal", "aar_stage_lpt",
     "aar_stage_readout", "aar_stage_readout_glass", "aar_copy_spectrum", "aar_copy_field", "aar_gaussian_spectrum_noalloc", "aar_c2r", "aar_r2c", "aar_last_launch_count", "aar_profile_enable", "aar_profile_report",
     "aar_last_error", "aar_plan_destroy", "aar_version",
+    "aar_batch_create", "aar_batch_run", "aar_batch_launch_count", "aar_batch_last_error", "aar_batch_destroy",
 ]
 
 
@@ -93,6 +94,13 @@ def load(build_if_missing: bool = False):
     L.aar_last_launch_count.argtypes = [vp]
     L.aar_profile_enable.argtypes = [vp, i32]
     L.aar_profile_report.argtypes = [vp, C.c_char_p, i32]
+    L.aar_batch_create.argtypes = [C.POINTER(vp), i32, C.POINTER(vp)]
+    L.aar_batch_run.argtypes = [vp, C.POINTER(vp), C.POINTER(i64), C.POINTER(vp), C.POINTER(vp), vp]
+    L.aar_batch_launch_count.argtypes = [vp]
+    L.aar_batch_last_error.argtypes = [vp]
+    L.aar_batch_last_error.restype = C.c_char_p
+    L.aar_batch_destroy.argtypes = [vp]
+    L.aar_batch_destroy.restype = None
     L.aar_last_error.argtypes = [vp]
     L.aar_last_error.restype = C.c_char_p
     L.aar_plan_destroy.argtypes = [vp]

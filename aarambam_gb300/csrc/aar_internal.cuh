@@ -73,17 +73,20 @@ struct Plan {
   float* d_twb = nullptr;     // per n^2 T(k) / (Dplus Beta)
   float* d_sinc = nullptr;    // per grid index: CIC window sin(x)/x
   float* d_qtab = nullptr;    // [M][nsq] field filters q_p per n^2
-  float* d_rtab = nullptr;    // [M][nsq] radial parts rho_r per n^2
+  float* d_rtab = nullptr;    // [nsq][rtab_stride] radial parts rho_r per n^2 (r fastest)
+  int rtab_stride = 0;
   int64_t nsq = 0;            // 3 (N/2)^2 + 1
   int qtab_m = 0;             // modes the tables were allocated for
   void* d_rlxpow = nullptr;   // skip-ahead powers (U576[32])
   int rlx_seg = 0;            // refills per seed-table thread
   // modal term list (device)
   void* d_terms = nullptr;
+  std::vector<char> host_terms;  // the same term list on the host (kernel parameter of the row combine)
   int nterms = 0, nr_active = 0;
   // plain FP64 form
   void* plain = nullptr;
   int last_launches = 0;      // kernels launched by the last run
+  uint64_t generation = 0;    // bumped by every set_* call (captured graphs of the plan go stale)
   size_t used_bytes = 0;      // device bytes this plan holds
   // optional per-kernel timing: events recorded around every launch
   bool profiling = false;

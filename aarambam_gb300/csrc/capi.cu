@@ -270,6 +270,9 @@ static int alloc_fused(Plan* p, int M) {
 //                                         (P_{n-1}(kbar) - X0[n-1]) k^{2-ns}
 //   rho_n (radial part, main.c:833-860):  k^{s(n-3)} (n <= 3),  (P_{n-1}(kbar) - X0[n-1]) / k^2
 // with s = (4-ns)/3, kbar = -1 + 2 (k^s - kmin^s)/(kmax^s - kmin^s).
+// q is stored per mode ([M][nsq]: a filter pass reads one mode); rho per
+// |k|^2 ([nsq][rtab_stride], mode fastest: the accumulation reads every mode
+// of one cell, a few sectors instead of one per mode).
 static int mode_tables(Plan* p) {
   int N = p->N, M = p->M;
   int64_t nsq = 3LL * (N / 2) * (N / 2) + 1;
@@ -277,11 +280,12 @@ static int mode_tables(Plan* p) {
     // reuse the allocation
   } else {
     if (p->d_qtab) cudaFree(p->d_qtab), p->used_bytes -= sizeof(float) * p->nsq * p->qtab_m;
-    if (p->d_rtab) cudaFree(p->d_rtab), p->used_bytes -= sizeof(float) * p->nsq * p->qtab_m;
+    if (p->d_rtab) cudaFree(p->d_rtab), p->used_bytes -= sizeof(float) * p->nsq * p->rtab_stride;
     p->d_qtab = p->d_rtab = nullptr;
     int rc;
     if ((rc = plan_alloc(p, (void**)&p->d_qtab, sizeof(float) * nsq * M))) return rc;
-    if ((rc = plan_alloc(p, (void**)&p->d_rtab, sizeof(float) * nsq * M))) return rc;
+    p->rtab_stride = (M + 3) / 4 * 4;
+    if ((rc = plan_alloc(p, (void**)&p->d_rtab, sizeof(float) * nsq * p->rtab_stride))) return rc;
     p->qtab_m = M;
   }
   p->nsq = nsq;
@@ -289,7 +293,8 @@ static int mode_tables(Plan* p) {
   const double kmin = 2 * kPi / box, kmax = 2 * kPi / box * p->prm.nmax;
   const double sx = (4 - ns) / 3, kmin_ns = pow(kmin, sx), kmax_ns = pow(kmax, sx);
   const double kF = 2 * kPi / box;
-  std::vector<float> qt((size_t)nsq * M), rt((size_t)nsq * M);
+  const int rs = p->rtab_stride;
+  std::vector<float> qt((size_t)nsq * M), rt((size_t)nsq * rs, 0.f);
   std::vector<double> P(std::max(M, 2));
   for (int64_t n2 = 1; n2 < nsq; ++n2) {
     double k1 = kF * sqrt((double)n2), k2 = k1 * k1;
@@ -310,10 +315,10 @@ static int mode_tables(Plan* p) {
         in = d * p2n;
       }
       qt[(size_t)n * nsq + n2] = (float)in;
-      rt[(size_t)n * nsq + n2] = (float)out;
+      rt[(size_t)n2 * rs + n] = (float)out;
     }
   }
-  for (int n = 0; n < M; ++n) qt[(size_t)n * nsq] = rt[(size_t)n * nsq] = 0.f;
+  for (int n = 0; n < M; ++n) qt[(size_t)n * nsq] = 0.f;
   AAR_CUDA_TRY(p, cudaMemcpy(p->d_qtab, qt.data(), sizeof(float) * qt.size(), cudaMemcpyHostToDevice));
   AAR_CUDA_TRY(p, cudaMemcpy(p->d_rtab, rt.data(), sizeof(float) * rt.size(), cudaMemcpyHostToDevice));
   return AAR_OK;
@@ -449,6 +454,7 @@ int aar_set_tables(aar_plan* h, const double* alpha, const double* x0, int32_t M
     if (!isfinite(alpha[i])) return set_err(p, "non-finite alpha coefficient"), AAR_ERR_ARG;
   for (int i = 0; i < M; ++i)
     if (!isfinite(x0[i])) return set_err(p, "non-finite X0 coefficient"), AAR_ERR_ARG;
+  ++p->generation;
   p->alpha.assign(alpha, alpha + n3);
   p->x0.assign(x0, x0 + M);
   p->M = M;
@@ -467,6 +473,7 @@ int aar_set_tables(aar_plan* h, const double* alpha, const double* x0, int32_t M
 
 int aar_set_transfer(aar_plan* h, const double* k, const double* t, int32_t n) {
   if (!h) return AAR_ERR_ARG;
+  ++h->p.generation;
   plain_free(&h->p);
   return set_transfer(&h->p, k, t, n);
 }
@@ -482,6 +489,7 @@ int aar_set_seed(aar_plan* h, int32_t seed) {
   if (!h) return AAR_ERR_ARG;
   if (seed < 0) return set_err(&h->p, "Seed must be >= 0"), AAR_ERR_ARG;
   h->p.prm.seed = seed;
+  ++h->p.generation;
   return AAR_OK;
 }
 
@@ -691,6 +699,152 @@ int aar_copy_field(aar_plan* h, int32_t which, float* d_out, void* stream) {
   AAR_CUDA_TRY(p, cudaMemcpy2DAsync(d_out, sizeof(float) * N, src, sizeof(float) * 2 * p->HP, sizeof(float) * N,
                                     (size_t)N * N, cudaMemcpyDeviceToDevice, S(stream)));
   return AAR_OK;
+}
+
+// ------------------------------------------------------------- batches
+// Several fused plans (realisations with their own seed, coefficient table,
+// mode count and buffers) captured once into one CUDA graph: every plan's
+// aar_run work is a branch of the graph on its own stream, so small kernels
+// of different realisations overlap; later runs replay the graph with one
+// launch.  The graph is captured again when the buffer pointers or particle
+// counts change.
+struct aar_batch {
+  std::vector<aar_plan*> plans;
+  std::vector<cudaStream_t> streams;
+  std::vector<cudaEvent_t> done;
+  cudaEvent_t fork = nullptr;
+  cudaStream_t cap = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  std::vector<uintptr_t> key;  // pointers and counts the graph was captured with
+  std::string err;
+  int launches = 0;
+};
+
+static int batch_err(aar_batch* b, const std::string& e, int code) {
+  b->err = e;
+  return code;
+}
+
+static void batch_drop_graph(aar_batch* b) {
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  b->exec = nullptr;
+  b->graph = nullptr;
+  b->key.clear();
+}
+
+int aar_batch_create(aar_plan* const* plans, int32_t nplans, aar_batch** out) {
+  if (!plans || nplans < 1 || !out) return AAR_ERR_ARG;
+  *out = nullptr;
+  aar_batch* b = new (std::nothrow) aar_batch();
+  if (!b) return AAR_ERR_OOM;
+  int dev = -1;
+  for (int i = 0; i < nplans; ++i) {
+    if (!plans[i] || plans[i]->p.prm.precision != AAR_FUSED_FP32 || (i > 0 && plans[i]->p.dev != dev)) {
+      delete b;
+      return AAR_ERR_ARG;
+    }
+    dev = plans[i]->p.dev;
+    b->plans.push_back(plans[i]);
+  }
+  bool ok = cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking) == cudaSuccess &&
+            cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) == cudaSuccess;
+  for (int i = 0; ok && i < nplans; ++i) {
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev = nullptr;
+    ok = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) == cudaSuccess &&
+         cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) == cudaSuccess;
+    if (st) b->streams.push_back(st);
+    if (ev) b->done.push_back(ev);
+  }
+  if (!ok) {
+    aar_batch_destroy(b);
+    return AAR_ERR_CUDA;
+  }
+  *out = b;
+  return AAR_OK;
+}
+
+static int batch_capture(aar_batch* b, const float* const* d_lagr, const int64_t* npart, float* const* d_pos,
+                         float* const* d_vel) {
+  const int n = (int)b->plans.size();
+  if (cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+    return batch_err(b, "cudaStreamBeginCapture failed", AAR_ERR_CUDA);
+  int rc = AAR_OK;
+  int launches = 0;
+  if (cudaEventRecord(b->fork, b->cap) != cudaSuccess) rc = batch_err(b, "cudaEventRecord failed", AAR_ERR_CUDA);
+  for (int i = 0; i < n && rc == AAR_OK; ++i) {
+    Plan* p = &b->plans[i]->p;
+    const bool prof = p->profiling;
+    p->profiling = false;  // no event records inside the graph
+    cudaStream_t st = b->streams[i];
+    if (cudaStreamWaitEvent(st, b->fork, 0) != cudaSuccess) {
+      rc = batch_err(b, "cudaStreamWaitEvent failed", AAR_ERR_CUDA);
+    } else {
+      rc = aar_run(b->plans[i], d_lagr[i], npart[i], d_pos[i], d_vel[i], st);
+      if (rc) b->err = "plan " + std::to_string(i) + ": " + p->err;
+      launches += p->last_launches;
+    }
+    p->profiling = prof;
+    if (rc == AAR_OK && (cudaEventRecord(b->done[i], st) != cudaSuccess ||
+                         cudaStreamWaitEvent(b->cap, b->done[i], 0) != cudaSuccess))
+      rc = batch_err(b, "joining the plan streams failed", AAR_ERR_CUDA);
+  }
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture(b->cap, &g);
+  if (rc == AAR_OK && e != cudaSuccess) rc = batch_err(b, std::string("capture: ") + cudaGetErrorString(e), AAR_ERR_CUDA);
+  if (rc != AAR_OK) {
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    return rc;
+  }
+  b->graph = g;
+  e = cudaGraphInstantiate(&b->exec, g, 0);
+  if (e != cudaSuccess) {
+    batch_drop_graph(b);
+    return batch_err(b, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e), AAR_ERR_CUDA);
+  }
+  b->launches = launches;
+  return AAR_OK;
+}
+
+int aar_batch_run(aar_batch* b, const float* const* d_lagr, const int64_t* npart, float* const* d_pos,
+                  float* const* d_vel, void* stream) {
+  if (!b || !d_lagr || !npart || !d_pos || !d_vel) return AAR_ERR_ARG;
+  const int n = (int)b->plans.size();
+  std::vector<uintptr_t> key;
+  for (int i = 0; i < n; ++i) {
+    if (npart[i] < 0 || (npart[i] > 0 && (!d_lagr[i] || !d_pos[i] || !d_vel[i])))
+      return batch_err(b, "bad particle arrays for plan " + std::to_string(i), AAR_ERR_ARG);
+    int rc = ready(&b->plans[i]->p);
+    if (rc) return batch_err(b, "plan " + std::to_string(i) + ": " + b->plans[i]->p.err, rc);
+    key.insert(key.end(), {(uintptr_t)d_lagr[i], (uintptr_t)npart[i], (uintptr_t)d_pos[i], (uintptr_t)d_vel[i],
+                           (uintptr_t)b->plans[i]->p.generation});
+  }
+  if (!b->exec || key != b->key) {
+    batch_drop_graph(b);
+    int rc = batch_capture(b, d_lagr, npart, d_pos, d_vel);
+    if (rc) return rc;
+    b->key = key;
+  }
+  cudaError_t e = cudaGraphLaunch(b->exec, S(stream));
+  if (e != cudaSuccess) return batch_err(b, std::string("cudaGraphLaunch: ") + cudaGetErrorString(e), AAR_ERR_CUDA);
+  return AAR_OK;
+}
+
+int aar_batch_launch_count(const aar_batch* b) { return b ? b->launches : 0; }
+
+const char* aar_batch_last_error(const aar_batch* b) { return b ? b->err.c_str() : "null batch"; }
+
+void aar_batch_destroy(aar_batch* b) {
+  if (!b) return;
+  batch_drop_graph(b);
+  for (auto st : b->streams) cudaStreamDestroy(st);
+  for (auto ev : b->done) cudaEventDestroy(ev);
+  if (b->fork) cudaEventDestroy(b->fork);
+  if (b->cap) cudaStreamDestroy(b->cap);
+  delete b;
 }
 
 }  // extern "C"

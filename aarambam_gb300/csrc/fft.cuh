@@ -141,9 +141,11 @@ __host__ __device__ constexpr int num_stages(int N, int E) {
   return s;
 }
 
-// padded shared-memory index: one spare slot per 32 entries
-__device__ __forceinline__ int spad(int i) { return i + (i >> 5); }
-__host__ __device__ constexpr int spad_len(int n) { return n + n / 32 + 4; }
+// padded shared-memory index: one spare slot per 16 entries, so that the
+// first Stockham stage's stores (lane j writes j R + r, R = 8 or 16) and the
+// natural-order loads both fall on distinct banks within a half-warp
+__device__ __forceinline__ int spad(int i) { return i + (i >> 4); }
+__host__ __device__ constexpr int spad_len(int n) { return n + n / 16 + 4; }
 
 // Twiddle table for length N in global memory: tw[m] = exp(-2 pi i m / N).
 // Runtime twiddle exp(SIGN 2 pi i m / N).

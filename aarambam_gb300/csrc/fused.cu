@@ -117,7 +117,7 @@ __device__ __forceinline__ float mode_in(const ModalArgs& a, int n, const KCell&
 // while moving a tile between global and shared memory fall in 32 distinct
 // banks.
 __host__ __device__ constexpr int tile_ls(int N) {
-  int base = N + N / 32;
+  int base = N + N / 16;
   return base + ((2 - base % 16) + 16) % 16;
 }
 
@@ -188,64 +188,47 @@ __device__ __forceinline__ int64_t tile_elem(int N, int HP, int o, int c0, int n
   return ((int64_t)o * N + n) * HP + c0 + w;
 }
 
-// Last modal pass: for each active r, forward x transform of slot r, times
-// rho_r(k) (per-|k|^2 table), summed over r with Neumaier compensation (sum
-// and compensation interleaved in shared memory, one float4 per element);
-// then phi <- phi + fnl_n3 * acc, DC = 0 (main.c:1101-1126).
-template <int N, int W>
-__global__ void __launch_bounds__(AxisCfg<N, W>::THREADS, AxisCfg<N, W>::THREADS >= 512 ? 1 : 2) k_modal_xacc(ModalArgs a, float2* phi,
-                                                                           const float2* work, int64_t fs, int HP,
-                                                                           float fnl_n3, const float2* __restrict__ tw,
-                                                                           const DevTerms* __restrict__ dt,
-                                                                           const float* __restrict__ rtab,
-                                                                           int64_t nsq) {
-  using C = AxisCfg<N, W>;
-  extern __shared__ float2 sm[];
-  float4* acc = (float4*)(sm + W * C::LS);  // (sum.x, sum.y, comp.x, comp.y) per tile element
-  int ncol = HP / W;
-  int o = blockIdx.x / ncol, c0 = (blockIdx.x % ncol) * W;
-  const int ky = sidx(o, N);
-  for (int e = threadIdx.x; e < N * W; e += C::THREADS) acc[e] = make_float4(0.f, 0.f, 0.f, 0.f);
+// Last modal step, after the forward x transform of every active slot r:
+// acc = sum_r rho_r(k) g_r(k) (per-|k|^2 table, Neumaier-compensated in
+// registers), then phi <- phi + fnl_n3 * acc, DC = 0 (main.c:1101-1126).
+// One thread per half-spectrum element (padding columns are not touched);
+// cut cells keep phi as it is.  A streaming kernel: the R slot reads of a thread are
+// independent, so many are in flight per SM.
+template <int N>
+__global__ void __launch_bounds__(256) k_modal_acc(ModalArgs a, float2* phi, const float2* __restrict__ work,
+                                                   int64_t fs, int HP, float fnl_n3, const DevTerms* __restrict__ dt,
+                                                   const float* __restrict__ rtab, int rstride) {
+  constexpr int K = N / 2 + 1;  // kz = 0 .. N/2 of a row
+  constexpr int64_t total = (int64_t)N * N * K;
   const int nr = dt->tl.nr;
-  for (int sl = 0; sl < nr; ++sl) {
-    const int r = dt->tl.r_of_slot[sl];
-    __syncthreads();
-    tile_load_async<N, W, 0>(sm, work + (int64_t)r * fs, HP, o, c0);
-    cp_async_commit();
-    cp_async_wait<0>();
-    __syncthreads();
-    tile_fft<N, W, -1>(sm, tw);
-    __syncthreads();
-    const float* rt = rtab + (int64_t)r * nsq;
-    for (int e = threadIdx.x; e < N * W; e += C::THREADS) {
-      int n = e / W, w = e % W;
-      int kz = c0 + w, kx = sidx(n, N);
-      int n2 = kx * kx + ky * ky + kz * kz;
-      if (kz > N / 2 || n2 == 0 || !keep_cell(a.g, kx, ky, kz)) continue;
-      float rho = __ldg(rt + n2);
-      float2 v = sm[w * C::LS + spad(n)];
-      float4 s4 = acc[e];
-      float tx = v.x * rho, ty = v.y * rho;
-      float sx = s4.x + tx, sy = s4.y + ty;
-      s4.z += (fabsf(s4.x) >= fabsf(tx)) ? (s4.x - sx) + tx : (tx - sx) + s4.x;
-      s4.w += (fabsf(s4.y) >= fabsf(ty)) ? (s4.y - sy) + ty : (ty - sy) + s4.y;
-      s4.x = sx;
-      s4.y = sy;
-      acc[e] = s4;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t row = i / K;
+    const int kz = (int)(i - row * K);
+    const int64_t e = row * HP + kz;
+    const int kx = sidx((int)(row / N), N), ky = sidx((int)(row % N), N);
+    const int n2 = kx * kx + ky * ky + kz * kz;
+    if (n2 == 0) {
+      phi[e] = make_float2(0.f, 0.f);
+      continue;
     }
-  }
-  __syncthreads();
-  for (int e = threadIdx.x; e < N * W; e += C::THREADS) {
-    int n = e / W, w = e % W;
-    int kz = c0 + w;
-    if (kz > N / 2) continue;
-    int64_t gi = tile_elem<0>(N, HP, o, c0, n, w);
-    float2 ph = phi[gi];
-    float4 s4 = acc[e];
-    ph.x += fnl_n3 * (s4.x + s4.z);
-    ph.y += fnl_n3 * (s4.y + s4.w);
-    if (n == 0 && o == 0 && kz == 0) ph = make_float2(0.f, 0.f);
-    phi[gi] = ph;
+    if (!keep_cell(a.g, kx, ky, kz)) continue;
+    float sx = 0.f, sy = 0.f, cx = 0.f, cy = 0.f;
+#pragma unroll 4
+    for (int sl = 0; sl < nr; ++sl) {
+      const int r = dt->tl.r_of_slot[sl];
+      const float rho = __ldg(rtab + (int64_t)n2 * rstride + r);
+      const float2 v = __ldg(work + (int64_t)r * fs + e);
+      const float tx = v.x * rho, ty = v.y * rho;
+      const float ux = sx + tx, uy = sy + ty;
+      cx += (fabsf(sx) >= fabsf(tx)) ? (sx - ux) + tx : (tx - ux) + sx;
+      cy += (fabsf(sy) >= fabsf(ty)) ? (sy - uy) + ty : (ty - uy) + sy;
+      sx = ux;
+      sy = uy;
+    }
+    float2 ph = phi[e];
+    ph.x += fnl_n3 * (sx + cx);
+    ph.y += fnl_n3 * (sy + cy);
+    phi[e] = ph;
   }
 }
 
@@ -292,6 +275,35 @@ __device__ __forceinline__ void row_c2r_pre(const float2* __restrict__ X, float2
   }
 }
 
+// The same pre-step in place, on X_0..X_{N/2} already staged in `line`
+// (element k at spad(k)): each lane rewrites the pair (k, H - k) it reads.
+template <int N>
+__device__ __forceinline__ void row_c2r_pre_inplace(float2* line, int t, int T, const float2* __restrict__ twN) {
+  constexpr int H = N / 2;
+  for (int k = t; k <= H / 2; k += T) {
+    int k2 = H - k;
+    float2 a = line[spad(k)], b = line[spad(k2)];
+    if (k == 0) {
+      a.y = 0.f;
+      b.y = 0.f;
+    }
+    float2 w = __ldg(twN + k);
+    w.y = -w.y;
+    float2 e = make_float2(a.x + b.x, a.y - b.y);
+    float2 d = make_float2(a.x - b.x, a.y + b.y);
+    float2 o = cmul(d, w);
+    line[spad(k)] = make_float2(e.x - o.y, e.y + o.x);
+    if (k2 != k && k2 < H) {
+      float2 w2 = __ldg(twN + k2);
+      w2.y = -w2.y;
+      float2 e2 = make_float2(b.x + a.x, b.y - a.y);
+      float2 d2 = make_float2(b.x - a.x, b.y + a.y);
+      float2 o2 = cmul(d2, w2);
+      line[spad(k2)] = make_float2(e2.x - o2.y, e2.y + o2.x);
+    }
+  }
+}
+
 // after the forward half-length FFT of z_n = (x_{2n}, x_{2n+1}) in `line`,
 // write X_k = (Z_k + conj Z_{H-k})/2 - i e^{-2 pi i k/N} (Z_k - conj Z_{H-k})/2
 template <int N>
@@ -312,28 +324,50 @@ __device__ __forceinline__ void row_r2c_post(const float2* line, float2* __restr
 // Generic row kernel.  For each row (blockIdx.x = x*N + y): c2r of `nin`
 // input fields (slots in_slot[]), a per-position combine step Op, r2c of
 // `nout` output lines into slots out_slot[].  One warp per line at a time.
+// THREADS = 256 with two resident blocks per SM: while one block waits at a
+// phase barrier (its last round of lines keeps only some warps busy) the
+// other block's warps issue.
+constexpr int kRowThreads = 256;
 template <int N, class Op>
-__global__ void __launch_bounds__(512, 1) k_rows(Op op, float2* work, int64_t fs, int HP,
-                                              const float2* __restrict__ twN, const float2* __restrict__ twH) {
+__global__ void __launch_bounds__(kRowThreads, 2) k_rows(Op op, float2* work, int64_t fs, int HP,
+                                                       const float2* __restrict__ twN, const float2* __restrict__ twH) {
   using C = RowCfg<N>;
   constexpr int H = C::H;
   extern __shared__ float2 sm[];
   int64_t row = blockIdx.x;
   int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  int nwarps = blockDim.x >> 5;
+  constexpr int nwarps = kRowThreads / 32;
   int sub = lane / C::T, t = lane % C::T;
+  // phase 0: stage X_0..X_{N/2} of every input line at once (one exposed
+  // memory latency per row instead of one per line)
+  for (int l = 0; l < op.nin(); ++l) {
+    const float2* X = work + (int64_t)op.in_slot(l) * fs + row * HP;
+    float2* line = sm + l * C::LS;
+    for (int k = threadIdx.x; k <= H; k += kRowThreads) cp_async8(line + spad(k), X + k);
+  }
+  cp_async_commit();
+  cp_async_wait<0>();
+  __syncthreads();
   // phase 1: inverse transforms
   for (int l0 = warp * C::LPW; l0 < op.nin(); l0 += nwarps * C::LPW) {
     int l = l0 + sub;
     bool act = l < op.nin() && sub < C::LPW;
     float2* line = sm + (act ? l : 0) * C::LS;
-    if (act) row_c2r_pre<N>(work + (int64_t)op.in_slot(l) * fs + row * HP, line, t, C::T, twN);
+    if (act) row_c2r_pre_inplace<N>(line, t, C::T, twN);
     __syncwarp();
     line_fft_smem<H, C::T, +1>(line, t, twH, act);
   }
   __syncthreads();
   // phase 2: per position combine (in place in the line buffers)
-  for (int n = threadIdx.x; n < H; n += blockDim.x) op.combine(sm, n, C::LS);
+  for (int n = threadIdx.x; n < H; n += 2 * kRowThreads) {
+    if (n + kRowThreads < H) {
+      const int pos[2] = {spad(n), spad(n + kRowThreads)};
+      op.template combine<2>(sm, pos, C::LS);
+    } else {
+      const int pos[1] = {spad(n)};
+      op.template combine<1>(sm, pos, C::LS);
+    }
+  }
   __syncthreads();
   // phase 3: forward transforms of the output lines
   for (int l0 = warp * C::LPW; l0 < op.nout(); l0 += nwarps * C::LPW) {
@@ -346,43 +380,69 @@ __global__ void __launch_bounds__(512, 1) k_rows(Op op, float2* work, int64_t fs
   }
 }
 
-// modal products: lines 0..M-1 hold f_p; line r is overwritten by g_r
+// One product term of the row combine, as a kernel parameter: the shared-
+// memory offsets of lines p and q, and bit 31 set for the counter-term that
+// is evaluated early into g_1 (see ModalRowOp).
+struct TermC {
+  uint32_t off;  // p LS | (q LS) << 16 | early << 31
+  float c;
+};
+
+// modal products: lines 0..M-1 hold f_p; line r is overwritten by g_r.  The
+// term list travels in the kernel's parameter space, so every thread reads
+// a term through the uniform constant path; each thread forms two positions
+// per term.
 struct ModalRowOp {
-  int M;
-  const DevTerms* dt;
+  int M, nr;
+  int r_of_slot[kMaxModes];
+  int begin[kMaxModes + 1];
+  TermC t[kMaxTerms];
   __device__ int nin() const { return M; }
   __device__ int in_slot(int l) const { return l; }
-  __device__ int nout() const { return dt->tl.nr; }
-  __device__ int out_line(int l) const { return dt->tl.r_of_slot[l]; }
-  __device__ int out_slot(int l) const { return dt->tl.r_of_slot[l]; }
+  __device__ int nout() const { return nr; }
+  __device__ int out_line(int l) const { return r_of_slot[l]; }
+  __device__ int out_slot(int l) const { return r_of_slot[l]; }
   // Slots in descending r: g_r only needs f_p f_q with p <= q <= r, so once
   // g_r is formed nothing later reads f_r and it is stored over it at once.
   // (The counter-term f_0 f_2 -> g_1 reads f_2 after g_2 has replaced it;
   // that term is evaluated first, in the pass for r = 2, into a register.)
-  __device__ void combine(float2* sm, int n, int LS) const {
-    const int nr = dt->tl.nr;
-    float2 g1_extra = make_float2(0.f, 0.f);
+  template <int K>
+  __device__ void combine(float2* sm, const int* pos, int LS) const {
+    float2 g1_extra[K];
+#pragma unroll
+    for (int i = 0; i < K; ++i) g1_extra[i] = make_float2(0.f, 0.f);
     for (int s = nr - 1; s >= 0; --s) {
-      const int r = dt->tl.r_of_slot[s];
-      float2 acc = make_float2(0.f, 0.f);
-      const int tb = dt->tl.begin[s], te = dt->tl.begin[s + 1];
-      for (int t = tb; t < te; ++t) {
-        Term tm = dt->t[t];
-        float2 fp = sm[tm.p * LS + spad(n)], fq = sm[tm.q * LS + spad(n)];
-        float2 v = make_float2(tm.c * fp.x * fq.x, tm.c * fp.y * fq.y);
-        if (tm.r == r) {
-          acc.x += v.x;
-          acc.y += v.y;
-        } else {  // a term stored early (its r is below this slot's)
-          g1_extra.x += v.x;
-          g1_extra.y += v.y;
+      const int r = r_of_slot[s];
+      float2 acc[K];
+#pragma unroll
+      for (int i = 0; i < K; ++i) acc[i] = make_float2(0.f, 0.f);
+      const int tb = begin[s], te = begin[s + 1];
+#pragma unroll 2
+      for (int ti = tb; ti < te; ++ti) {
+        const TermC tm = t[ti];
+        const int po = (int)(tm.off & 0xFFFFu), qo = (int)((tm.off >> 16) & 0x7FFFu);
+        const bool early = (tm.off >> 31) != 0u;
+#pragma unroll
+        for (int i = 0; i < K; ++i) {
+          const float2 fp = sm[po + pos[i]], fq = sm[qo + pos[i]];
+          const float vx = tm.c * fp.x * fq.x, vy = tm.c * fp.y * fq.y;
+          if (early) {
+            g1_extra[i].x += vx;
+            g1_extra[i].y += vy;
+          } else {
+            acc[i].x += vx;
+            acc[i].y += vy;
+          }
         }
       }
-      if (r == 1) {
-        acc.x += g1_extra.x;
-        acc.y += g1_extra.y;
+#pragma unroll
+      for (int i = 0; i < K; ++i) {
+        if (r == 1) {
+          acc[i].x += g1_extra[i].x;
+          acc[i].y += g1_extra[i].y;
+        }
+        sm[r * LS + pos[i]] = acc[i];
       }
-      sm[r * LS + spad(n)] = acc;
     }
   }
 };
@@ -396,14 +456,18 @@ struct SourceRowOp {
   __device__ int nout() const { return 1; }
   __device__ int out_line(int) const { return 0; }
   __device__ int out_slot(int) const { return out; }
-  __device__ void combine(float2* sm, int n, int LS) const {
-    float2 d[6];
+  template <int K>
+  __device__ void combine(float2* sm, const int* pos, int LS) const {
 #pragma unroll
-    for (int i = 0; i < 6; ++i) d[i] = sm[i * LS + spad(n)];
-    float2 s;
-    s.x = d[0].x * (d[3].x + d[5].x) + d[3].x * d[5].x - d[1].x * d[1].x - d[2].x * d[2].x - d[4].x * d[4].x;
-    s.y = d[0].y * (d[3].y + d[5].y) + d[3].y * d[5].y - d[1].y * d[1].y - d[2].y * d[2].y - d[4].y * d[4].y;
-    sm[spad(n)] = s;
+    for (int i = 0; i < K; ++i) {
+      float2 d[6];
+#pragma unroll
+      for (int c = 0; c < 6; ++c) d[c] = sm[c * LS + pos[i]];
+      float2 s;
+      s.x = d[0].x * (d[3].x + d[5].x) + d[3].x * d[5].x - d[1].x * d[1].x - d[2].x * d[2].x - d[4].x * d[4].x;
+      s.y = d[0].y * (d[3].y + d[5].y) + d[3].y * d[5].y - d[1].y * d[1].y - d[2].y * d[2].y - d[4].y * d[4].y;
+      sm[pos[i]] = s;
+    }
   }
 };
 
@@ -448,7 +512,7 @@ struct ReadArgs {
   int N, HP;
   int64_t fs;           // field stride in floats
   float box, inv_n3, vp1, vp2;
-  double n_over_box;
+  float nb_hi, nb_lo;  // N / Box as a two-float sum
 };
 
 __device__ __forceinline__ void readout_one(const ReadArgs& a, const float* __restrict__ F, float px, float py,
@@ -458,13 +522,38 @@ __device__ __forceinline__ void readout_one(const ReadArgs& a, const float* __re
   int ii[3], jj[3];
   float fr[3];
   for (int d = 0; d < 3; ++d) {
-    double u = (double)p[d] * a.n_over_box;
-    if (!(u >= 0.0)) u = 0.0;  // also catches NaN: the cell index stays inside the grid
-    if (u > (double)N) u = (double)N;
-    int i = (int)u;
-    if (i >= N) i = N - 1;
-    if (i < 0) i = 0;
-    fr[d] = (float)(u - (double)i);
+    // u = Pos N / Box (main.c:1444-1446) to ~1e-7 of a cell in FP32: the
+    // product with a two-float split of N/Box, then the cell index and the
+    // fraction with the reference's clamps (main.c:1452-1463)
+    float hi = p[d] * a.nb_hi;
+    float lo = fmaf(p[d], a.nb_hi, -hi) + p[d] * a.nb_lo;
+    if (!(hi >= 0.f)) {  // also catches NaN: the cell index stays inside the grid
+      hi = 0.f;
+      lo = 0.f;
+    }
+    if (hi > (float)N) {
+      hi = (float)N;
+      lo = 0.f;
+    }
+    const float fl = floorf(hi);
+    int i = (int)fl;
+    float f = (hi - fl) + lo;  // hi - fl is exact
+    if (f < 0.f) {
+      i -= 1;
+      f += 1.f;
+    } else if (f >= 1.f) {
+      i += 1;
+      f -= 1.f;
+    }
+    if (i < 0) {  // (int) truncates: u in (-1, 0) reads cell 0 with a negative fraction
+      f = (float)i + f;
+      i = 0;
+    }
+    if (i >= N) {
+      f += (float)(i - (N - 1));
+      i = N - 1;
+    }
+    fr[d] = f;
     ii[d] = i;
     jj[d] = (i + 1 == N) ? 0 : i + 1;
   }
@@ -560,9 +649,6 @@ struct Launch {
     return (const int*)((const char*)p->d_terms + offsetof(DevTerms, tl) + offsetof(TermList, r_of_slot));
   }
   static int configure(Plan* p) {
-    using A = AxisCfg<N, W>;
-    size_t sm_acc = A::SMEM + sizeof(float4) * N * W;
-    AAR_CUDA_TRY(p, cudaFuncSetAttribute(k_modal_xacc<N, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_acc));
     size_t sm_rows = sizeof(float2) * (size_t)(kMaxModes + 1) * RowCfg<N>::LS;
     AAR_CUDA_TRY(p, cudaFuncSetAttribute(k_rows<N, ModalRowOp>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_rows));
     AAR_CUDA_TRY(p, cudaFuncSetAttribute(k_rows<N, SourceRowOp>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_rows));
@@ -581,21 +667,41 @@ struct Launch {
     if (rc) return rc;
     if ((rc = ypass<+1>(p, p->d_work, a.M, nullptr, st, "modal_ypass_inv"))) return rc;
     size_t sm_rows = sizeof(float2) * (size_t)(a.M + 1) * RowCfg<N>::LS;
-    ModalRowOp op{a.M, (const DevTerms*)p->d_terms};
+    static_assert(sizeof(ModalRowOp) < 32000, "kernel parameter space");
+    ModalRowOp op;
+    {
+      const TermList& tl = *(const TermList*)p->host_terms.data();
+      const Term* ft = (const Term*)(p->host_terms.data() + sizeof(TermList));
+      constexpr int LS = RowCfg<N>::LS;
+      static_assert(kMaxModes * LS < 0x8000, "line offsets fit 15 bits");
+      op.M = a.M;
+      op.nr = tl.nr;
+      for (int i = 0; i < kMaxModes; ++i) op.r_of_slot[i] = tl.r_of_slot[i];
+      for (int i = 0; i <= kMaxModes; ++i) op.begin[i] = tl.begin[i];
+      for (int sl = 0; sl < tl.nr; ++sl)
+        for (int i = tl.begin[sl]; i < tl.begin[sl + 1]; ++i) {
+          const uint32_t early = ft[i].r != tl.r_of_slot[sl] ? 1u : 0u;
+          op.t[i].off = (uint32_t)(ft[i].p * LS) | ((uint32_t)(ft[i].q * LS) << 16) | (early << 31);
+          op.t[i].c = ft[i].c;
+        }
+    }
     {
       ProfScope ps_(p, "modal_rows", st);
-      k_rows<N, ModalRowOp><<<(unsigned)((int64_t)N * N), 512, sm_rows, st>>>(op, p->d_work, fs, p->HP, p->d_twN,
+      k_rows<N, ModalRowOp><<<(unsigned)((int64_t)N * N), kRowThreads, sm_rows, st>>>(op, p->d_work, fs, p->HP, p->d_twN,
                                                                                p->d_twH);
     }
     AAR_CUDA_TRY(p, cudaGetLastError());
     p->last_launches += 1;
     if ((rc = ypass<-1>(p, p->d_work, p->nr_active, slot_map(p), st, "modal_ypass_fwd"))) return rc;
-    using A = AxisCfg<N, W>;
+    {
+      AxisOp<N, W, 0, -1> xf{p->d_work, fs, tiles(p), p->HP, slot_map(p)};
+      if ((rc = run_pass<N>(p, xf, p->nr_active * tiles(p), st, "modal_xfwd"))) return rc;
+    }
     float fnl_n3 = (float)(p->prm.fnl / ((double)N * N * N));
     {
-      ProfScope ps_(p, "modal_xacc", st);
-      k_modal_xacc<N, W><<<(unsigned)tiles(p), A::THREADS, A::SMEM + sizeof(float4) * N * W, st>>>(
-          a, p->d_phik, p->d_work, fs, p->HP, fnl_n3, p->d_twN, (const DevTerms*)p->d_terms, p->d_rtab, p->nsq);
+      ProfScope ps_(p, "modal_acc", st);
+      k_modal_acc<N><<<(unsigned)(p->num_sms * 8), 256, 0, st>>>(a, p->d_phik, p->d_work, fs, p->HP, fnl_n3,
+                                                             (const DevTerms*)p->d_terms, p->d_rtab, p->rtab_stride);
     }
     AAR_CUDA_TRY(p, cudaGetLastError());
     p->last_launches += 1;
@@ -611,7 +717,7 @@ struct Launch {
     SourceRowOp op{6};
     {
       ProfScope ps_(p, "lpt_rows_source", st);
-      k_rows<N, SourceRowOp><<<(unsigned)((int64_t)N * N), 256, sm_rows, st>>>(op, p->d_work, fs, p->HP, p->d_twN,
+      k_rows<N, SourceRowOp><<<(unsigned)((int64_t)N * N), kRowThreads, sm_rows, st>>>(op, p->d_work, fs, p->HP, p->d_twN,
                                                                                 p->d_twH);
     }
     AAR_CUDA_TRY(p, cudaGetLastError());
@@ -708,6 +814,8 @@ static int build_terms(Plan* p) {
   DevTerms* dt = (DevTerms*)p->d_terms;
   AAR_CUDA_TRY(p, cudaMemcpy(&dt->tl, &tl, sizeof(tl), cudaMemcpyHostToDevice));
   if (!flat.empty()) AAR_CUDA_TRY(p, cudaMemcpy(dt->t, flat.data(), sizeof(Term) * flat.size(), cudaMemcpyHostToDevice));
+  p->host_terms.assign((const char*)&tl, (const char*)&tl + sizeof(tl));
+  p->host_terms.insert(p->host_terms.end(), (const char*)flat.data(), (const char*)(flat.data() + flat.size()));
   p->nterms = tl.nterms;
   p->nr_active = nr;
   return AAR_OK;
@@ -746,7 +854,9 @@ static ReadArgs read_args(Plan* p) {
   a.inv_n3 = (float)(1.0 / (double)(float)n3);
   a.vp1 = (float)p->vel_prefac;
   a.vp2 = (float)p->vel_prefac2;
-  a.n_over_box = (double)p->N / p->prm.box;
+  const double nb = (double)p->N / p->prm.box;
+  a.nb_hi = (float)nb;
+  a.nb_lo = (float)(nb - (double)a.nb_hi);
   return a;
 }
 

@@ -209,3 +209,4 @@ struct LptOp {
     tile_store<N, W, 0>(b, work + (int64_t)(MODE == 2 ? 3 + comp : comp) * fs, HP, o, c0);
   }
 };
+

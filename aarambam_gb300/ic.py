@@ -174,3 +174,53 @@ class ICGenerator:
         check(self.L, self.h, self.L.aar_run_host(self.h, lagr.ctypes.data, lagr.shape[0], pos.ctypes.data,
                                                   vel.ctypes.data, self._stream()))
         return pos, vel
+
+
+class ICBatch:
+    """Several ICGenerator plans (each with its own seed, table and mode
+    count, one device) run as one CUDA graph (aar_batch_*): the first run
+    captures every realisation as a branch of the graph, later runs replay it
+    with a single launch on the current stream."""
+
+    def __init__(self, gens):
+        self.gens = list(gens)
+        self.L = _lib.load()
+        arr = (C.c_void_p * len(self.gens))(*[g.h.value for g in self.gens])
+        b = C.c_void_p()
+        rc = self.L.aar_batch_create(arr, len(self.gens), C.byref(b))
+        if rc != _lib.AAR_OK:
+            raise AarError(rc, "aar_batch_create failed (fused plans on one device required)")
+        self.b = b
+        self.device = self.gens[0].device
+
+    def close(self):
+        if getattr(self, "b", None):
+            self.L.aar_batch_destroy(self.b)
+            self.b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def launches(self) -> int:
+        return self.L.aar_batch_launch_count(self.b)
+
+    def run(self, lagrs, poss, vels):
+        """One realisation per plan: lagrs[i] float32 [n_i, 3] on the device;
+        results are written into poss[i], vels[i]."""
+        n = len(self.gens)
+        if not (len(lagrs) == len(poss) == len(vels) == n):
+            raise ValueError("one Lagrangian/position/velocity array per plan")
+        vp = C.c_void_p
+        la = (vp * n)(*[_ptr(t) for t in lagrs])
+        pa = (vp * n)(*[_ptr(t) for t in poss])
+        va = (vp * n)(*[_ptr(t) for t in vels])
+        na = (C.c_int64 * n)(*[t.shape[0] for t in lagrs])
+        stream = C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
+        rc = self.L.aar_batch_run(self.b, la, na, pa, va, stream)
+        if rc != _lib.AAR_OK:
+            msg = self.L.aar_batch_last_error(self.b)
+            raise AarError(rc, msg.decode() if msg else "")

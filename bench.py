@@ -155,7 +155,7 @@ def alg_bytes(name: str, N: int, M: int, R: int, npart: int) -> float:
     table = {
         "seedtable": 4.0 * N * N, "noise": F + 4.0 * N * N,
         "modal_xinv": (1 + M) * F, "modal_ypass_inv": 2 * M * F, "modal_rows": (M + R) * F,
-        "modal_ypass_fwd": 2 * R * F, "modal_xacc": (R + 2) * F,
+        "modal_ypass_fwd": 2 * R * F, "modal_xfwd": 2 * R * F, "modal_acc": (R + 2) * F,
         "lpt_xinv_hess": 7 * F, "lpt_ypass_inv_hess": 12 * F, "lpt_rows_source": 7 * F,
         "lpt_ypass_fwd_source": 2 * F, "lpt_xfwd_source": 2 * F, "lpt_xpsi2": 4 * F, "lpt_xpsi1": 4 * F,
         "lpt_ypass_inv_disp": 12 * F,
@@ -201,14 +201,67 @@ def cpu_baseline(wl: str, n_sample: int, steps: int = 1) -> dict:
     ts = []
     for _ in range(steps):
         t0 = time.perf_counter()
-        o.run(alpha, x0, lagr)
+        ref = o.run(alpha, x0, lagr)
         ts.append(time.perf_counter() - t0)
     t = min(ts)
     cores = os.cpu_count()
-    return {"value": n_sample ** 3 / t, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"oracle FP64 C restatement of the reference path (same {cfg['N_modes']}-mode table, "
-                      f"reference loop structure, OpenMP) on {n_sample}^3 particles/grid, {t:.2f} s/step, "
-                      f"{os.uname().machine}"}
+    out = {"value": n_sample ** 3 / t, "unit": UNIT, "cores": cores, "kind": "port",
+           "sample": f"oracle FP64 C restatement of the reference path (same {cfg['N_modes']}-mode table, "
+                     f"reference loop structure, OpenMP) on {n_sample}^3 particles/grid, {t:.2f} s/step, "
+                     f"{os.uname().machine}"}
+    return out, (cfg, alpha, x0, k, t, lagr, ref)
+
+
+def _rel(a, b) -> float:
+    a, b = np.asarray(a), np.asarray(b)
+    dt = np.complex128 if (np.iscomplexobj(a) or np.iscomplexobj(b)) else np.float64
+    a, b = a.astype(dt), b.astype(dt)
+    return float(np.linalg.norm((a - b).ravel()) / np.linalg.norm(b.ravel()))
+
+
+def _delta(psi1: np.ndarray, box: float) -> np.ndarray:
+    """delta = -div psi1 on the grid (spectral derivative), [3, N, N, N] in."""
+    N = psi1.shape[1]
+    k = 2 * np.pi / box * np.fft.fftfreq(N, 1.0 / N)
+    kz = 2 * np.pi / box * np.arange(N // 2 + 1)
+    ks = [k[:, None, None], k[None, :, None], kz[None, None, :]]
+    d = sum(1j * ks[a] * np.fft.rfftn(psi1[a]) for a in range(3))
+    return -np.fft.irfftn(d, s=(N, N, N))
+
+
+def precision_report(sample) -> dict:
+    """Relative RMS errors of the fused FP32 form (and of the plain FP64 form's
+    displacements) against the FP64 oracle on the cpu_baseline sample."""
+    import torch
+    from aarambam_gb300.ic import ICGenerator
+    cfg, alpha, x0, k, t, lagr, ref = sample
+    N, box = cfg["Nmesh"], cfg["Box"]
+    dev = torch.device("cuda", torch.cuda.current_device())
+    gl = torch.from_numpy(lagr).to(dev)
+    g = ICGenerator(cfg, alpha, x0, k, t)
+    g.stage("noise")
+    g.stage("modal")
+    phik = g.spectrum().cpu().numpy()
+    g.stage("lpt")
+    f = np.stack([g.field(i).double().cpu().numpy() for i in range(6)])
+    pos, _ = g.readout(gl)
+    o_tot = ref["total"][..., 0] + 1j * ref["total"][..., 1]
+    o_disp = ref["disp"]
+
+    def dspl(p):
+        d = np.asarray(p, np.float64) - lagr.astype(np.float64)
+        return d - box * np.round(d / box)
+    want = dspl(ref["pos"].reshape(-1, 3))
+    out = {"n": N, "phi": _rel(phik, o_tot), "delta": _rel(_delta(f[:3], box), _delta(o_disp[:3], box)),
+           "psi1": _rel(f[:3], o_disp[:3]), "psi2": _rel(f[3:], o_disp[3:]),
+           "displacement": _rel(dspl(pos.cpu().numpy()), want)}
+    del g
+    gp = ICGenerator(cfg, alpha, x0, k, t, precision="fp64")
+    pp, _ = gp.run(gl)
+    out["plain_fp64_displacement"] = _rel(dspl(pp.cpu().numpy()), want)
+    del gp
+    torch.cuda.empty_cache()
+    return {k_: (round(v, 12) if isinstance(v, float) else v) for k_, v in out.items()}
 
 
 def replica_seed(rank: int) -> int:
@@ -351,8 +404,10 @@ def gpu_arm(args):
         torch.cuda.empty_cache()
 
     cpu = None
+    precision = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(args.workload, args.cpu_sample_n)
+        cpu, sample = cpu_baseline(args.workload, args.cpu_sample_n)
+        precision = precision_report(sample)
 
     if rank == 0:
         out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -363,7 +418,7 @@ def gpu_arm(args):
                                       f"z=49", "nmesh": N, "n_modes": M, "l2": "working set >> L2 (no flush)",
                           "parallelism": "replicas" if world > 1 else "single GPU"},
                "roofline": roofline, "path_roofline": path_roof, "cpu_baseline": cpu, "e2e": e2e, "plain_fp64": plain,
-               "gpu_launches": launches, "clocks": clocks, "kernels": kernels}
+               "gpu_launches": launches, "clocks": clocks, "precision_vs_fp64_oracle": precision, "kernels": kernels}
         print(json.dumps(out))
     if world > 1:
         dist.destroy_process_group()
@@ -376,11 +431,11 @@ def reference_arm(args):
     cfg = make_cfg(args.workload, 1234)
     n = args.cpu_sample_n
     # size the sample so the whole run stays within a few minutes
-    first = cpu_baseline(args.workload, n, 1)
+    first = cpu_baseline(args.workload, n, 1)[0]
     per = n ** 3 / first["value"]
     while n > 32 and per * (args.steps + args.warmup) > 240:
         n //= 2
-        first = cpu_baseline(args.workload, n, 1)
+        first = cpu_baseline(args.workload, n, 1)[0]
         per = n ** 3 / first["value"]
     for _ in range(max(0, args.warmup - 1)):
         cpu_baseline(args.workload, n, 1)

@@ -153,6 +153,25 @@ int aar_gaussian_spectrum_noalloc(aar_plan* plan, void* d_out, void* stream);
 int aar_c2r(aar_plan* plan, const void* d_in, float* d_out, void* stream);
 int aar_r2c(aar_plan* plan, const float* d_in, void* d_out, void* stream);
 
+/* ---- batches (no counterpart in the reference, whose executable makes one
+   realisation per process) ----
+   Several fused plans (realisations with their own seed, coefficient table,
+   mode count and buffers; one device) run as one CUDA graph.  The first
+   aar_batch_run captures every plan's aar_run work as a branch of the graph
+   (one stream per plan, so small kernels of different realisations overlap);
+   later runs replay it with one graph launch on `stream`.  The graph is
+   captured again when a buffer pointer, a particle count or a plan
+   (aar_set_seed / aar_set_tables / aar_set_transfer) changes.  Arrays are
+   indexed by plan; the plans' profiling is suspended while capturing. */
+typedef struct aar_batch aar_batch;
+int aar_batch_create(aar_plan* const* plans, int32_t nplans, aar_batch** out);
+int aar_batch_run(aar_batch* batch, const float* const* d_lagr_pos, const int64_t* npart, float* const* d_pos,
+                  float* const* d_vel, void* stream);
+/* Kernels in one replay of the batch graph. */
+int aar_batch_launch_count(const aar_batch* batch);
+const char* aar_batch_last_error(const aar_batch* batch);
+void aar_batch_destroy(aar_batch* batch);
+
 /* Per-kernel timing: when enabled, CUDA events are recorded on the launching
    stream around every kernel; aar_profile_report synchronises the device and
    writes "kernel,launches,total_ms" lines for everything recorded since the

@@ -96,6 +96,9 @@ struct Plan {
   };
   std::vector<ProfRec> prof;
   std::vector<cudaEvent_t> event_pool;
+  // adjoint: term / triple tables and coefficient sums (grown on demand)
+  void* d_adj_scratch = nullptr;
+  size_t adj_scratch_bytes = 0;
   // staging buffers of aar_run_host (grown on demand, kept for reuse)
   float* d_io = nullptr;
   int64_t io_cap = 0;
@@ -132,6 +135,10 @@ int fused_c2r(Plan* p, const float2* in, float* out, cudaStream_t st);
 int fused_r2c(Plan* p, const float* in, float2* out, cudaStream_t st);
 int fused_configure_xform(Plan* p);
 int noalloc_gaussian(Plan* p, void* d_out, cudaStream_t st);
+int adj_spectral(Plan* p, int op, int comp, int mode, const float2* in, float2* out, int accumulate,
+                 cudaStream_t st);
+int adj_source(Plan* p, const float* d, const float* gS, float* gd, cudaStream_t st);
+int adj_products(Plan* p, const float* f, const float* gg, float* gf, double* galpha, cudaStream_t st);
 
 }  // namespace aar
 

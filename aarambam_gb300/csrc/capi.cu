@@ -232,7 +232,7 @@ static void plan_release(Plan* p) {
   p->prof.clear();
   for (auto e : p->event_pool) cudaEventDestroy(e);
   p->event_pool.clear();
-  void* ptrs[] = {p->d_phik, p->d_work, p->d_seed, p->d_twN, p->d_twH, p->d_amp, p->d_twb, p->d_rlxpow, p->d_terms, p->d_io, p->d_qtab, p->d_rtab, p->d_sinc};
+  void* ptrs[] = {p->d_phik, p->d_work, p->d_seed, p->d_twN, p->d_twH, p->d_amp, p->d_twb, p->d_rlxpow, p->d_terms, p->d_io, p->d_qtab, p->d_rtab, p->d_sinc, p->d_adj_scratch};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   p->d_phik = p->d_work = nullptr;
@@ -243,6 +243,8 @@ static void plan_release(Plan* p) {
   p->d_qtab = p->d_rtab = nullptr;
   p->d_io = nullptr;
   p->io_cap = 0;
+  p->d_adj_scratch = nullptr;
+  p->adj_scratch_bytes = 0;
   plain_free(p);
 }
 
@@ -699,6 +701,46 @@ int aar_copy_field(aar_plan* h, int32_t which, float* d_out, void* stream) {
   AAR_CUDA_TRY(p, cudaMemcpy2DAsync(d_out, sizeof(float) * N, src, sizeof(float) * 2 * p->HP, sizeof(float) * N,
                                     (size_t)N * N, cudaMemcpyDeviceToDevice, S(stream)));
   return AAR_OK;
+}
+
+// ------------------------------------------------------------- adjoint
+int aar_set_spectrum(aar_plan* h, const void* d_in, void* stream) {
+  if (!h || !d_in) return AAR_ERR_ARG;
+  Plan* p = &h->p;
+  if (p->prm.precision != AAR_FUSED_FP32 || !p->d_phik) return set_err(p, "aar_set_spectrum is for the fused form"), AAR_ERR_ARG;
+  const int N = p->N, H = N / 2 + 1;
+  AAR_CUDA_TRY(p, cudaMemcpy2DAsync(p->d_phik, sizeof(float2) * p->HP, d_in, sizeof(float2) * H, sizeof(float2) * H,
+                                    (size_t)N * N, cudaMemcpyDeviceToDevice, S(stream)));
+  return AAR_OK;
+}
+
+static int adj_ready(Plan* p) {
+  int rc = ready(p);
+  if (rc) return rc;
+  if (p->prm.precision != AAR_FUSED_FP32) return set_err(p, "the adjoint is for the fused form"), AAR_ERR_ARG;
+  return AAR_OK;
+}
+
+int aar_adj_spectral(aar_plan* h, int32_t op, int32_t comp, int32_t mode, const void* d_in, void* d_out,
+                     int32_t accumulate, void* stream) {
+  if (!h || !d_in || !d_out) return AAR_ERR_ARG;
+  int rc = adj_ready(&h->p);
+  if (rc) return rc;
+  return adj_spectral(&h->p, op, comp, mode, (const float2*)d_in, (float2*)d_out, accumulate, S(stream));
+}
+
+int aar_adj_source(aar_plan* h, const float* d_hess, const float* d_gsource, float* d_out, void* stream) {
+  if (!h || !d_hess || !d_gsource || !d_out) return AAR_ERR_ARG;
+  int rc = adj_ready(&h->p);
+  if (rc) return rc;
+  return adj_source(&h->p, d_hess, d_gsource, d_out, S(stream));
+}
+
+int aar_adj_products(aar_plan* h, const float* d_f, const float* d_gg, float* d_gf, double* d_galpha, void* stream) {
+  if (!h || !d_f || !d_gg || !d_gf || !d_galpha) return AAR_ERR_ARG;
+  int rc = adj_ready(&h->p);
+  if (rc) return rc;
+  return adj_products(&h->p, d_f, d_gg, d_gf, d_galpha, S(stream));
 }
 
 // ------------------------------------------------------------- batches

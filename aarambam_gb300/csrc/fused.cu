@@ -31,34 +31,10 @@
 
 #include "aar_internal.cuh"
 #include "fft.cuh"
+#include "spectral.cuh"
 
 namespace aar {
 
-// ----------------------------------------------------------- parameters
-struct ModalArgs {
-  Grid g;
-  float s;          // (4 - ns) / 3
-  float ns;
-  float kmin_s;     // kmin^s
-  float inv_dks;    // 1 / (kmax^s - kmin^s)
-  float ln_kF;      // log(kF)
-  int M;
-  float x0[32];     // X0[n]
-};
-
-struct Term {      // one product f_p f_q with coefficient c into g_r
-  int p, q, r;
-  float c;
-};
-
-constexpr int kMaxModes = 32;
-constexpr int kMaxTerms = 2048;
-
-struct TermList {
-  int nterms, nr;
-  int r_of_slot[kMaxModes];       // active r values (ascending)
-  int begin[kMaxModes + 1];       // terms of slot s: [begin[s], begin[s+1])
-};
 
 // term list in plan-owned device memory (read uniformly by all threads)
 struct DevTerms {
@@ -66,50 +42,6 @@ struct DevTerms {
   Term t[kMaxTerms];
 };
 size_t terms_bytes() { return sizeof(DevTerms); }
-
-// ----------------------------------------------------------- k helpers
-struct KCell {
-  float k2, k1, kbar;
-  bool keep;
-};
-
-__device__ __forceinline__ KCell kcell(const ModalArgs& a, int kx, int ky, int kz) {
-  KCell c;
-  int n2 = kx * kx + ky * ky + kz * kz;
-  c.keep = n2 != 0 && keep_cell(a.g, kx, ky, kz);
-  float nn = (float)(n2 ? n2 : 1);
-  c.k2 = a.g.kF * a.g.kF * nn;
-  c.k1 = a.g.kF * sqrtf(nn);
-  // k^s = exp(s (ln kF + ln n / 2))
-  float ks = expf(a.s * (a.ln_kF + 0.5f * logf(nn)));
-  c.kbar = -1.f + 2.f * (ks - a.kmin_s) * a.inv_dks;
-  return c;
-}
-
-// P_l(x) by the Bonnet recurrence
-__device__ __forceinline__ float legendre(int l, float x) {
-  if (l == 0) return 1.f;
-  float p0 = 1.f, p1 = x;
-  for (int n = 2; n <= l; ++n) {
-    float p2 = ((2 * n - 1) * x * p1 - (n - 1) * p0) / (float)n;
-    p0 = p1;
-    p1 = p2;
-  }
-  return p1;
-}
-
-// radial part of mode n (main.c:833-860): k^{s(n-3)} (n <= 3) or
-// (P_{n-1}(kbar) - X0[n-1]) / k^2
-__device__ __forceinline__ float mode_out(const ModalArgs& a, int n, const KCell& c) {
-  if (n <= 3) return expf(a.s * (float)(n - 3) * logf(c.k1));
-  return (legendre(n - 1, c.kbar) - a.x0[n - 1]) / c.k2;
-}
-// field filter (main.c:606-637): mode_out * k^{4-ns}
-__device__ __forceinline__ float mode_in(const ModalArgs& a, int n, const KCell& c) {
-  float lk = logf(c.k1);
-  if (n <= 3) return expf((a.s * (float)(n - 3) + 4.f - a.ns) * lk);
-  return (legendre(n - 1, c.kbar) - a.x0[n - 1]) * expf((2.f - a.ns) * lk);
-}
 
 // ----------------------------------------------------------- tile passes
 // Line stride of a tile in shared memory: at least the padded line length,
@@ -493,13 +425,6 @@ __global__ void __launch_bounds__(256) k_rows_c2r(float2* work, int64_t fs, int 
 }
 
 // ----------------------------------------------------------- 2LPT passes
-struct LptArgs {
-  ModalArgs m;       // grid and k helpers
-  float inv_Dbeta;   // 1 / (Dplus Beta)
-  const float* twb;  // per n^2: T(k) / (Dplus Beta)
-  const float* sinc; // per grid index: sin(x)/x, x = k Box / 2N (1 at k = 0)
-  float box_over_2n;
-};
 
 __device__ __forceinline__ float sincf(float x) { return x == 0.f ? 1.f : sinf(x) / x; }
 
@@ -762,19 +687,10 @@ static int dispatch_n(int N, F&& f) {
   }
 }
 
-static ModalArgs modal_args(Plan* p) {
+ModalArgs modal_args(Plan* p) {
   ModalArgs a;
   a.g = p->grid;
-  double ns = p->prm.primordial_index;
-  double s = (4 - ns) / 3;
-  double kmin = 2 * kPi / p->prm.box, kmax = 2 * kPi / p->prm.box * p->prm.nmax;
-  a.s = (float)s;
-  a.ns = (float)ns;
-  a.kmin_s = (float)pow(kmin, s);
-  a.inv_dks = (float)(1.0 / (pow(kmax, s) - pow(kmin, s)));
-  a.ln_kF = (float)log(2 * kPi / p->prm.box);
   a.M = p->M;
-  for (int i = 0; i < 32; ++i) a.x0[i] = i < p->M ? (float)p->x0[i] : 0.f;
   return a;
 }
 
@@ -834,13 +750,18 @@ int fused_modal(Plan* p, cudaStream_t st) {
   return dispatch_n(p->N, [&](auto nc) { return Launch<decltype(nc)::value>::modal(p, a, st); });
 }
 
-int fused_lpt(Plan* p, cudaStream_t st) {
+LptArgs lpt_args(Plan* p) {
   LptArgs a;
   a.m = modal_args(p);
   a.inv_Dbeta = (float)(1.0 / (p->Dplus * p->Beta));
   a.twb = p->d_twb;
   a.sinc = p->d_sinc;
   a.box_over_2n = (float)(p->prm.box / 2 / p->N);
+  return a;
+}
+
+int fused_lpt(Plan* p, cudaStream_t st) {
+  LptArgs a = lpt_args(p);
   return dispatch_n(p->N, [&](auto nc) { return Launch<decltype(nc)::value>::lpt(p, a, st); });
 }
 

@@ -127,14 +127,10 @@ struct XinvOp {
 
 // 2LPT passes (MODE 0: Hessians, items tile * 6 + comp; MODE 1: ZA
 // displacements, items tile * 3 + a; MODE 2: 2LPT displacements, items
-// tile * 3 + a).
-//  MODE 0: d_ab = -k_a k_b T/(D Beta) phi (main.c:1238-1277), inverse x FFT
-//  MODE 1: psi1_a = i k_a T/(D Beta) phi smth (main.c:1180-1216), inverse x
-//  MODE 2: psi2_a = -i k_a/k^2 S smth (main.c:1311-1368) from the source
-//          slot already transformed along x, inverse x
-// smth = [sinc(kx Box/2N) sinc(ky Box/2N) sinc(kz Box/2N)]^-2 (CORRECT_CIC),
-// from a per-index sinc table.  Outputs: Hessians to slots 0..5, psi1 to
-// slots 0..2, psi2 to slots 3..5.
+// tile * 3 + a): the factor lpt_factor<MODE> (main.c:1180-1368) on phi, or
+// for MODE 2 on the source slot already transformed along x, then the
+// inverse x FFT.  Outputs: Hessians to slots 0..5, psi1 to slots 0..2, psi2
+// to slots 3..5.
 template <int N, int W, int MODE>
 struct LptOp {
   LptArgs a;
@@ -159,37 +155,16 @@ struct LptOp {
   // multiply the tile in place by the spectral factor of component comp
   __device__ void apply(float2* b, int o, int c0, int comp) const {
     using C = AxisCfg<N, W>;
-    const int ax = MODE == 0 ? (comp < 3 ? 0 : (comp < 5 ? 1 : 2)) : comp;
-    const int bx = MODE == 0 ? (comp == 0 ? 0 : comp == 1 ? 1 : comp == 2 ? 2 : comp == 3 ? 1 : 2) : comp;
     const int ky = sidx(o, N);
-    const float kF = a.m.g.kF;
-    const float sy = MODE == 0 ? 1.f : __ldg(a.sinc + o);
 #pragma unroll 2
     for (int i = 0; i < C::PER; ++i) {
       int e, n, w;
       tile_owned<N, W>(i, e, n, w);
       const int kz = c0 + w, kx = sidx(n, N);
       const int n2 = kx * kx + ky * ky + kz * kz;
-      const float ka = kF * (float)(ax == 0 ? kx : ax == 1 ? ky : kz);
       float2& v = b[w * C::LS + spad(n)];
       float2 r = make_float2(0.f, 0.f);
-      if (kz <= N / 2) {
-        if (MODE == 0) {
-          const float kb = kF * (float)(bx == 0 ? kx : bx == 1 ? ky : kz);
-          float f = -ka * kb * __ldg(a.twb + n2);
-          r = make_float2(v.x * f, v.y * f);
-        } else {
-          float ff = 1.f / (__ldg(a.sinc + n) * sy * __ldg(a.sinc + kz));
-          float smth = ff * ff;
-          if (MODE == 1) {
-            float f = ka * __ldg(a.twb + n2) * smth;
-            r = make_float2(-f * v.y, f * v.x);
-          } else if (n2 > 0) {
-            float f = ka / (kF * kF * (float)n2) * smth;
-            r = make_float2(f * v.y, -f * v.x);
-          }
-        }
-      }
+      if (kz <= N / 2) r = cmul(v, lpt_factor<MODE>(a, comp, n, o, kz, kx, ky, n2));
       v = r;
     }
   }

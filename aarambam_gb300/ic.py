@@ -89,6 +89,19 @@ class ICGenerator:
     def launches(self) -> int:
         return self.L.aar_last_launch_count(self.h)
 
+    @property
+    def n_modes(self) -> int:
+        return self._alpha.shape[0]
+
+    def set_tables(self, alpha: np.ndarray, x0: np.ndarray = None) -> None:
+        """Replace the coefficient tables (no-op when they are unchanged)."""
+        alpha = np.ascontiguousarray(alpha, dtype=np.float64)
+        x0 = self._x0 if x0 is None else np.ascontiguousarray(x0, dtype=np.float64)
+        if alpha.shape == self._alpha.shape and np.array_equal(alpha, self._alpha) and np.array_equal(x0, self._x0):
+            return
+        self._alpha, self._x0 = alpha, x0
+        check(self.L, self.h, self.L.aar_set_tables(self.h, _dptr(self._alpha), _dptr(self._x0), alpha.shape[0]))
+
     def set_seed(self, seed: int) -> None:
         check(self.L, self.h, self.L.aar_set_seed(self.h, int(seed)))
         self.cfg["Seed"] = int(seed)

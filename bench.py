@@ -45,6 +45,13 @@ WORKLOADS = {
     "scalarI_m12_n256": (256, 1000.0, "scalarI_m12_L1000_n512", 12, 512, 100.0),
     "local_m8_n128": (128, 500.0, "local_m8_L500_n128", 8, 128, 10.0),
 }
+# Batching: 32 realisations at 256^3, Box 500, each with its own seed and a
+# template cycling over Local / Equilateral / ScalarI (mass 0.5, 1, 1.5) with
+# 6..16 modes, run as one CUDA graph (aar_batch_*).
+BATCH_TEMPLATES = [("local_m6_L500_n256", 6, 10.0), ("equil_m9_L500_n256", 9, 100.0),
+                   ("scalarI_m10_L500_n256", 10, 100.0), ("scalarI_m13_L500_n256_mu0p5", 13, 100.0),
+                   ("scalarI_m16_L500_n256_mu1p5", 16, 100.0)]
+BATCH_WORKLOADS = {"batch32_n256": (32, 256, 500.0)}
 
 
 def parse():
@@ -53,7 +60,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
-    ap.add_argument("--workload", default="scalarI_m20_n1024", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="scalarI_m20_n1024", choices=sorted(WORKLOADS) + sorted(BATCH_WORKLOADS))
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-n", type=int, default=128)
@@ -203,11 +210,11 @@ def cpu_baseline(wl: str, n_sample: int, steps: int = 1) -> dict:
         t0 = time.perf_counter()
         ref = o.run(alpha, x0, lagr)
         ts.append(time.perf_counter() - t0)
-    t = min(ts)
+    sec = min(ts)
     cores = os.cpu_count()
-    out = {"value": n_sample ** 3 / t, "unit": UNIT, "cores": cores, "kind": "port",
+    out = {"value": n_sample ** 3 / sec, "unit": UNIT, "cores": cores, "kind": "port",
            "sample": f"oracle FP64 C restatement of the reference path (same {cfg['N_modes']}-mode table, "
-                     f"reference loop structure, OpenMP) on {n_sample}^3 particles/grid, {t:.2f} s/step, "
+                     f"reference loop structure, OpenMP) on {n_sample}^3 particles/grid, {sec:.2f} s/step, "
                      f"{os.uname().machine}"}
     return out, (cfg, alpha, x0, k, t, lagr, ref)
 
@@ -226,7 +233,7 @@ def _delta(psi1: np.ndarray, box: float) -> np.ndarray:
     kz = 2 * np.pi / box * np.arange(N // 2 + 1)
     ks = [k[:, None, None], k[None, :, None], kz[None, None, :]]
     d = sum(1j * ks[a] * np.fft.rfftn(psi1[a]) for a in range(3))
-    return -np.fft.irfftn(d, s=(N, N, N))
+    return -np.fft.irfftn(d, s=(N, N, N), axes=(0, 1, 2))
 
 
 def precision_report(sample) -> dict:
@@ -424,10 +431,76 @@ def gpu_arm(args):
         dist.destroy_process_group()
 
 
+def batch_arm(args):
+    """Batching workload: all realisations of the batch per step, one graph
+    launch (value = particles of all realisations / step time)."""
+    import torch
+    from aarambam_gb300 import _lib
+    from aarambam_gb300.ic import ICBatch, ICGenerator
+    _lib.load(build_if_missing=True)
+    nreal, N, box = BATCH_WORKLOADS[args.workload]
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    base = make_cfg("scalarI_m12_n256", 0)
+    gens, bytes_step = [], 0.0
+    for i in range(nreal):
+        tab, M, fnl = BATCH_TEMPLATES[i % len(BATCH_TEMPLATES)]
+        cfg = dict(base, Nmesh=N, Nsample=N, Nmax=256, Box=box, Seed=1234 + i, Fnl=fnl, N_modes=M, table=tab)
+        alpha, x0, k, t = load_tables(tab, M)
+        gens.append(ICGenerator(cfg, alpha, x0, k, t))
+        bytes_step += 4.0 * N ** 3 * (46 + 9 * M)
+    lagr = lattice_positions(N, box, dev)
+    npart = lagr.shape[0]
+    lagrs = [lagr] * nreal
+    poss = [torch.empty_like(lagr) for _ in range(nreal)]
+    vels = [torch.empty_like(lagr) for _ in range(nreal)]
+    b = ICBatch(gens)
+    for _ in range(args.warmup):
+        b.run(lagrs, poss, vels)
+    torch.cuda.synchronize()
+    clk = Clocks(0)
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        b.run(lagrs, poss, vels)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    el = e0.elapsed_time(e1) / 1e3
+    # the same realisations one after another without the graph, for comparison
+    torch.cuda.synchronize()
+    s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s0.record(stream)
+    for g, p, v in zip(gens, poss, vels):
+        g.run(lagr, p, v)
+    s1.record(stream)
+    torch.cuda.synchronize()
+    serial = s0.elapsed_time(s1) / 1e3
+    pk = peaks()
+    per = el / args.steps
+    value = nreal * npart * args.steps / el
+    print(json.dumps({
+        "metric": f"IC particles/s, batch of {nreal} realisations at {N}^3 (fused FP32 form, one CUDA graph)",
+        "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * per, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": f"{args.workload}: {nreal} realisations, {N}^3, Box {box}, templates "
+                               + ", ".join(f"{tb} ({m} modes)" for tb, m, _ in BATCH_TEMPLATES) + " cycled, own seeds",
+                   "nmesh": N, "realisations": nreal, "l2": "working set >> L2 (no flush)"},
+        "roofline": {"kernel": "whole batch graph", "bound": "hbm", "achieved": round(bytes_step / per / 1e9, 1),
+                     "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": round(bytes_step / per / 1e9 / pk["hbm_gbs"], 4),
+                     "traffic": None, "peak_source": pk["source"]},
+        "serial_ms": 1e3 * serial, "graph_speedup_vs_serial": round(serial / per, 3),
+        "gpu_launches": b.launches * args.steps, "clocks": clocks, "cpu_baseline": None, "e2e": None}))
+
+
 def reference_arm(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
+    if args.workload not in WORKLOADS:  # batches: the reference runs one realisation per process
+        args.workload = "scalarI_m12_n256"
     cfg = make_cfg(args.workload, 1234)
     n = args.cpu_sample_n
     # size the sample so the whole run stays within a few minutes
@@ -458,5 +531,7 @@ if __name__ == "__main__":
     a = parse()
     if a.impl == "reference":
         reference_arm(a)
+    elif a.workload in BATCH_WORKLOADS:
+        batch_arm(a)
     else:
         gpu_arm(a)

@@ -153,6 +153,37 @@ int aar_gaussian_spectrum_noalloc(aar_plan* plan, void* d_out, void* stream);
 int aar_c2r(aar_plan* plan, const void* d_in, float* d_out, void* stream);
 int aar_r2c(aar_plan* plan, const float* d_in, void* d_out, void* stream);
 
+/* ---- adjoint of the fused chain (no counterpart in the reference) ----
+   Building blocks of a reverse-mode pass over white noise w -> Gaussian
+   potential -> modal non-Gaussian potential -> ZA + 2LPT displacements
+   (aarambam_gb300/adjoint.py drives them with aar_c2r / aar_r2c).  Complex
+   data are [N][N][N/2+1] float2, real fields [N][N][N] float. */
+#define AAR_ADJ_OP_ONE 0    /* 1 */
+#define AAR_ADJ_OP_GAUSS 1  /* noise amplitude on the cells the noise draw writes (main.c:405-459) */
+#define AAR_ADJ_OP_Q 2      /* field filter q_comp(k) of mode comp (main.c:580-637) */
+#define AAR_ADJ_OP_RHO 3    /* Fnl/N^3 rho_comp(k) of mode comp (main.c:825-867, 1111-1116) */
+#define AAR_ADJ_OP_HESS 4   /* -k_a k_b T/(D Beta), comp 0..5 = 00 01 02 11 12 22 (main.c:1238-1277) */
+#define AAR_ADJ_OP_PSI1 5   /* i k_a T/(D Beta) smth, comp = axis (main.c:1180-1216, 1332-1367) */
+#define AAR_ADJ_OP_PSI2 6   /* -i k_a/k^2 smth, comp = axis (main.c:1311-1368) */
+/* Write d_in into the plan's potential spectrum (what aar_stage_noise
+   would have written), so that aar_stage_modal / aar_stage_lpt continue from
+   a caller-made Gaussian potential. */
+int aar_set_spectrum(aar_plan* plan, const void* d_in, void* stream);
+/* d_out (+)= M(F) d_in per cell, F the factor of (op, comp); mode 0: F,
+   1: conj(F) w, 2: conj(F)/w, 3: conj(F), with w = 1 on the kz = 0 and N/2
+   planes and 2 elsewhere (c2r^T = w r2c, r2c^T = c2r(./w)). */
+int aar_adj_spectral(aar_plan* plan, int32_t op, int32_t comp, int32_t mode, const void* d_in, void* d_out,
+                     int32_t accumulate, void* stream);
+/* Transpose of the 2LPT source: d_hess and d_out are 6 real fields
+   (00 01 02 11 12 22), d_gsource the source gradient. */
+int aar_adj_source(aar_plan* plan, const float* d_hess, const float* d_gsource, float* d_out, void* stream);
+/* Transpose of the modal products g_r = sum alpha' f_p f_q: d_f the M fields
+   f_p, d_gg the M gradients of g_r (zero for unused r), d_gf (out) the M
+   gradients of f_p, d_galpha (out, FP64 [M][M][M]) the gradient with respect
+   to alpha at every sorted index p <= q <= r (the counter-terms of
+   main.c:1045-1050 included); synchronises the stream. */
+int aar_adj_products(aar_plan* plan, const float* d_f, const float* d_gg, float* d_gf, double* d_galpha, void* stream);
+
 /* ---- batches (no counterpart in the reference, whose executable makes one
    realisation per process) ----
    Several fused plans (realisations with their own seed, coefficient table,

@@ -42,7 +42,7 @@ def _stale(obj: str, src: str) -> bool:
 
 def build(verbose: bool = False) -> str:
     os.makedirs(OUT, exist_ok=True)
-    flags = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
+    flags = ["-std=c++20", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
              "-I" + os.path.join(os.path.dirname(HERE), "include")] + ARCH
     procs = []
     objs = []

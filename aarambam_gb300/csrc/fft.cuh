@@ -11,6 +11,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <utility>
+
 namespace aar {
 
 // ---------------------------------------------------------------- complex
@@ -155,46 +157,113 @@ __device__ __forceinline__ float2 tw_load(const float2* __restrict__ tw, int m) 
   return SIGN < 0 ? w : make_float2(w.x, -w.y);
 }
 
+// Shared-memory addresses of the stage loads and stores.  With the padding
+// spad(i) = i + i/16, an index t-part + C (C a multiple of 16) pads to
+// spad(t-part) + C + C/16, so a lane computes one padded base per stage and
+// every other address is that base plus a compile-time constant.  This holds
+// for the loads (t + T b + r N/R) when T and N/R are multiples of 16, and for
+// the stores when the span Ns divides T (j/Ns = t/Ns + T b/Ns, j%Ns = t%Ns;
+// the r Ns part never carries into the next 16-block together with t%Ns) or
+// Ns = N/R (the last stage: base = j + r Ns).  Other shapes (short lines)
+// use the plain formula.
+template <int N, int T, int R>
+struct LoadAddr {
+  static constexpr bool kAffine = T % 16 == 0 && (N / R) % 16 == 0;
+  static __device__ __forceinline__ int base(int t) { return t + (t >> 4); }
+  template <int B, int RR>
+  static __device__ __forceinline__ int at(int pb, int t) {
+    constexpr int C = T * B + RR * (N / R);
+    if constexpr (kAffine) return pb + C + C / 16;
+    else return spad(t + C);
+  }
+};
+
+template <int N, int T, int R, int Ns>
+struct StoreAddr {
+  static constexpr bool kLast = Ns * R == N;
+  static constexpr bool kDivides = !kLast && T % Ns == 0 && Ns * R >= 16 && (T * R) % 16 == 0;
+  static constexpr bool kAffine = kLast ? (T % 16 == 0 && Ns % 16 == 0) : kDivides;
+  static __device__ __forceinline__ int base(int t) {
+    if constexpr (kLast) {
+      return t + (t >> 4);
+    } else {
+      const int u0 = (t / Ns) * Ns * R + (t % Ns);
+      return u0 + (u0 >> 4);
+    }
+  }
+  template <int B, int RR>
+  static __device__ __forceinline__ int at(int pb, int t) {
+    if constexpr (kAffine) {
+      if constexpr (kLast) {
+        constexpr int C = T * B + RR * Ns;
+        return pb + C + C / 16;
+      } else {
+        constexpr int C = T * B * R;  // from j/Ns = t/Ns + T B/Ns
+        constexpr int D = RR * Ns;
+        return pb + C + C / 16 + D + (D >> 4);
+      }
+    } else {
+      const int j = t + T * B;
+      return spad((j / Ns) * Ns * R + (j % Ns) + RR * Ns);
+    }
+  }
+};
+
+template <int B, int NB, int R, class F>
+__device__ __forceinline__ void unroll_br(F&& f) {
+  if constexpr (B < NB) {
+    [&]<int... RR>(std::integer_sequence<int, RR...>) { (f.template operator()<B, RR>(), ...); }(
+        std::make_integer_sequence<int, R>{});
+    unroll_br<B + 1, NB, R>(f);
+  }
+}
+
 // One Stockham stage on the values a lane holds: v[b*R + r] = x[j + r N/R],
-// j = t + T b.  On return v[b*R + r] = y[(j/Ns) Ns R + j%Ns + r Ns].
+// j = t + T b.  On return v[b*R + r] = y[(j/Ns) Ns R + j%Ns + r Ns].  When Ns
+// divides T the twiddle exponent k = j mod Ns = t mod Ns is the same for
+// every group b, so the R - 1 twiddles are loaded once per stage.
 template <int N, int T, int R, int Ns, int SIGN>
 __device__ __forceinline__ void stage_compute(float2* v, int t, const float2* __restrict__ tw) {
   constexpr int E = N / T;
+  if constexpr (Ns > 1 && T % Ns == 0 && E / R > 1) {
+    const int k = t % Ns;
+    float2 w[R];
 #pragma unroll
-  for (int b = 0; b < E / R; ++b) {
-    int j = t + T * b;
-    if constexpr (Ns > 1) {
-      int k = j % Ns;
+    for (int r = 1; r < R; ++r) w[r] = tw_load<SIGN>(tw, r * k * (N / (Ns * R)));
 #pragma unroll
-      for (int r = 1; r < R; ++r) v[b * R + r] = cmul(v[b * R + r], tw_load<SIGN>(tw, r * k * (N / (Ns * R))));
+    for (int b = 0; b < E / R; ++b) {
+#pragma unroll
+      for (int r = 1; r < R; ++r) v[b * R + r] = cmul(v[b * R + r], w[r]);
+      DFT<R, SIGN>::run(v + b * R);
     }
-    DFT<R, SIGN>::run(v + b * R);
+  } else {
+#pragma unroll
+    for (int b = 0; b < E / R; ++b) {
+      int j = t + T * b;
+      if constexpr (Ns > 1) {
+        int k = j % Ns;
+#pragma unroll
+        for (int r = 1; r < R; ++r) v[b * R + r] = cmul(v[b * R + r], tw_load<SIGN>(tw, r * k * (N / (Ns * R))));
+      }
+      DFT<R, SIGN>::run(v + b * R);
+    }
   }
 }
 
 // Write stage outputs into the line buffer (natural index, padded).
 template <int N, int T, int R, int Ns>
 __device__ __forceinline__ void stage_store(const float2* v, float2* s, int t) {
-  constexpr int E = N / T;
-#pragma unroll
-  for (int b = 0; b < E / R; ++b) {
-    int j = t + T * b;
-    int base = (j / Ns) * Ns * R + (j % Ns);
-#pragma unroll
-    for (int r = 0; r < R; ++r) s[spad(base + r * Ns)] = v[b * R + r];
-  }
+  using A = StoreAddr<N, T, R, Ns>;
+  const int pb = A::base(t);
+  unroll_br<0, N / T / R, R>([&]<int B, int RR>() { s[A::template at<B, RR>(pb, t)] = v[B * R + RR]; });
 }
 
 // Read the inputs of a stage of radix R from the line buffer.
 template <int N, int T, int R>
 __device__ __forceinline__ void stage_load(float2* v, const float2* s, int t) {
-  constexpr int E = N / T;
-#pragma unroll
-  for (int b = 0; b < E / R; ++b) {
-    int j = t + T * b;
-#pragma unroll
-    for (int r = 0; r < R; ++r) v[b * R + r] = s[spad(j + r * (N / R))];
-  }
+  using A = LoadAddr<N, T, R>;
+  const int pb = A::base(t);
+  unroll_br<0, N / T / R, R>([&]<int B, int RR>() { v[B * R + RR] = s[A::template at<B, RR>(pb, t)]; });
 }
 
 // Barrier among the T lanes that share a line: a warp barrier when the line

@@ -62,7 +62,7 @@ struct AxisCfg {
   static constexpr int LS = tile_ls(N);  // smem line stride (float2)
   static constexpr size_t SMEM = sizeof(float2) * (size_t)W * LS;
   static constexpr int PER = N * W / THREADS;  // tile elements per thread
-  static constexpr int MINB = THREADS >= 512 ? 2 : 3;  // resident blocks per SM aimed at
+  static constexpr int MINB = THREADS >= 512 ? 2 : 4;  // resident blocks per SM aimed at
 };
 
 // asynchronous global -> shared copies (sm_80+ cp.async), 8 bytes each
@@ -76,30 +76,52 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(K) : "memory");
 }
 
-template <int AXIS>
-__device__ __forceinline__ int64_t tile_elem(int N, int HP, int o, int c0, int n, int w);
+// Tile indexing.  Axis 0 (x): rows n = x, other index o = y.  Axis 1 (y):
+// rows n = y, o = x.  Column w covers kz = c0 + w.
+// Tile element ownership: thread t owns column w = t % W and rows
+// n = t / W + q THREADS/W, q < PER; with THREADS/W a multiple of 16 the
+// padded shared index and the global offset are a per-thread base plus a
+// compile-time (shared) or per-launch (global) stride times q.
+template <int N, int W, int AXIS>
+struct TileAddr {
+  using C = AxisCfg<N, W>;
+  static constexpr int DN = C::THREADS / W;  // row step between a thread's elements
+  int w, n0, sbase;
+  int64_t gbase, gstep;
+  __device__ __forceinline__ TileAddr(int HP, int o, int c0) {
+    w = threadIdx.x % W;
+    n0 = threadIdx.x / W;
+    sbase = w * C::LS + spad(n0);
+    if (AXIS == 0) {
+      gbase = ((int64_t)n0 * N + o) * HP + c0 + w;
+      gstep = (int64_t)DN * N * HP;
+    } else {
+      gbase = ((int64_t)o * N + n0) * HP + c0 + w;
+      gstep = (int64_t)DN * HP;
+    }
+  }
+  __device__ __forceinline__ int s(int q) const {
+    if constexpr (DN % 16 == 0) return sbase + q * (DN + DN / 16);
+    else return w * C::LS + spad(n0 + q * DN);
+  }
+  __device__ __forceinline__ int64_t g(int q) const { return gbase + q * gstep; }
+};
 
 // issue the asynchronous copy of a tile (rows along AXIS) into shared memory
 template <int N, int W, int AXIS>
 __device__ __forceinline__ void tile_load_async(float2* sm, const float2* __restrict__ f, int HP, int o, int c0) {
   using C = AxisCfg<N, W>;
+  const TileAddr<N, W, AXIS> ta(HP, o, c0);
 #pragma unroll 4
-  for (int q = 0; q < C::PER; ++q) {
-    int e = threadIdx.x + C::THREADS * q;
-    int n = e / W, w = e % W;
-    cp_async8(sm + w * C::LS + spad(n), f + tile_elem<AXIS>(N, HP, o, c0, n, w));
-  }
+  for (int q = 0; q < C::PER; ++q) cp_async8(sm + ta.s(q), f + ta.g(q));
 }
 
 template <int N, int W, int AXIS>
 __device__ __forceinline__ void tile_store(const float2* sm, float2* __restrict__ f, int HP, int o, int c0) {
   using C = AxisCfg<N, W>;
+  const TileAddr<N, W, AXIS> ta(HP, o, c0);
 #pragma unroll 4
-  for (int q = 0; q < C::PER; ++q) {
-    int e = threadIdx.x + C::THREADS * q;
-    int n = e / W, w = e % W;
-    f[tile_elem<AXIS>(N, HP, o, c0, n, w)] = sm[w * C::LS + spad(n)];
-  }
+  for (int q = 0; q < C::PER; ++q) f[ta.g(q)] = sm[ta.s(q)];
 }
 
 // run the W line FFTs of a tile held in shared memory
@@ -110,14 +132,6 @@ __device__ __forceinline__ void tile_fft(float2* sm, const float2* __restrict__ 
   int t = threadIdx.x % C::T;
   bool act = line < W;
   line_fft_smem<N, C::T, SIGN>(sm + (act ? line : 0) * C::LS, t, tw, act, 1 + (act ? line : 0));
-}
-
-// Tile indexing.  Axis 0 (x): rows n = x, other index o = y.  Axis 1 (y):
-// rows n = y, o = x.  Column w covers kz = c0 + w.
-template <int AXIS>
-__device__ __forceinline__ int64_t tile_elem(int N, int HP, int o, int c0, int n, int w) {
-  if (AXIS == 0) return ((int64_t)n * N + o) * HP + c0 + w;
-  return ((int64_t)o * N + n) * HP + c0 + w;
 }
 
 // Last modal step, after the forward x transform of every active slot r:

@@ -6,8 +6,11 @@
 // persistent loop over items lets the compiler keep loop-invariant twiddles
 // live across items and spill, and a second tile buffer for prefetching
 // halves the resident blocks; both were slower.)  An Op supplies
+//   early(f, item)    per-element factors of the prologue (table lookups),
+//                     issued before the tile wait so that both latencies
+//                     overlap (f: one float per owned element, or nothing)
 //   load(buf, item)   issue the cp.async copy of the item's input tile
-//   pre(buf, item)    optional in-place prologue once the tile has landed
+//   pre(buf, item, f) optional in-place prologue once the tile has landed
 //                     (returns true when it wrote shared memory)
 //   body(buf, item)   the FFT(s) and mid-stage work (ends with a barrier)
 //   store(buf, item)  epilogue + store to global memory
@@ -23,19 +26,23 @@ __global__ void __launch_bounds__(AxisCfg<N, W>::THREADS, AxisCfg<N, W>::MINB) k
   const int64_t it = blockIdx.x;
   op.load(sm, it);
   cp_async_commit();
+  typename Op::Early f;
+  op.early(f, it);
   cp_async_wait<0>();
   __syncthreads();
-  if (op.pre(sm, it)) __syncthreads();
+  if (op.pre(sm, it, f)) __syncthreads();
   op.body(sm, it, tw);
   op.store(sm, it);
 }
 
-// element (n, w) of the e-th entry a thread owns in a tile
+// element (n, w) of the i-th entry a thread owns in a tile (column w =
+// t % W, rows t / W + i THREADS/W, as TileAddr lays them out)
 template <int N, int W>
 __device__ __forceinline__ void tile_owned(int i, int& e, int& n, int& w) {
-  e = threadIdx.x + AxisCfg<N, W>::THREADS * i;
-  n = e / W;
-  w = e % W;
+  constexpr int DN = AxisCfg<N, W>::THREADS / W;
+  w = threadIdx.x % W;
+  n = threadIdx.x / W + i * DN;
+  e = n * W + w;
 }
 
 // In-place complex FFT along AXIS of fields (slot_map[f] or f), items
@@ -61,7 +68,9 @@ struct AxisOp {
     coords(item, o, c0);
     tile_load_async<N, W, AXIS>(b, field(item), HP, o, c0);
   }
-  __device__ bool pre(float2*, int64_t) const { return false; }
+  struct Early {};
+  __device__ void early(Early&, int64_t) const {}
+  __device__ bool pre(float2*, int64_t, const Early&) const { return false; }
   __device__ void body(float2* b, int64_t, const float2* tw) const {
     tile_fft<N, W, SIGN>(b, tw);
     __syncthreads();
@@ -95,13 +104,16 @@ struct XinvOp {
     coords(item, o, c0, p);
     tile_load_async<N, W, 0>(b, phi, HP, o, c0);
   }
-  __device__ bool pre(float2* b, int64_t item) const {
+  struct Early {
+    float f[AxisCfg<N, W>::PER];
+  };
+  __device__ void early(Early& r, int64_t item) const {
     using C = AxisCfg<N, W>;
     int o, c0, p;
     coords(item, o, c0, p);
     const int ky = sidx(o, N);
     const float* q = qtab + (int64_t)p * nsq;
-#pragma unroll 4
+#pragma unroll
     for (int i = 0; i < C::PER; ++i) {
       int e, n, w;
       tile_owned<N, W>(i, e, n, w);
@@ -109,8 +121,17 @@ struct XinvOp {
       int n2 = kx * kx + ky * ky + kz * kz;
       float f = 0.f;
       if (kz <= N / 2 && n2 != 0 && keep_cell(a.g, kx, ky, kz)) f = __ldg(q + n2);
+      r.f[i] = f;
+    }
+  }
+  __device__ bool pre(float2* b, int64_t, const Early& r) const {
+    using C = AxisCfg<N, W>;
+#pragma unroll
+    for (int i = 0; i < C::PER; ++i) {
+      int e, n, w;
+      tile_owned<N, W>(i, e, n, w);
       float2& v = b[w * C::LS + spad(n)];
-      v = make_float2(v.x * f, v.y * f);
+      v = make_float2(v.x * r.f[i], v.y * r.f[i]);
     }
     return true;
   }
@@ -152,26 +173,40 @@ struct LptOp {
     const float2* src = MODE == 2 ? work + (int64_t)src_slot * fs : phi;
     tile_load_async<N, W, 0>(b, src, HP, o, c0);
   }
-  // multiply the tile in place by the spectral factor of component comp
-  __device__ void apply(float2* b, int o, int c0, int comp) const {
+  // the spectral factor of component comp per owned element: real for
+  // MODE 0, imaginary for MODE 1 and 2 (stored as its imaginary part)
+  struct Early {
+    float f[AxisCfg<N, W>::PER];
+  };
+  __device__ void early(Early& r, int64_t item) const {
     using C = AxisCfg<N, W>;
+    int o, c0, comp;
+    coords(item, o, c0, comp);
     const int ky = sidx(o, N);
-#pragma unroll 2
+#pragma unroll
     for (int i = 0; i < C::PER; ++i) {
       int e, n, w;
       tile_owned<N, W>(i, e, n, w);
       const int kz = c0 + w, kx = sidx(n, N);
       const int n2 = kx * kx + ky * ky + kz * kz;
-      float2& v = b[w * C::LS + spad(n)];
-      float2 r = make_float2(0.f, 0.f);
-      if (kz <= N / 2) r = cmul(v, lpt_factor<MODE>(a, comp, n, o, kz, kx, ky, n2));
-      v = r;
+      float f = 0.f;
+      if (kz <= N / 2) {
+        const float2 g = lpt_factor<MODE>(a, comp, n, o, kz, kx, ky, n2);
+        f = MODE == 0 ? g.x : g.y;
+      }
+      r.f[i] = f;
     }
   }
-  __device__ bool pre(float2* b, int64_t item) const {
-    int o, c0, comp;
-    coords(item, o, c0, comp);
-    apply(b, o, c0, comp);
+  __device__ bool pre(float2* b, int64_t, const Early& r) const {
+    using C = AxisCfg<N, W>;
+#pragma unroll
+    for (int i = 0; i < C::PER; ++i) {
+      int e, n, w;
+      tile_owned<N, W>(i, e, n, w);
+      float2& v = b[w * C::LS + spad(n)];
+      const float f = r.f[i];
+      v = MODE == 0 ? make_float2(v.x * f, v.y * f) : make_float2(-f * v.y, f * v.x);
+    }
     return true;
   }
   __device__ void body(float2* b, int64_t item, const float2* tw) const {

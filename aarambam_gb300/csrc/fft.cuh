@@ -282,9 +282,12 @@ __device__ __forceinline__ void line_sync(int bar_id) {
 // this together; lanes with act == false (no line of their own) only take
 // part in the barriers.  bar_id names the barrier of a line spread over
 // several warps.
-template <int N, int T, int SIGN, int S = 0>
+// SCALE multiplies the values of the first stage as they are loaded (line
+// element t + T b + r N/R sits at v[b R + r]) by sc[b R + r] (SCALE 1) or by
+// i sc[b R + r] (SCALE 2): a per-element filter folded into the transform.
+template <int N, int T, int SIGN, int S = 0, int SCALE = 0>
 __device__ __forceinline__ void line_fft_smem(float2* s, int t, const float2* __restrict__ tw, bool act,
-                                              int bar_id = 1) {
+                                              int bar_id = 1, const float* sc = nullptr) {
   constexpr int E = N / T;
   constexpr int NS = num_stages(N, E);
   if constexpr (S < NS) {
@@ -292,14 +295,27 @@ __device__ __forceinline__ void line_fft_smem(float2* s, int t, const float2* __
     constexpr int Ns = stage_span(N, E, S);
     float2 v[E];
     if (act) stage_load<N, T, R>(v, s, t);
+    if constexpr (S == 0 && SCALE != 0) {
+#pragma unroll
+      for (int i = 0; i < E; ++i)
+        v[i] = SCALE == 1 ? make_float2(v[i].x * sc[i], v[i].y * sc[i]) : make_float2(-sc[i] * v[i].y, sc[i] * v[i].x);
+    }
     line_sync<T>(bar_id);
     if (act) {
       stage_compute<N, T, R, Ns, SIGN>(v, t, tw);
       stage_store<N, T, R, Ns>(v, s, t);
     }
     line_sync<T>(bar_id);
-    line_fft_smem<N, T, SIGN, S + 1>(s, t, tw, act, bar_id);
+    line_fft_smem<N, T, SIGN, S + 1, 0>(s, t, tw, act, bar_id);
   }
+}
+
+// Line index of the i-th value a lane holds after the first stage load.
+template <int N, int T>
+__host__ __device__ constexpr int first_load_index(int t, int i) {
+  constexpr int E = N / T;
+  constexpr int R = stage_radix(N, E, 0);
+  return t + T * (i / R) + (i % R) * (N / R);
 }
 
 // lanes per line: 16 values per lane for N >= 512, 8 below

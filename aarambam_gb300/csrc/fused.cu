@@ -124,22 +124,28 @@ __device__ __forceinline__ void tile_store(const float2* sm, float2* __restrict_
   for (int q = 0; q < C::PER; ++q) f[ta.g(q)] = sm[ta.s(q)];
 }
 
-// run the W line FFTs of a tile held in shared memory
-template <int N, int W, int SIGN>
-__device__ __forceinline__ void tile_fft(float2* sm, const float2* __restrict__ tw) {
+// run the W line FFTs of a tile held in shared memory (SCALE: optional
+// per-element factors of the first stage, see line_fft_smem)
+template <int N, int W, int SIGN, int SCALE = 0>
+__device__ __forceinline__ void tile_fft(float2* sm, const float2* __restrict__ tw, const float* sc = nullptr) {
   using C = AxisCfg<N, W>;
+  // lines spread over several warps synchronise on named barriers 1..W;
+  // barrier ids stop at 15
+  static_assert(C::T <= 32 || W <= 15, "too many multi-warp lines per tile for the named barriers");
   int line = threadIdx.x / C::T;
   int t = threadIdx.x % C::T;
   bool act = line < W;
-  line_fft_smem<N, C::T, SIGN>(sm + (act ? line : 0) * C::LS, t, tw, act, 1 + (act ? line : 0));
+  line_fft_smem<N, C::T, SIGN, 0, SCALE>(sm + (act ? line : 0) * C::LS, t, tw, act, 1 + (act ? line : 0), sc);
 }
 
 // Last modal step, after the forward x transform of every active slot r:
 // acc = sum_r rho_r(k) g_r(k) (per-|k|^2 table, Neumaier-compensated in
 // registers), then phi <- phi + fnl_n3 * acc, DC = 0 (main.c:1101-1126).
 // One thread per half-spectrum element (padding columns are not touched);
-// cut cells keep phi as it is.  A streaming kernel: the R slot reads of a thread are
-// independent, so many are in flight per SM.
+// cut cells keep phi as it is.  A streaming kernel: the R slot reads of a
+// thread are independent, so many are in flight per SM.  (Measured: pairs of
+// cells per thread with 16-byte loads were slower, 36.5 vs 30.8 ms at
+// 1024^3; so was the slot list as a kernel parameter, 39.0 ms.)
 template <int N>
 __global__ void __launch_bounds__(256) k_modal_acc(ModalArgs a, float2* phi, const float2* __restrict__ work,
                                                    int64_t fs, int HP, float fnl_n3, const DevTerms* __restrict__ dt,
@@ -158,11 +164,12 @@ __global__ void __launch_bounds__(256) k_modal_acc(ModalArgs a, float2* phi, con
       continue;
     }
     if (!keep_cell(a.g, kx, ky, kz)) continue;
+    const float* rt = rtab + (int64_t)n2 * rstride;
     float sx = 0.f, sy = 0.f, cx = 0.f, cy = 0.f;
 #pragma unroll 4
-    for (int sl = 0; sl < nr; ++sl) {
-      const int r = dt->tl.r_of_slot[sl];
-      const float rho = __ldg(rtab + (int64_t)n2 * rstride + r);
+    for (int k = 0; k < nr; ++k) {
+      const int r = dt->tl.r_of_slot[k];
+      const float rho = __ldg(rt + r);
       const float2 v = __ldg(work + (int64_t)r * fs + e);
       const float tx = v.x * rho, ty = v.y * rho;
       const float ux = sx + tx, uy = sy + ty;
@@ -275,7 +282,7 @@ __device__ __forceinline__ void row_r2c_post(const float2* line, float2* __restr
 // other block's warps issue.
 constexpr int kRowThreads = 256;
 template <int N, class Op>
-__global__ void __launch_bounds__(kRowThreads, 2) k_rows(Op op, float2* work, int64_t fs, int HP,
+__global__ void __launch_bounds__(kRowThreads, Op::min_blocks(N)) k_rows(Op op, float2* work, int64_t fs, int HP,
                                                        const float2* __restrict__ twN, const float2* __restrict__ twH) {
   using C = RowCfg<N>;
   constexpr int H = C::H;
@@ -339,6 +346,9 @@ struct TermC {
 // a term through the uniform constant path; each thread forms two positions
 // per term.
 struct ModalRowOp {
+  // resident rows per SM: shared memory holds two at 1024^3 with 20 modes;
+  // below that registers decide (three rows: 80 registers, no spill)
+  static constexpr int min_blocks(int n) { return n >= 1024 ? 2 : 3; }
   int M, nr;
   int r_of_slot[kMaxModes];
   int begin[kMaxModes + 1];
@@ -396,6 +406,7 @@ struct ModalRowOp {
 // 2LPT source (main.c:1284-1294): lines 0..5 hold d00 d01 d02 d11 d12 d22;
 // the source goes to line 0, written to slot `out`.
 struct SourceRowOp {
+  static constexpr int min_blocks(int) { return 4; }  // seven lines per row
   int out;
   __device__ int nin() const { return 6; }
   __device__ int in_slot(int l) const { return l; }
@@ -521,7 +532,7 @@ __device__ __forceinline__ void readout_one(const ReadArgs& a, const float* __re
   }
 }
 
-__global__ void k_readout(ReadArgs a, const float* __restrict__ F, const float* __restrict__ lagr, int64_t np,
+__global__ void __launch_bounds__(256, 6) k_readout(ReadArgs a, const float* __restrict__ F, const float* __restrict__ lagr, int64_t np,
                           float* pos, float* vel) {
   int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= np) return;
@@ -640,7 +651,8 @@ struct Launch {
     {
       ProfScope ps_(p, "modal_acc", st);
       k_modal_acc<N><<<(unsigned)(p->num_sms * 8), 256, 0, st>>>(a, p->d_phik, p->d_work, fs, p->HP, fnl_n3,
-                                                             (const DevTerms*)p->d_terms, p->d_rtab, p->rtab_stride);
+                                                             (const DevTerms*)p->d_terms, p->d_rtab,
+                                                             p->rtab_stride);
     }
     AAR_CUDA_TRY(p, cudaGetLastError());
     p->last_launches += 1;

@@ -6,13 +6,15 @@
 // persistent loop over items lets the compiler keep loop-invariant twiddles
 // live across items and spill, and a second tile buffer for prefetching
 // halves the resident blocks; both were slower.)  An Op supplies
-//   early(f, item)    per-element factors of the prologue (table lookups),
+//   early(f, item)    per-element filter factors (table lookups) for the
+//                     values this thread loads in the first FFT stage,
 //                     issued before the tile wait so that both latencies
-//                     overlap (f: one float per owned element, or nothing)
+//                     overlap; the factors are applied as the first stage
+//                     loads its values (no separate pass over the tile)
 //   load(buf, item)   issue the cp.async copy of the item's input tile
 //   pre(buf, item, f) optional in-place prologue once the tile has landed
 //                     (returns true when it wrote shared memory)
-//   body(buf, item)   the FFT(s) and mid-stage work (ends with a barrier)
+//   body(buf, item, tw, f)  the FFT(s) (ends with a barrier)
 //   store(buf, item)  epilogue + store to global memory
 // Consecutive items run at the same time on consecutive blocks, so items
 // that share an input tile (one phi tile for the M filters, the six 2LPT
@@ -31,18 +33,19 @@ __global__ void __launch_bounds__(AxisCfg<N, W>::THREADS, AxisCfg<N, W>::MINB) k
   cp_async_wait<0>();
   __syncthreads();
   if (op.pre(sm, it, f)) __syncthreads();
-  op.body(sm, it, tw);
+  op.body(sm, it, tw, f);
   op.store(sm, it);
 }
 
-// element (n, w) of the i-th entry a thread owns in a tile (column w =
-// t % W, rows t / W + i THREADS/W, as TileAddr lays them out)
+// The (row n, column w) of the i-th value this thread takes in the first FFT
+// stage of a tile (line w = thread / T, lane t = thread % T); false for
+// threads without a line.
 template <int N, int W>
-__device__ __forceinline__ void tile_owned(int i, int& e, int& n, int& w) {
-  constexpr int DN = AxisCfg<N, W>::THREADS / W;
-  w = threadIdx.x % W;
-  n = threadIdx.x / W + i * DN;
-  e = n * W + w;
+__device__ __forceinline__ bool fft_owned(int i, int& n, int& w) {
+  using C = AxisCfg<N, W>;
+  w = threadIdx.x / C::T;
+  n = first_load_index<N, C::T>(threadIdx.x % C::T, i);
+  return w < W;
 }
 
 // In-place complex FFT along AXIS of fields (slot_map[f] or f), items
@@ -71,7 +74,7 @@ struct AxisOp {
   struct Early {};
   __device__ void early(Early&, int64_t) const {}
   __device__ bool pre(float2*, int64_t, const Early&) const { return false; }
-  __device__ void body(float2* b, int64_t, const float2* tw) const {
+  __device__ void body(float2* b, int64_t, const float2* tw, const Early&) const {
     tile_fft<N, W, SIGN>(b, tw);
     __syncthreads();
   }
@@ -105,7 +108,7 @@ struct XinvOp {
     tile_load_async<N, W, 0>(b, phi, HP, o, c0);
   }
   struct Early {
-    float f[AxisCfg<N, W>::PER];
+    float f[AxisCfg<N, W>::E];
   };
   __device__ void early(Early& r, int64_t item) const {
     using C = AxisCfg<N, W>;
@@ -114,29 +117,19 @@ struct XinvOp {
     const int ky = sidx(o, N);
     const float* q = qtab + (int64_t)p * nsq;
 #pragma unroll
-    for (int i = 0; i < C::PER; ++i) {
-      int e, n, w;
-      tile_owned<N, W>(i, e, n, w);
+    for (int i = 0; i < C::E; ++i) {
+      int n, w;
+      const bool own = fft_owned<N, W>(i, n, w);
       int kz = c0 + w, kx = sidx(n, N);
       int n2 = kx * kx + ky * ky + kz * kz;
       float f = 0.f;
-      if (kz <= N / 2 && n2 != 0 && keep_cell(a.g, kx, ky, kz)) f = __ldg(q + n2);
+      if (own && kz <= N / 2 && n2 != 0 && keep_cell(a.g, kx, ky, kz)) f = __ldg(q + n2);
       r.f[i] = f;
     }
   }
-  __device__ bool pre(float2* b, int64_t, const Early& r) const {
-    using C = AxisCfg<N, W>;
-#pragma unroll
-    for (int i = 0; i < C::PER; ++i) {
-      int e, n, w;
-      tile_owned<N, W>(i, e, n, w);
-      float2& v = b[w * C::LS + spad(n)];
-      v = make_float2(v.x * r.f[i], v.y * r.f[i]);
-    }
-    return true;
-  }
-  __device__ void body(float2* b, int64_t, const float2* tw) const {
-    tile_fft<N, W, +1>(b, tw);
+  __device__ bool pre(float2*, int64_t, const Early&) const { return false; }
+  __device__ void body(float2* b, int64_t, const float2* tw, const Early& r) const {
+    tile_fft<N, W, +1, 1>(b, tw, r.f);
     __syncthreads();
   }
   __device__ void store(const float2* b, int64_t item) const {
@@ -173,10 +166,10 @@ struct LptOp {
     const float2* src = MODE == 2 ? work + (int64_t)src_slot * fs : phi;
     tile_load_async<N, W, 0>(b, src, HP, o, c0);
   }
-  // the spectral factor of component comp per owned element: real for
-  // MODE 0, imaginary for MODE 1 and 2 (stored as its imaginary part)
+  // the spectral factor of component comp per value of the first FFT stage:
+  // real for MODE 0, imaginary for MODE 1 and 2 (stored as its imaginary part)
   struct Early {
-    float f[AxisCfg<N, W>::PER];
+    float f[AxisCfg<N, W>::E];
   };
   __device__ void early(Early& r, int64_t item) const {
     using C = AxisCfg<N, W>;
@@ -184,33 +177,22 @@ struct LptOp {
     coords(item, o, c0, comp);
     const int ky = sidx(o, N);
 #pragma unroll
-    for (int i = 0; i < C::PER; ++i) {
-      int e, n, w;
-      tile_owned<N, W>(i, e, n, w);
+    for (int i = 0; i < C::E; ++i) {
+      int n, w;
+      const bool own = fft_owned<N, W>(i, n, w);
       const int kz = c0 + w, kx = sidx(n, N);
       const int n2 = kx * kx + ky * ky + kz * kz;
       float f = 0.f;
-      if (kz <= N / 2) {
+      if (own && kz <= N / 2) {
         const float2 g = lpt_factor<MODE>(a, comp, n, o, kz, kx, ky, n2);
         f = MODE == 0 ? g.x : g.y;
       }
       r.f[i] = f;
     }
   }
-  __device__ bool pre(float2* b, int64_t, const Early& r) const {
-    using C = AxisCfg<N, W>;
-#pragma unroll
-    for (int i = 0; i < C::PER; ++i) {
-      int e, n, w;
-      tile_owned<N, W>(i, e, n, w);
-      float2& v = b[w * C::LS + spad(n)];
-      const float f = r.f[i];
-      v = MODE == 0 ? make_float2(v.x * f, v.y * f) : make_float2(-f * v.y, f * v.x);
-    }
-    return true;
-  }
-  __device__ void body(float2* b, int64_t item, const float2* tw) const {
-    tile_fft<N, W, +1>(b, tw);
+  __device__ bool pre(float2*, int64_t, const Early&) const { return false; }
+  __device__ void body(float2* b, int64_t, const float2* tw, const Early& r) const {
+    tile_fft<N, W, +1, MODE == 0 ? 1 : 2>(b, tw, r.f);
     __syncthreads();
   }
   __device__ void store(const float2* b, int64_t item) const {

@@ -271,6 +271,34 @@ def precision_report(sample) -> dict:
     return {k_: (round(v, 12) if isinstance(v, float) else v) for k_, v in out.items()}
 
 
+def precision_vs_plain(wl: str = "scalarI_m12_n512") -> dict:
+    """Relative RMS particle-displacement difference of the fused FP32 form
+    against the plain FP64 GPU form at full size (the 512^3 / 12-mode
+    workload; the FP64 oracle is too slow there)."""
+    import torch
+    from aarambam_gb300.ic import ICGenerator
+    cfg = make_cfg(wl, 1234)
+    N, box = cfg["Nmesh"], cfg["Box"]
+    alpha, x0, k, t = load_tables(cfg["table"], cfg["N_modes"])
+    dev = torch.device("cuda", torch.cuda.current_device())
+    lagr = lattice_positions(N, box, dev)
+    g = ICGenerator(cfg, alpha, x0, k, t)
+    pf, _ = g.run(lagr)
+    del g
+    torch.cuda.empty_cache()
+    gp = ICGenerator(cfg, alpha, x0, k, t, precision="fp64")
+    pp, _ = gp.run(lagr)
+    del gp
+    torch.cuda.empty_cache()
+
+    def dspl(p):
+        d = p.double() - lagr.double()
+        return d - box * torch.round(d / box)
+    want = dspl(pp)
+    err = float(torch.linalg.vector_norm(dspl(pf) - want) / torch.linalg.vector_norm(want))
+    return {"workload": wl, "n": N, "displacement": round(err, 12)}
+
+
 def replica_seed(rank: int) -> int:
     """Replicas run independent realisations: the seed of rank r is 1234 + r."""
     return 1234 + rank
@@ -415,6 +443,7 @@ def gpu_arm(args):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu, sample = cpu_baseline(args.workload, args.cpu_sample_n)
         precision = precision_report(sample)
+        precision["fused_vs_plain_fp64_at_512"] = precision_vs_plain()
 
     if rank == 0:
         out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

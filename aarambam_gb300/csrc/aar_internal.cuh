@@ -102,6 +102,8 @@ struct Plan {
   // staging buffers of aar_run_host (grown on demand, kept for reuse)
   float* d_io = nullptr;
   int64_t io_cap = 0;
+  cudaStream_t copy_stream = nullptr;  // side stream of the host-to-device copy
+  cudaEvent_t copy_start = nullptr, copy_done = nullptr;
 };
 
 // Records CUDA events around the kernels launched in its scope (when the

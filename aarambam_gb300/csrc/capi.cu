@@ -245,6 +245,11 @@ static void plan_release(Plan* p) {
   p->io_cap = 0;
   p->d_adj_scratch = nullptr;
   p->adj_scratch_bytes = 0;
+  if (p->copy_stream) cudaStreamDestroy(p->copy_stream);
+  if (p->copy_done) cudaEventDestroy(p->copy_done);
+  if (p->copy_start) cudaEventDestroy(p->copy_start);
+  p->copy_stream = nullptr;
+  p->copy_done = p->copy_start = nullptr;
   plain_free(p);
 }
 
@@ -580,6 +585,8 @@ int aar_run_glass(aar_plan* h, const float* d_glass, int64_t nglass, double glas
 int aar_run_host(aar_plan* h, const float* h_lagr, int64_t npart, float* h_pos, float* h_vel, void* stream) {
   if (!h || npart < 0 || (npart > 0 && (!h_lagr || !h_pos || !h_vel))) return AAR_ERR_ARG;
   Plan* p = &h->p;
+  int rc = ready(p);
+  if (rc) return rc;
   cudaStream_t st = S(stream);
   size_t bytes = sizeof(float) * 3 * (size_t)npart;
   if (npart > p->io_cap) {  // plan-owned staging: in, pos, vel
@@ -589,16 +596,35 @@ int aar_run_host(aar_plan* h, const float* h_lagr, int64_t npart, float* h_pos, 
       p->d_io = nullptr;
       p->io_cap = 0;
     }
-    int rc = plan_alloc(p, (void**)&p->d_io, 3 * bytes);
-    if (rc) return rc;
+    if ((rc = plan_alloc(p, (void**)&p->d_io, 3 * bytes))) return rc;
     p->io_cap = npart;
   }
   float* d_in = p->d_io;
   float* d_pos = d_in + 3 * (size_t)npart;
   float* d_vel = d_pos + 3 * (size_t)npart;
-  if (npart > 0) AAR_CUDA_TRY(p, cudaMemcpyAsync(d_in, h_lagr, bytes, cudaMemcpyHostToDevice, st));
-  int rc = aar_run(h, d_in, npart, d_pos, d_vel, stream);
-  if (rc) return rc;
+  if (p->prm.precision == AAR_PLAIN_FP64) {
+    if (npart > 0) AAR_CUDA_TRY(p, cudaMemcpyAsync(d_in, h_lagr, bytes, cudaMemcpyHostToDevice, st));
+    if ((rc = aar_run(h, d_in, npart, d_pos, d_vel, stream))) return rc;
+  } else {
+    // the Lagrangian positions are needed only by the read-out: their copy
+    // runs on a side stream while the fields are computed
+    if (!p->copy_stream) {
+      AAR_CUDA_TRY(p, cudaStreamCreateWithFlags(&p->copy_stream, cudaStreamNonBlocking));
+      AAR_CUDA_TRY(p, cudaEventCreateWithFlags(&p->copy_done, cudaEventDisableTiming));
+      AAR_CUDA_TRY(p, cudaEventCreateWithFlags(&p->copy_start, cudaEventDisableTiming));
+    }
+    AAR_CUDA_TRY(p, cudaEventRecord(p->copy_start, st));  // after earlier work on the caller's stream
+    AAR_CUDA_TRY(p, cudaStreamWaitEvent(p->copy_stream, p->copy_start, 0));
+    if (npart > 0)
+      AAR_CUDA_TRY(p, cudaMemcpyAsync(d_in, h_lagr, bytes, cudaMemcpyHostToDevice, p->copy_stream));
+    AAR_CUDA_TRY(p, cudaEventRecord(p->copy_done, p->copy_stream));
+    p->last_launches = 0;
+    if ((rc = run_noise(p, st))) return rc;
+    if ((rc = fused_modal(p, st))) return rc;
+    if ((rc = fused_lpt(p, st))) return rc;
+    AAR_CUDA_TRY(p, cudaStreamWaitEvent(st, p->copy_done, 0));
+    if ((rc = fused_readout(p, d_in, npart, d_pos, d_vel, st))) return rc;
+  }
   if (npart > 0) {
     AAR_CUDA_TRY(p, cudaMemcpyAsync(h_pos, d_pos, bytes, cudaMemcpyDeviceToHost, st));
     AAR_CUDA_TRY(p, cudaMemcpyAsync(h_vel, d_vel, bytes, cudaMemcpyDeviceToHost, st));

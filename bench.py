@@ -416,7 +416,18 @@ def gpu_arm(args):
             host_step()
         barrier()
         te = max_over_ranks(time.perf_counter() - t0, dev)
-        e2e = {"value": job_rate(world, ks, npart, te), "unit": UNIT, "h2d_bytes_per_step": 12 * npart,
+        # the copies alone, for the breakdown (pinned host memory)
+        c0, c1, c2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        c0.record(stream)
+        lagr.copy_(h_in, non_blocking=True)
+        c1.record(stream)
+        h_pos.copy_(pos, non_blocking=True)
+        h_vel.copy_(vel, non_blocking=True)
+        c2.record(stream)
+        torch.cuda.synchronize()
+        h2d_gbs = 12 * npart / (c0.elapsed_time(c1) / 1e3) / 1e9
+        d2h_gbs = 24 * npart / (c1.elapsed_time(c2) / 1e3) / 1e9
+        e2e = {"value": job_rate(world, ks, npart, te), "h2d_gbs": round(h2d_gbs, 1), "d2h_gbs": round(d2h_gbs, 1), "unit": UNIT, "h2d_bytes_per_step": 12 * npart,
                "d2h_bytes_per_step": 24 * npart, "steps": ks, "api": "aar_run_host (C ABI, pinned host buffers)"}
 
     plain = None

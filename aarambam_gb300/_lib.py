@@ -28,7 +28,7 @@ EXPORTS = [
     "aar_stage_readout", "aar_stage_readout_glass", "aar_copy_spectrum", "aar_copy_field", "aar_gaussian_spectrum_noalloc", "aar_c2r", "aar_r2c", "aar_last_launch_count", "aar_profile_enable", "aar_profile_report",
     "aar_last_error", "aar_plan_destroy", "aar_version",
     "aar_batch_create", "aar_batch_run", "aar_batch_launch_count", "aar_batch_last_error", "aar_batch_destroy",
-    "aar_set_spectrum", "aar_adj_spectral", "aar_adj_source", "aar_adj_products",
+    "aar_set_spectrum", "aar_adj_spectral", "aar_adj_source", "aar_adj_products", "aar_set_jit", "aar_jit_status",
 ]
 AAR_ADJ_OP_ONE, AAR_ADJ_OP_GAUSS, AAR_ADJ_OP_Q, AAR_ADJ_OP_RHO = 0, 1, 2, 3
 AAR_ADJ_OP_HESS, AAR_ADJ_OP_PSI1, AAR_ADJ_OP_PSI2 = 4, 5, 6
@@ -104,6 +104,9 @@ def load(build_if_missing: bool = False):
     L.aar_batch_last_error.restype = C.c_char_p
     L.aar_batch_destroy.argtypes = [vp]
     L.aar_batch_destroy.restype = None
+    L.aar_set_jit.argtypes = [vp, i32]
+    L.aar_jit_status.argtypes = [vp]
+    L.aar_jit_status.restype = C.c_char_p
     L.aar_set_spectrum.argtypes = [vp, vp, vp]
     L.aar_adj_spectral.argtypes = [vp, i32, i32, i32, vp, vp, i32, vp]
     L.aar_adj_source.argtypes = [vp, vp, vp, vp, vp]

@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libaarambam_gpu.so")
-SOURCES = ["noise.cu", "fused.cu", "capi.cu", "plain64.cu", "adjoint.cu"]
+SOURCES = ["noise.cu", "fused.cu", "capi.cu", "plain64.cu", "adjoint.cu", "jit.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -40,10 +40,29 @@ def _stale(obj: str, src: str) -> bool:
     return any(os.path.getmtime(d) > t for d in deps)
 
 
+def _embed_headers() -> None:
+    """_build/jit_embed.h: the device headers the run-time specialised row
+    kernel is compiled from (jit.cu), as raw string literals."""
+    out = os.path.join(OUT, "jit_embed.h")
+    parts = ["// generated by build.py from csrc/fft.cuh and csrc/rows.cuh\n#pragma once\n"]
+    for var, name in (("kEmbedFft", "fft.cuh"), ("kEmbedRows", "rows.cuh")):
+        with open(os.path.join(CSRC, name)) as f:
+            text = f.read()
+        if ")AARJIT\"" in text:
+            raise RuntimeError(name + " contains the raw-string delimiter")
+        parts.append("static const char* " + var + " = R\"AARJIT(" + text + ")AARJIT\";\n")
+    new = "".join(parts)
+    old = open(out).read() if os.path.exists(out) else None
+    if new != old:
+        with open(out, "w") as f:
+            f.write(new)
+
+
 def build(verbose: bool = False) -> str:
     os.makedirs(OUT, exist_ok=True)
+    _embed_headers()
     flags = ["-std=c++20", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
-             "-I" + os.path.join(os.path.dirname(HERE), "include")] + ARCH
+             "-I" + os.path.join(os.path.dirname(HERE), "include"), "-I" + OUT] + ARCH
     procs = []
     objs = []
     for src in SOURCES:
@@ -64,7 +83,7 @@ def build(verbose: bool = False) -> str:
         libdir = os.path.join(cuda_home(), "lib")
     if procs or not os.path.exists(LIB):
         tmp = LIB + ".tmp"
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-L" + libdir, "-lcufft",
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-L" + libdir, "-lcufft", "-lnvrtc",
                                                                   "-Xlinker", "-rpath=" + libdir]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:

@@ -11,6 +11,7 @@
 
 namespace aar {
 
+constexpr int kRowThreadsHost = 256;  // block size of the row kernels (rows.cuh kRowThreads)
 constexpr double kPi = 3.14159265358979323846;  // PI as the reference defines it
 
 // signed wavenumber index of grid index i (main.c:410-423): N/2 -> -N/2
@@ -82,6 +83,10 @@ struct Plan {
   // modal term list (device)
   void* d_terms = nullptr;
   std::vector<char> host_terms;  // the same term list on the host (kernel parameter of the row combine)
+  int row_ls = 0;                // row-kernel line stride (float2) of this grid size
+  void* jit = nullptr;           // run-time specialised modal row kernel (jit.cu), or null
+  int jit_mode = 1;              // 0 off, 1 for N >= 256, 2 always
+  std::string jit_status = "off";
   int nterms = 0, nr_active = 0;
   // plain FP64 form
   void* plain = nullptr;
@@ -137,6 +142,9 @@ int fused_c2r(Plan* p, const float2* in, float* out, cudaStream_t st);
 int fused_r2c(Plan* p, const float* in, float2* out, cudaStream_t st);
 int fused_configure_xform(Plan* p);
 int noalloc_gaussian(Plan* p, void* d_out, cudaStream_t st);
+int jit_prepare(Plan* p);
+int jit_modal_rows(Plan* p, float2* work, int64_t fs, cudaStream_t st);
+void jit_free(Plan* p);
 int adj_spectral(Plan* p, int op, int comp, int mode, const float2* in, float2* out, int accumulate,
                  cudaStream_t st);
 int adj_source(Plan* p, const float* d, const float* gS, float* gd, cudaStream_t st);

@@ -245,6 +245,7 @@ static void plan_release(Plan* p) {
   p->io_cap = 0;
   p->d_adj_scratch = nullptr;
   p->adj_scratch_bytes = 0;
+  jit_free(p);
   if (p->copy_stream) cudaStreamDestroy(p->copy_stream);
   if (p->copy_done) cudaEventDestroy(p->copy_done);
   if (p->copy_start) cudaEventDestroy(p->copy_start);
@@ -728,6 +729,18 @@ int aar_copy_field(aar_plan* h, int32_t which, float* d_out, void* stream) {
                                     (size_t)N * N, cudaMemcpyDeviceToDevice, S(stream)));
   return AAR_OK;
 }
+
+// ------------------------------------------------------------- JIT rows
+int aar_set_jit(aar_plan* h, int32_t mode) {
+  if (!h || mode < 0 || mode > 2) return AAR_ERR_ARG;
+  Plan* p = &h->p;
+  p->jit_mode = mode;
+  ++p->generation;
+  if (!p->have_tables || p->prm.precision != AAR_FUSED_FP32) return AAR_OK;
+  return jit_prepare(p);
+}
+
+const char* aar_jit_status(const aar_plan* h) { return h ? h->p.jit_status.c_str() : "null plan"; }
 
 // ------------------------------------------------------------- adjoint
 int aar_set_spectrum(aar_plan* h, const void* d_in, void* stream) {

@@ -8,10 +8,13 @@
 // span Ns: inputs x[j + r N/R], twiddle exp(s 2 pi i r (j mod Ns)/(Ns R)),
 // outputs y[(j/Ns) Ns R + (j mod Ns) + r Ns]).
 #pragma once
+#ifndef __CUDACC_RTC__
 #include <cuda_runtime.h>
 #include <stdint.h>
-
-#include <utility>
+#else
+typedef long long int64_t;
+typedef unsigned int uint32_t;
+#endif
 
 namespace aar {
 
@@ -209,12 +212,16 @@ struct StoreAddr {
   }
 };
 
-template <int B, int NB, int R, class F>
+// f.template operator()<B, RR>() for every group B < NB and RR < R
+template <int B, int NB, int R, int RR = 0, class F>
 __device__ __forceinline__ void unroll_br(F&& f) {
   if constexpr (B < NB) {
-    [&]<int... RR>(std::integer_sequence<int, RR...>) { (f.template operator()<B, RR>(), ...); }(
-        std::make_integer_sequence<int, R>{});
-    unroll_br<B + 1, NB, R>(f);
+    if constexpr (RR < R) {
+      f.template operator()<B, RR>();
+      unroll_br<B, NB, R, RR + 1>(f);
+    } else {
+      unroll_br<B + 1, NB, R, 0>(f);
+    }
   }
 }
 

@@ -31,6 +31,7 @@
 
 #include "aar_internal.cuh"
 #include "fft.cuh"
+#include "rows.cuh"
 #include "spectral.cuh"
 
 namespace aar {
@@ -64,18 +65,6 @@ struct AxisCfg {
   static constexpr int PER = N * W / THREADS;  // tile elements per thread
   static constexpr int MINB = THREADS >= 512 ? 2 : 4;  // resident blocks per SM aimed at
 };
-
-// asynchronous global -> shared copies (sm_80+ cp.async), 8 bytes each
-__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
-  unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int K>
-__device__ __forceinline__ void cp_async_wait() {
-  asm volatile("cp.async.wait_group %0;\n" ::"n"(K) : "memory");
-}
-
 
 // Tile indexing.  Axis 0 (x): rows n = x, other index o = y.  Axis 1 (y):
 // rows n = y, o = x.  Column w covers kz = c0 + w.
@@ -187,152 +176,11 @@ __global__ void __launch_bounds__(256) k_modal_acc(ModalArgs a, float2* phi, con
 }
 
 // ----------------------------------------------------------- row passes
-// Row layout: complex row X[0..N/2] at field + (x N + y) HP; the real row
-// x[0..N-1] occupies the same bytes (float2 z_n = (x_{2n}, x_{2n+1})).
-template <int N>
-struct RowCfg {
-  static constexpr int H = N / 2;             // complex FFT length
-  static constexpr int T = lanes_for(H);
-  static constexpr int LPW = 32 / T;
-  static constexpr int LS = spad_len(H);
-};
-
-// load X_k (k = 0..N/2) of a row and form Z_k = E_k + i O_k for the
-// inverse half-length FFT (FFTW c2r semantics: Im X_0, Im X_{N/2} dropped)
-template <int N>
-__device__ __forceinline__ void row_c2r_pre(const float2* __restrict__ X, float2* line, int t, int T,
-                                            const float2* __restrict__ twN) {
-  constexpr int H = N / 2;
-  for (int k = t; k <= H / 2; k += T) {
-    int k2 = H - k;
-    float2 a = X[k], b = X[k2];
-    if (k == 0) {
-      a.y = 0.f;
-      b.y = 0.f;
-    }
-    // E_k = X_k + conj(X_{H-k}); O_k = (X_k - conj(X_{H-k})) e^{+2 pi i k / N}
-    float2 w = __ldg(twN + k);
-    w.y = -w.y;
-    float2 e = make_float2(a.x + b.x, a.y - b.y);
-    float2 d = make_float2(a.x - b.x, a.y + b.y);
-    float2 o = cmul(d, w);
-    line[spad(k)] = make_float2(e.x - o.y, e.y + o.x);
-    if (k2 != k && k2 < H) {
-      // Z_{H-k}: E = X_{H-k} + conj(X_k), O = (X_{H-k} - conj(X_k)) e^{+2 pi i (H-k)/N}
-      float2 w2 = __ldg(twN + k2);
-      w2.y = -w2.y;
-      float2 e2 = make_float2(b.x + a.x, b.y - a.y);
-      float2 d2 = make_float2(b.x - a.x, b.y + a.y);
-      float2 o2 = cmul(d2, w2);
-      line[spad(k2)] = make_float2(e2.x - o2.y, e2.y + o2.x);
-    }
-  }
-}
-
-// The same pre-step in place, on X_0..X_{N/2} already staged in `line`
-// (element k at spad(k)): each lane rewrites the pair (k, H - k) it reads.
-template <int N>
-__device__ __forceinline__ void row_c2r_pre_inplace(float2* line, int t, int T, const float2* __restrict__ twN) {
-  constexpr int H = N / 2;
-  for (int k = t; k <= H / 2; k += T) {
-    int k2 = H - k;
-    float2 a = line[spad(k)], b = line[spad(k2)];
-    if (k == 0) {
-      a.y = 0.f;
-      b.y = 0.f;
-    }
-    float2 w = __ldg(twN + k);
-    w.y = -w.y;
-    float2 e = make_float2(a.x + b.x, a.y - b.y);
-    float2 d = make_float2(a.x - b.x, a.y + b.y);
-    float2 o = cmul(d, w);
-    line[spad(k)] = make_float2(e.x - o.y, e.y + o.x);
-    if (k2 != k && k2 < H) {
-      float2 w2 = __ldg(twN + k2);
-      w2.y = -w2.y;
-      float2 e2 = make_float2(b.x + a.x, b.y - a.y);
-      float2 d2 = make_float2(b.x - a.x, b.y + a.y);
-      float2 o2 = cmul(d2, w2);
-      line[spad(k2)] = make_float2(e2.x - o2.y, e2.y + o2.x);
-    }
-  }
-}
-
-// after the forward half-length FFT of z_n = (x_{2n}, x_{2n+1}) in `line`,
-// write X_k = (Z_k + conj Z_{H-k})/2 - i e^{-2 pi i k/N} (Z_k - conj Z_{H-k})/2
-template <int N>
-__device__ __forceinline__ void row_r2c_post(const float2* line, float2* __restrict__ X, int t, int T,
-                                             const float2* __restrict__ twN) {
-  constexpr int H = N / 2;
-  for (int k = t; k <= H; k += T) {
-    float2 z = line[spad(k % H)], zc = line[spad((H - k) % H)];
-    zc.y = -zc.y;
-    float2 e = make_float2(0.5f * (z.x + zc.x), 0.5f * (z.y + zc.y));
-    float2 d = make_float2(0.5f * (z.x - zc.x), 0.5f * (z.y - zc.y));
-    float2 w = (k < H) ? __ldg(twN + k) : make_float2(-1.f, 0.f);
-    float2 od = cmul(d, w);  // e^{-2 pi i k/N} d
-    X[k] = make_float2(e.x + od.y, e.y - od.x);  // e - i od
-  }
-}
-
-// Generic row kernel.  For each row (blockIdx.x = x*N + y): c2r of `nin`
-// input fields (slots in_slot[]), a per-position combine step Op, r2c of
-// `nout` output lines into slots out_slot[].  One warp per line at a time.
-// THREADS = 256 with two resident blocks per SM: while one block waits at a
-// phase barrier (its last round of lines keeps only some warps busy) the
-// other block's warps issue.
-constexpr int kRowThreads = 256;
+// (rows.cuh: RowCfg, the c2r / r2c row steps and rows_body)
 template <int N, class Op>
 __global__ void __launch_bounds__(kRowThreads, Op::min_blocks(N)) k_rows(Op op, float2* work, int64_t fs, int HP,
                                                        const float2* __restrict__ twN, const float2* __restrict__ twH) {
-  using C = RowCfg<N>;
-  constexpr int H = C::H;
-  extern __shared__ float2 sm[];
-  int64_t row = blockIdx.x;
-  int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  constexpr int nwarps = kRowThreads / 32;
-  int sub = lane / C::T, t = lane % C::T;
-  // phase 0: stage X_0..X_{N/2} of every input line at once (one exposed
-  // memory latency per row instead of one per line; staging round by round
-  // with a barrier per round measured slower: 148 vs 141 ms at 1024^3)
-  for (int l = 0; l < op.nin(); ++l) {
-    const float2* X = work + (int64_t)op.in_slot(l) * fs + row * HP;
-    float2* line = sm + l * C::LS;
-    for (int k = threadIdx.x; k <= H; k += kRowThreads) cp_async8(line + spad(k), X + k);
-  }
-  cp_async_commit();
-  cp_async_wait<0>();
-  __syncthreads();
-  // phase 1: inverse transforms
-  for (int l0 = warp * C::LPW; l0 < op.nin(); l0 += nwarps * C::LPW) {
-    int l = l0 + sub;
-    bool act = l < op.nin() && sub < C::LPW;
-    float2* line = sm + (act ? l : 0) * C::LS;
-    if (act) row_c2r_pre_inplace<N>(line, t, C::T, twN);
-    __syncwarp();
-    line_fft_smem<H, C::T, +1>(line, t, twH, act);
-  }
-  __syncthreads();
-  // phase 2: per position combine (in place in the line buffers)
-  for (int n = threadIdx.x; n < H; n += 2 * kRowThreads) {
-    if (n + kRowThreads < H) {
-      const int pos[2] = {spad(n), spad(n + kRowThreads)};
-      op.template combine<2>(sm, pos, C::LS);
-    } else {
-      const int pos[1] = {spad(n)};
-      op.template combine<1>(sm, pos, C::LS);
-    }
-  }
-  __syncthreads();
-  // phase 3: forward transforms of the output lines
-  for (int l0 = warp * C::LPW; l0 < op.nout(); l0 += nwarps * C::LPW) {
-    int l = l0 + sub;
-    bool act = l < op.nout() && sub < C::LPW;
-    float2* line = sm + (act ? op.out_line(l) : 0) * C::LS;
-    line_fft_smem<H, C::T, -1>(line, t, twH, act);
-    if (act) row_r2c_post<N>(line, work + (int64_t)op.out_slot(l) * fs + row * HP, t, C::T, twN);
-    __syncwarp();
-  }
+  rows_body<N>(op, work, fs, HP, twN, twH);
 }
 
 // One product term of the row combine, as a kernel parameter: the shared-
@@ -351,6 +199,7 @@ struct ModalRowOp {
   // resident rows per SM: shared memory holds two at 1024^3 with 20 modes;
   // below that registers decide (three rows: 80 registers, no spill)
   static constexpr int min_blocks(int n) { return n >= 1024 ? 2 : 3; }
+  static constexpr bool kPairs = true;
   int M, nr;
   int r_of_slot[kMaxModes];
   int begin[kMaxModes + 1];
@@ -409,6 +258,7 @@ struct ModalRowOp {
 // the source goes to line 0, written to slot `out`.
 struct SourceRowOp {
   static constexpr int min_blocks(int) { return 4; }  // seven lines per row
+  static constexpr bool kPairs = true;
   int out;
   __device__ int nin() const { return 6; }
   __device__ int in_slot(int l) const { return l; }
@@ -619,6 +469,11 @@ struct Launch {
     if (rc) return rc;
     if ((rc = ypass<+1>(p, p->d_work, a.M, nullptr, st, "modal_ypass_inv"))) return rc;
     size_t sm_rows = sizeof(float2) * (size_t)(a.M + 1) * RowCfg<N>::LS;
+    if (p->jit) {
+      if ((rc = jit_modal_rows(p, p->d_work, fs, st))) return rc;
+      if ((rc = ypass<-1>(p, p->d_work, p->nr_active, slot_map(p), st, "modal_ypass_fwd"))) return rc;
+      return modal_tail(p, a, fs, st);
+    }
     static_assert(sizeof(ModalRowOp) < 32000, "kernel parameter space");
     ModalRowOp op;
     {
@@ -645,6 +500,11 @@ struct Launch {
     AAR_CUDA_TRY(p, cudaGetLastError());
     p->last_launches += 1;
     if ((rc = ypass<-1>(p, p->d_work, p->nr_active, slot_map(p), st, "modal_ypass_fwd"))) return rc;
+    return modal_tail(p, a, fs, st);
+  }
+  // forward x of the active slots, then the accumulation into phi
+  static int modal_tail(Plan* p, const ModalArgs& a, int64_t fs, cudaStream_t st) {
+    int rc;
     {
       AxisOp<N, W, 0, -1> xf{p->d_work, fs, tiles(p), p->HP, slot_map(p)};
       if ((rc = run_pass<N>(p, xf, p->nr_active * tiles(p), st, "modal_xfwd"))) return rc;
@@ -769,8 +629,15 @@ int fused_prepare(Plan* p) {
   if (p->M > kMaxModes) return set_err(p, "N_modes above 32 is not supported"), AAR_ERR_ARG;
   int rc = build_terms(p);
   if (rc) return rc;
-  return dispatch_n(p->N, [&](auto nc) { return Launch<decltype(nc)::value>::configure(p); });
+  if ((rc = dispatch_n(p->N, [&](auto nc) {
+         p->row_ls = RowCfg<decltype(nc)::value>::LS;
+         return Launch<decltype(nc)::value>::configure(p);
+       })))
+    return rc;
+  return jit_prepare(p);
 }
+
+static_assert(kRowThreads == kRowThreadsHost, "row kernel block size");
 
 int fused_modal(Plan* p, cudaStream_t st) {
   ModalArgs a = modal_args(p);

@@ -1,0 +1,184 @@
+// Run-time specialised modal row kernel.
+//
+// The generic row kernel (fused.cu, ModalRowOp) reads its term list at run
+// time, so every term costs four shared-memory loads (f_p and f_q at two
+// positions).  Here the kernel is generated for the plan's term structure
+// and compiled with NVRTC for sm_103a: a thread loads the M values f_p of
+// its positions into registers once and every term is two multiply-adds with
+// compile-time register indices; the coefficients sit in the module's
+// __constant__ memory, so a new alpha table with the same nonzero pattern
+// (same terms) only rewrites them.  The FFT and row code are the same
+// headers the library is built from (fft.cuh, rows.cuh, embedded at build
+// time).  If NVRTC or the module load fails, the plan keeps the generic
+// kernel and records why.
+#include <cuda_runtime.h>
+#include <nvrtc.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "aar_internal.cuh"
+#include "jit_embed.h"  // kEmbedFft, kEmbedRows (generated by build.py)
+#include "spectral.cuh"
+
+namespace aar {
+
+struct JitState {
+  cudaLibrary_t lib = nullptr;
+  cudaKernel_t kern = nullptr;
+  float* coef = nullptr;  // the module's __constant__ coefficients
+  std::string key;        // N, M and the term structure the module was made for
+  size_t smem = 0;
+  int nterms = 0;
+};
+
+static std::string gen_source(int N, int M, int minb, int pairs, const TermList& tl, const std::vector<Term>& terms) {
+  std::string s;
+  // kCoef at global scope: its symbol name is not mangled (cudaLibraryGetGlobal)
+  s += "#include \"rows.cuh\"\n";
+  s += "__constant__ float kCoef[" + std::to_string(terms.empty() ? 1 : terms.size()) + "];\n";
+  s += "namespace aar {\n";
+  s += "struct JitRowOp {\n";
+  s += "  static constexpr int min_blocks(int) { return " + std::to_string(minb) + "; }\n";
+  s += "  static constexpr bool kPairs = " + std::string(pairs ? "true" : "false") + ";\n";
+  s += "  __device__ int nin() const { return " + std::to_string(M) + "; }\n";
+  s += "  __device__ int in_slot(int l) const { return l; }\n";
+  s += "  __device__ int nout() const { return " + std::to_string(tl.nr) + "; }\n";
+  s += "  __device__ int out_line(int l) const {\n    switch (l) {\n";
+  for (int i = 0; i < tl.nr; ++i) s += "      case " + std::to_string(i) + ": return " + std::to_string(tl.r_of_slot[i]) + ";\n";
+  s += "    }\n    return 0;\n  }\n";
+  s += "  __device__ int out_slot(int l) const { return out_line(l); }\n";
+  s += "  template <int K>\n  __device__ __forceinline__ void combine(float2* sm, const int* pos, int LS) const {\n";
+  s += "    float2 f[" + std::to_string(M) + "][K];\n";
+  s += "#pragma unroll\n    for (int p = 0; p < " + std::to_string(M) + "; ++p)\n";
+  s += "#pragma unroll\n      for (int i = 0; i < K; ++i) f[p][i] = sm[p * LS + pos[i]];\n";
+  // one block per output slot; terms accumulate in list order (the
+  // counter-term f0 f2 -> g1 into its own target r)
+  for (int sl = 0; sl < tl.nr; ++sl) {
+    const int r = tl.r_of_slot[sl];
+    s += "    {\n      float2 a[K];\n#pragma unroll\n      for (int i = 0; i < K; ++i) a[i] = make_float2(0.f, 0.f);\n";
+    for (size_t t = 0; t < terms.size(); ++t) {
+      if (terms[t].r != r) continue;
+      const std::string c = "kCoef[" + std::to_string(t) + "]", fp = "f[" + std::to_string(terms[t].p) + "][i]",
+                        fq = "f[" + std::to_string(terms[t].q) + "][i]";
+      s += "#pragma unroll\n      for (int i = 0; i < K; ++i) { a[i].x += " + c + " * " + fp + ".x * " + fq + ".x; a[i].y += " +
+           c + " * " + fp + ".y * " + fq + ".y; }\n";
+    }
+    s += "#pragma unroll\n      for (int i = 0; i < K; ++i) sm[" + std::to_string(r) + " * LS + pos[i]] = a[i];\n    }\n";
+  }
+  s += "  }\n};\n}  // namespace aar\n";
+  s += "extern \"C\" __global__ void __launch_bounds__(aar::kRowThreads, " + std::to_string(minb) +
+       ") aar_modal_rows_jit(float2* work, long long fs, int HP, const float2* __restrict__ twN, "
+       "const float2* __restrict__ twH) {\n";
+  s += "  aar::rows_body<" + std::to_string(N) + ">(aar::JitRowOp{}, work, fs, HP, twN, twH);\n}\n";
+  return s;
+}
+
+static void jit_release(JitState* j) {
+  if (!j) return;
+  if (j->lib) cudaLibraryUnload(j->lib);
+  delete j;
+}
+
+void jit_free(Plan* p) {
+  jit_release((JitState*)p->jit);
+  p->jit = nullptr;
+}
+
+// Build (or reuse) the specialised kernel for the plan's current term list.
+// Returns AAR_OK with p->jit set, or AAR_OK with p->jit == nullptr and the
+// reason in p->jit_status when the generic kernel stays in use.
+int jit_prepare(Plan* p) {
+  const bool want = p->jit_mode == 2 || (p->jit_mode == 1 && p->N >= 256);
+  if (!want || p->prm.precision != AAR_FUSED_FP32 || p->nr_active == 0) {
+    jit_free(p);
+    p->jit_status = want ? "no modal terms" : "off";
+    return AAR_OK;
+  }
+  const TermList& tl = *(const TermList*)p->host_terms.data();
+  const Term* ft = (const Term*)(p->host_terms.data() + sizeof(TermList));
+  std::vector<Term> terms(ft, ft + tl.nterms);
+  const int N = p->N, M = p->M;
+  const int minb = N >= 1024 ? 2 : 3;
+  const int regcap = 65536 / (kRowThreadsHost * minb);
+  const int pairs = 2 * 2 * M + 16 <= regcap * 3 / 4;  // f values of two positions fit the register budget
+  std::string key = std::to_string(N) + ":" + std::to_string(M) + ":" + std::to_string(minb) + ":" +
+                    std::to_string(pairs) + ":";
+  for (const Term& t : terms) key += std::to_string(t.p) + "," + std::to_string(t.q) + "," + std::to_string(t.r) + ";";
+  std::vector<float> coef(terms.size());
+  for (size_t i = 0; i < terms.size(); ++i) coef[i] = terms[i].c;
+  JitState* j = (JitState*)p->jit;
+  if (!j || j->key != key) {
+    jit_free(p);
+    const std::string src = gen_source(N, M, minb, pairs, tl, terms);
+    nvrtcProgram prog;
+    const char* hdrs[2] = {kEmbedFft, kEmbedRows};
+    const char* names[2] = {"fft.cuh", "rows.cuh"};
+    if (nvrtcCreateProgram(&prog, src.c_str(), "aar_modal_rows_jit.cu", 2, hdrs, names) != NVRTC_SUCCESS) {
+      p->jit_status = "nvrtcCreateProgram failed";
+      return AAR_OK;
+    }
+    const char* opts[] = {"--gpu-architecture=sm_103a", "-std=c++20", "-lineinfo", "-default-device"};
+    nvrtcResult cr = nvrtcCompileProgram(prog, 4, opts);
+    if (cr != NVRTC_SUCCESS) {
+      size_t n = 0;
+      nvrtcGetProgramLogSize(prog, &n);
+      std::string log(n, '\0');
+      if (n) nvrtcGetProgramLog(prog, &log[0]);
+      nvrtcDestroyProgram(&prog);
+      p->jit_status = "NVRTC: " + log.substr(0, 2000);
+      return AAR_OK;
+    }
+    size_t nbin = 0;
+    nvrtcGetCUBINSize(prog, &nbin);
+    std::vector<char> bin(nbin);
+    nvrtcGetCUBIN(prog, bin.data());
+    nvrtcDestroyProgram(&prog);
+    j = new JitState();
+    if (cudaLibraryLoadData(&j->lib, bin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0) != cudaSuccess ||
+        cudaLibraryGetKernel(&j->kern, j->lib, "aar_modal_rows_jit") != cudaSuccess) {
+      cudaGetLastError();
+      jit_release(j);
+      p->jit_status = "module load failed";
+      return AAR_OK;
+    }
+    size_t csize = 0;
+    if (cudaLibraryGetGlobal((void**)&j->coef, &csize, j->lib, "kCoef") != cudaSuccess) {
+      cudaGetLastError();
+      jit_release(j);
+      p->jit_status = "coefficient symbol missing";
+      return AAR_OK;
+    }
+    j->key = key;
+    j->nterms = (int)terms.size();
+    p->jit = j;
+  }
+  j->smem = sizeof(float2) * (size_t)(M + 1) * p->row_ls;
+  if (cudaFuncSetAttribute((const void*)j->kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)j->smem) !=
+      cudaSuccess) {
+    cudaGetLastError();
+    jit_free(p);
+    p->jit_status = "shared-memory attribute refused";
+    return AAR_OK;
+  }
+  if (!coef.empty()) AAR_CUDA_TRY(p, cudaMemcpy(j->coef, coef.data(), sizeof(float) * coef.size(), cudaMemcpyHostToDevice));
+  p->jit_status = "on";
+  return AAR_OK;
+}
+
+int jit_modal_rows(Plan* p, float2* work, int64_t fs, cudaStream_t st) {
+  JitState* j = (JitState*)p->jit;
+  long long fsl = fs;
+  int hp = p->HP;
+  void* args[] = {&work, &fsl, &hp, &p->d_twN, &p->d_twH};
+  {
+    ProfScope ps_(p, "modal_rows", st);
+    AAR_CUDA_TRY(p, cudaLaunchKernel((const void*)j->kern, dim3((unsigned)((int64_t)p->N * p->N)),
+                                     dim3(kRowThreadsHost), args, j->smem, st));
+  }
+  p->last_launches += 1;
+  return AAR_OK;
+}
+
+}  // namespace aar

@@ -102,6 +102,17 @@ class ICGenerator:
         self._alpha, self._x0 = alpha, x0
         check(self.L, self.h, self.L.aar_set_tables(self.h, _dptr(self._alpha), _dptr(self._x0), alpha.shape[0]))
 
+    def set_jit(self, mode: int) -> str:
+        """Run-time specialised modal row kernel: 0 off, 1 for N >= 256 (the
+        default), 2 always.  Returns the status ("on", "off" or the reason
+        the generic kernel is used)."""
+        check(self.L, self.h, self.L.aar_set_jit(self.h, int(mode)))
+        return self.jit_status
+
+    @property
+    def jit_status(self) -> str:
+        return self.L.aar_jit_status(self.h).decode()
+
     def set_seed(self, seed: int) -> None:
         check(self.L, self.h, self.L.aar_set_seed(self.h, int(seed)))
         self.cfg["Seed"] = int(seed)

@@ -203,6 +203,15 @@ int aar_batch_launch_count(const aar_batch* batch);
 const char* aar_batch_last_error(const aar_batch* batch);
 void aar_batch_destroy(aar_batch* batch);
 
+/* Run-time specialised modal row kernel (no counterpart in the reference):
+   mode 0 off, 1 (default) for Nmesh >= 256, 2 always.  The kernel is
+   compiled with NVRTC for the plan's alpha-term structure when the tables
+   are set (a new table with the same nonzero pattern only updates its
+   coefficients); when compiling or loading fails the generic kernel stays
+   in use and aar_jit_status says why ("on", "off" or the reason). */
+int aar_set_jit(aar_plan* plan, int32_t mode);
+const char* aar_jit_status(const aar_plan* plan);
+
 /* Per-kernel timing: when enabled, CUDA events are recorded on the launching
    stream around every kernel; aar_profile_report synchronises the device and
    writes "kernel,launches,total_ms" lines for everything recorded since the

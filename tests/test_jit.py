@@ -1,0 +1,61 @@
+"""The run-time specialised (NVRTC) modal row kernel against the generic
+kernel and the FP64 oracle."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import oracle as O
+from tests.common import bbks, make_cfg, rel_rms, table
+
+pytestmark = pytest.mark.gpu
+
+
+def ng_spectrum(g):
+    g.stage("noise")
+    g.stage("modal")
+    return g.spectrum()
+
+
+@pytest.mark.parametrize("N,tab,M", [(256, "scalarI_m12_L1000_n512", 12), (128, "scalarI_m16_L500_n256_mu1p5", 16)])
+def test_jit_matches_generic_kernel(cuda, N, tab, M):
+    from aarambam_gb300.ic import ICGenerator
+    cfg = make_cfg(N, 1000.0, 77, 100.0, M, tab, 512)
+    g = ICGenerator(cfg, *table(tab, M), *bbks())
+    assert g.set_jit(2) == "on"
+    a = ng_spectrum(g)
+    assert g.set_jit(0) == "off"
+    b = ng_spectrum(g)
+    assert rel_rms(a.cpu().numpy(), b.cpu().numpy()) < 1e-6
+    # same nonzero pattern, new coefficients: the module is kept, values change
+    alpha, x0 = table(tab, M)
+    assert g.set_jit(2) == "on"
+    g.set_tables(alpha * 1.5, x0)
+    assert g.jit_status == "on"
+    c = ng_spectrum(g)
+    g.set_jit(0)
+    d = ng_spectrum(g)
+    assert rel_rms(c.cpu().numpy(), d.cpu().numpy()) < 1e-6
+    assert rel_rms(c.cpu().numpy(), a.cpu().numpy()) > 1e-4
+
+
+def test_jit_vs_oracle_small(cuda):
+    from aarambam_gb300.ic import ICGenerator
+    tab, M = "scalarI_m10_L500_n256", 10
+    cfg = make_cfg(32, 500.0, 4321, 100.0, M, tab, 256, Nsample=24, PhaseFlip=1)
+    alpha, x0 = table(tab, M)
+    k, t = bbks()
+    g = ICGenerator(cfg, alpha, x0, k, t)
+    assert g.set_jit(2) == "on"
+    g.stage("noise")
+    gauss = g.spectrum().cpu().numpy().astype(np.complex128)
+    g.stage("modal")
+    got = g.spectrum().cpu().numpy().astype(np.complex128)
+    o = O.Oracle(cfg, k, t)
+    gs = o.gauss()
+    acc = o.modal_acc(alpha, x0, gs)
+    tot = o.combine(gs, acc)
+    want = tot[..., 0] + 1j * tot[..., 1]
+    wg = gs[..., 0] + 1j * gs[..., 1]
+    N = cfg["Nmesh"]
+    assert rel_rms((got - gauss) * N**3, (want - wg) * N**3) < 2e-4  # the non-Gaussian part alone
+    assert rel_rms(got, want) < 1e-6

@@ -256,10 +256,12 @@ static void plan_release(Plan* p) {
 
 static bool pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
 
+// Work fields: the path needs max(M, 8) (2LPT: six Hessians, the source and
+// T/(D Beta) phi); the standalone transforms (M = 0) need one.
 static int alloc_fused(Plan* p, int M) {
   int N = p->N;
   size_t fbytes = sizeof(float2) * (size_t)N * N * p->HP;
-  int nwork = std::max(M, 7);
+  int nwork = M == 0 ? 1 : std::max(M, 8);
   if (p->d_work && p->nwork >= nwork) return AAR_OK;
   if (p->d_work) {
     cudaFree(p->d_work);
@@ -654,7 +656,7 @@ int aar_gaussian_spectrum_noalloc(aar_plan* h, void* d_out, void* stream) {
 static int need_work(Plan* p) {
   if (p->prm.precision != AAR_FUSED_FP32) return set_err(p, "transforms are for the fused form"), AAR_ERR_ARG;
   if (!p->d_work) {
-    int rc = alloc_fused(p, 1);
+    int rc = alloc_fused(p, 0);
     if (rc) return rc;
     if ((rc = fused_configure_xform(p))) return rc;
   }

@@ -175,6 +175,24 @@ __global__ void __launch_bounds__(256) k_modal_acc(ModalArgs a, float2* phi, con
   }
 }
 
+// phi_T = T(k)/(D Beta) phi on every half-spectrum cell (padding columns
+// are not touched): the factor the Hessians and psi1 share.
+template <int N>
+__global__ void __launch_bounds__(256) k_scale_twb(const float2* __restrict__ phi, float2* out, int HP,
+                                                   const float* __restrict__ twb) {
+  constexpr int K = N / 2 + 1;
+  constexpr int64_t total = (int64_t)N * N * K;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t row = i / K;
+    const int kz = (int)(i - row * K);
+    const int64_t e = row * HP + kz;
+    const int kx = sidx((int)(row / N), N), ky = sidx((int)(row % N), N);
+    const float t = __ldg(twb + kx * kx + ky * ky + kz * kz);
+    const float2 v = phi[e];
+    out[e] = make_float2(v.x * t, v.y * t);
+  }
+}
+
 // ----------------------------------------------------------- row passes
 // (rows.cuh: RowCfg, the c2r / r2c row steps and rows_body)
 template <int N, class Op>
@@ -522,7 +540,14 @@ struct Launch {
   }
   static int lpt(Plan* p, const LptArgs& a, cudaStream_t st) {
     int64_t fs = fstride(p);
-    LptOp<N, W, 0> ho{a, p->d_phik, p->d_work, fs, tiles(p), p->HP, 6};
+    float2* phit = p->d_work + 7 * fs;  // T/(D Beta) phi, read by the Hessian and psi1 passes
+    {
+      ProfScope ps_(p, "lpt_scale_twb", st);
+      k_scale_twb<N><<<(unsigned)(p->num_sms * 8), 256, 0, st>>>(p->d_phik, phit, p->HP, p->d_twb);
+    }
+    AAR_CUDA_TRY(p, cudaGetLastError());
+    p->last_launches += 1;
+    LptOp<N, W, 0> ho{a, phit, p->d_work, fs, tiles(p), p->HP, 6};
     int rc = run_pass<N>(p, ho, tiles(p) * 6, st, "lpt_xinv_hess");
     if (rc) return rc;
     if ((rc = ypass<+1>(p, p->d_work, 6, nullptr, st, "lpt_ypass_inv_hess"))) return rc;
@@ -543,7 +568,7 @@ struct Launch {
     }
     LptOp<N, W, 2> m2{a, p->d_phik, p->d_work, fs, tiles(p), p->HP, 6};
     if ((rc = run_pass<N>(p, m2, tiles(p) * 3, st, "lpt_xpsi2"))) return rc;
-    LptOp<N, W, 1> m1{a, p->d_phik, p->d_work, fs, tiles(p), p->HP, 6};
+    LptOp<N, W, 1> m1{a, phit, p->d_work, fs, tiles(p), p->HP, 6};
     if ((rc = run_pass<N>(p, m1, tiles(p) * 3, st, "lpt_xpsi1"))) return rc;
     if ((rc = ypass<+1>(p, p->d_work, 6, nullptr, st, "lpt_ypass_inv_disp"))) return rc;
     using R = RowCfg<N>;

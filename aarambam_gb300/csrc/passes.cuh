@@ -141,9 +141,11 @@ struct XinvOp {
 
 // 2LPT passes (MODE 0: Hessians, items tile * 6 + comp; MODE 1: ZA
 // displacements, items tile * 3 + a; MODE 2: 2LPT displacements, items
-// tile * 3 + a): the factor lpt_factor<MODE> (main.c:1180-1368) on phi, or
-// for MODE 2 on the source slot already transformed along x, then the
-// inverse x FFT.  Outputs: Hessians to slots 0..5, psi1 to slots 0..2, psi2
+// tile * 3 + a): the factor lpt_factor<MODE> (main.c:1180-1368) on
+// T/(D Beta) phi (MODE 0, 1: `phi` points at that product, made once by
+// k_scale_twb, so the per-|k|^2 table is not gathered nine times), or for
+// MODE 2 on the source slot already transformed along x; then the inverse x
+// FFT.  Outputs: Hessians to slots 0..5, psi1 to slots 0..2, psi2
 // to slots 3..5.
 template <int N, int W, int MODE>
 struct LptOp {
@@ -184,7 +186,7 @@ struct LptOp {
       const int n2 = kx * kx + ky * ky + kz * kz;
       float f = 0.f;
       if (own && kz <= N / 2) {
-        const float2 g = lpt_factor<MODE>(a, comp, n, o, kz, kx, ky, n2);
+        const float2 g = lpt_factor<MODE, false>(a, comp, n, o, kz, kx, ky, n2);
         f = MODE == 0 ? g.x : g.y;
       }
       r.f[i] = f;

@@ -41,8 +41,9 @@ LptArgs lpt_args(Plan* p);
 //   MODE 0  Hessian ab:   -k_a k_b T/(D Beta)          (comp 0..5 = 00 01 02 11 12 22)
 //   MODE 1  ZA psi1_a:    i k_a T/(D Beta) smth
 //   MODE 2  2LPT psi2_a: -i k_a / k^2 smth            (0 at k = 0)
-// smth = [sinc_x sinc_y sinc_z]^-2 (CORRECT_CIC).
-template <int MODE>
+// smth = [sinc_x sinc_y sinc_z]^-2 (CORRECT_CIC).  TWB = false leaves out
+// the T/(D Beta) factor, for a phi that already carries it.
+template <int MODE, bool TWB = true>
 __device__ __forceinline__ float2 lpt_factor(const LptArgs& a, int comp, int i, int j, int kz, int kx, int ky, int n2) {
   const float kF = a.m.g.kF;
   const int ax = MODE == 0 ? (comp < 3 ? 0 : (comp < 5 ? 1 : 2)) : comp;
@@ -50,11 +51,11 @@ __device__ __forceinline__ float2 lpt_factor(const LptArgs& a, int comp, int i, 
   if (MODE == 0) {
     const int bx = comp == 0 ? 0 : comp == 1 ? 1 : comp == 2 ? 2 : comp == 3 ? 1 : 2;
     const float kb = kF * (float)(bx == 0 ? kx : bx == 1 ? ky : kz);
-    return make_float2(-ka * kb * __ldg(a.twb + n2), 0.f);
+    return make_float2(TWB ? -ka * kb * __ldg(a.twb + n2) : -ka * kb, 0.f);
   }
   const float ff = 1.f / (__ldg(a.sinc + i) * __ldg(a.sinc + j) * __ldg(a.sinc + kz));
   const float smth = ff * ff;
-  if (MODE == 1) return make_float2(0.f, ka * __ldg(a.twb + n2) * smth);
+  if (MODE == 1) return make_float2(0.f, TWB ? ka * __ldg(a.twb + n2) * smth : ka * smth);
   if (n2 == 0) return make_float2(0.f, 0.f);
   return make_float2(0.f, -ka / (kF * kF * (float)n2) * smth);
 }

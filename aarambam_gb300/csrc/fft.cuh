@@ -330,4 +330,11 @@ __host__ __device__ constexpr int lanes_for(int N) {
   return N >= 512 ? N / 16 : (N / 8 >= 1 ? (N / 8 < 32 ? N / 8 : 32) : 1);
 }
 
+// lanes per line of the strided (tile) passes: 32 values per lane for
+// N >= 512, so that a 512- or 1024-point line is two Stockham stages
+// (32 x 16, 32 x 32) instead of three, one warp per line.  (The row kernels
+// keep lanes_for: their 512-point half lines with 32 values per lane were
+// slower, 140 vs 95 ms at 1024^3.)
+__host__ __device__ constexpr int lanes_for_tile(int N) { return N >= 512 ? N / 32 : lanes_for(N); }
+
 }  // namespace aar

@@ -56,14 +56,15 @@ __host__ __device__ constexpr int tile_ls(int N) {
 
 template <int N, int W>
 struct AxisCfg {
-  static constexpr int T = lanes_for(N);  // lanes per line (may span two warps)
+  static constexpr int T = lanes_for_tile(N);  // lanes per line
   static constexpr int E = N / T;
   static constexpr int THREADS = ((W * T + 31) / 32) * 32;
   static constexpr int WARPS = THREADS / 32;
   static constexpr int LS = tile_ls(N);  // smem line stride (float2)
   static constexpr size_t SMEM = sizeof(float2) * (size_t)W * LS;
   static constexpr int PER = N * W / THREADS;  // tile elements per thread
-  static constexpr int MINB = THREADS >= 512 ? 2 : 4;  // resident blocks per SM aimed at
+  // resident blocks per SM aimed at: 32 values per lane need ~128 registers
+  static constexpr int MINB = E >= 32 ? (THREADS >= 256 ? 2 : 4) : THREADS >= 512 ? 2 : 4;
 };
 
 // Tile indexing.  Axis 0 (x): rows n = x, other index o = y.  Axis 1 (y):

@@ -51,6 +51,25 @@ def test_batch_graph_matches_single_runs(cuda):
     b.close()
 
 
+def test_batch_graph_with_runtime_row_kernel(cuda):
+    # 256^3: the modal rows run the NVRTC-specialised kernel inside the graph
+    N, n = 256, 2
+    gens = make_gens(N, n)
+    assert all(g.jit_status == "on" for g in gens)
+    lagr = [lattice(N, 500.0, cuda) for _ in range(n)]
+    want = [g.run(l) for g, l in zip(gens, lagr)]
+    torch.cuda.synchronize()
+    b = ICBatch(gens)
+    pos = [torch.empty_like(l) for l in lagr]
+    vel = [torch.empty_like(l) for l in lagr]
+    for _ in range(2):
+        b.run(lagr, pos, vel)
+        torch.cuda.synchronize()
+        for i in range(n):
+            assert torch.equal(pos[i], want[i][0]) and torch.equal(vel[i], want[i][1]), i
+    b.close()
+
+
 def test_batch_rejects_bad_arrays(cuda):
     gens = make_gens(32, 2)
     b = ICBatch(gens)

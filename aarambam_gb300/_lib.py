@@ -20,6 +20,8 @@ AAR_ERR_TRANSFER = 1111
 AAR_ERR_TRANSFER_DUP = 777
 AAR_FUSED_FP32 = 0
 AAR_PLAIN_FP64 = 1
+AAR_VARIANT_BASIS = 0
+AAR_VARIANT_RESBASIS = 1
 
 # every symbol include/aarambam.h declares
 EXPORTS = [
@@ -42,7 +44,8 @@ class Params(C.Structure):
                 ("unit_mass_in_g", C.c_double), ("unit_velocity_in_cm_per_s", C.c_double),
                 ("input_spectrum_unit_length_in_cm", C.c_double), ("fixed_amplitude", C.c_int32),
                 ("phase_flip", C.c_int32), ("sphere_mode", C.c_int32), ("precision", C.c_int32),
-                ("mem_limit_bytes", C.c_int64)]
+                ("mem_limit_bytes", C.c_int64), ("variant", C.c_int32), ("which_spectrum", C.c_int32),
+                ("a_res", C.c_double), ("w_res", C.c_double), ("phi_res", C.c_double)]
 
 
 class Scalars(C.Structure):

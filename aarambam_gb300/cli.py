@@ -1,5 +1,8 @@
-"""`Aarambam-2LPT-Basis <paramfile>`: the reference executable's command line
-(Aarambam/LPT/Basis/cli.py:5-10 -> main.c:53-102) on one GPU.
+"""`Aarambam-2LPT-Basis <paramfile>` and `Aarambam-2LPT-ResBasis <paramfile>`:
+the reference executables' command lines (Aarambam/LPT/Basis/cli.py:5-10 and
+LPT/ResBasis/cli.py:5-10 -> main.c:53-102) on one GPU.  ResBasis reads three
+more tags (A_res, w_res, phi_res) and takes WhichSpectrum 0, 1 or 2 as its
+P(k) oscillation mode.
 
 Reads the same parameter file, coefficient tables, transfer table and glass,
 runs the path through libaarambam_gpu.so and writes the same files:
@@ -60,6 +63,18 @@ def _growth(a, om, ol):
                      epsrel=1e-10, limit=200)[0]
 
 
+def power_osc(cfg, k):
+    """The P(k) oscillation of 2LPTResBasis (ResBasis/power.c:240-260); 1 for
+    a Basis parameter set."""
+    if "A_res" not in cfg:
+        return 1.0
+    if cfg["WhichSpectrum"] == 1:
+        return 1 + cfg["A_res"] * math.cos(cfg["w_res"] * k + cfg["phi_res"])
+    if cfg["WhichSpectrum"] == 2:
+        return 1 + cfg["A_res"] * math.cos(cfg["w_res"] * math.log(k) + cfg["phi_res"])
+    return 1.0
+
+
 def print_spec(path, cfg, norm, transfer):
     """inputspec_<FileBase>.txt (main.c:1631-1694): k, Delta^2, k_nl, Delta^2_nl
     (Peacock & Dodds)."""
@@ -70,7 +85,7 @@ def print_spec(path, cfg, norm, transfer):
 
     def pk(k):
         t = transfer(k)
-        return norm * math.exp(cfg["PrimordialIndex"] * math.log(k)) * t * t
+        return norm * math.exp(cfg["PrimordialIndex"] * math.log(k)) * power_osc(cfg, k) * t * t
 
     lines = [f"{cfg['Redshift']:12g} {ddd:12g}"]
     k = 2 * PI / (1000.0 * (3.085678e24 / ul))
@@ -119,8 +134,13 @@ def run(cfg: dict, precision: str = "fp32", log=print) -> dict:
 
     from .ic import ICGenerator
 
-    if cfg["WhichSpectrum"] != 0 or cfg["WhichTransfer"] != 2:
-        raise ValueError("only WhichSpectrum 0 with a tabulated transfer function (WhichTransfer 2) is supported")
+    if cfg["WhichTransfer"] != 2:
+        raise ValueError("only a tabulated transfer function (WhichTransfer 2) is supported")
+    if "A_res" in cfg:
+        if cfg["WhichSpectrum"] not in (0, 1, 2):
+            raise ValueError("2LPTResBasis: WhichSpectrum must be 0, 1 or 2")
+    elif cfg["WhichSpectrum"] != 0:
+        raise ValueError("2LPTBasis: only WhichSpectrum 0 (the tabulated transfer function) is supported")
     if cfg["WDM_On"]:
         raise ValueError("WDM_On is not supported")
     M = cfg["N_modes"]
@@ -160,14 +180,14 @@ def run(cfg: dict, precision: str = "fp32", log=print) -> dict:
     return dict(pos=pos, vel=vel, ids=ids, scalars=sc, **out)
 
 
-def main(argv=None) -> int:
+def main(argv=None, variant: str = "basis") -> int:
     argv = sys.argv[1:] if argv is None else argv
     if not argv:
         sys.stdout.write("\nParameters are missing.\nCall with <ParameterFile>\n\n")
         return 0
     sys.stdout.write("RUNNING LPTPNG WITH 1 TASKS")
     try:
-        cfg = params.read_parameterfile(argv[0])
+        cfg = params.read_parameterfile(argv[0], variant)
     except params.ParameterError as e:
         for m in e.messages:
             sys.stdout.write(m + "\n")
@@ -177,5 +197,13 @@ def main(argv=None) -> int:
     return 0
 
 
+def main_resbasis(argv=None) -> int:
+    """`Aarambam-2LPT-ResBasis <paramfile>`."""
+    return main(argv, "resbasis")
+
+
 if __name__ == "__main__":
+    # python -m aarambam_gb300.cli [--resbasis] <paramfile>
+    if sys.argv[1:2] == ["--resbasis"]:
+        sys.exit(main_resbasis(sys.argv[2:]))
     sys.exit(main())

@@ -17,6 +17,25 @@ constexpr double kPi = 3.14159265358979323846;  // PI as the reference defines i
 // signed wavenumber index of grid index i (main.c:410-423): N/2 -> -N/2
 __host__ __device__ __forceinline__ int sidx(int i, int N) { return i < N / 2 ? i : i - N; }
 
+// Row order of the fused form's fields.  A field (complex half-spectrum or
+// real) is N^2 rows of HP complex / 2 HP real values, one row per (x, y);
+// the row of (x, y) is row_of(x, y, N, xb), i.e. x is split into blocks of
+// xb: [x / xb][y][x % xb].  With xb = kXB the N rows of an x line lie in
+// N / kXB groups of kXB rows 4*HP bytes apart, instead of N rows N*HP*8 bytes
+// apart: measured on GB300 at N = 1024, a tile copy with the x-pass pattern
+// ran at 3.4 TB/s in natural order and 6.7 TB/s blocked (xb = 4 to 64),
+// while the y-pass pattern stayed at 7.0-7.2 TB/s for xb <= 8.  xb = 1 is
+// the natural [x][y] order of the reference and of the C-ABI's buffers.
+constexpr int kXB = 4;
+__host__ __device__ __forceinline__ int64_t row_of(int x, int y, int N, int xb) {
+  return ((int64_t)(x / xb) * N + y) * xb + x % xb;
+}
+__host__ __device__ __forceinline__ void row_xy(int64_t m, int N, int xb, int& x, int& y) {
+  const int64_t q = m / xb;
+  x = (int)((q / N) * xb + m % xb);
+  y = (int)(q % N);
+}
+
 // Geometry and scalars of one plan, passed by value to kernels.
 struct Grid {
   int N;       // Nmesh
@@ -49,6 +68,25 @@ __device__ __forceinline__ bool keep_cell(const Grid& g, int kx, int ky, int kz)
 int host_kcut(int nsample, double box);
 
 // ----------------------------------------------------------- plan state
+// ResBasis oscillation of the primordial spectrum.  power_osc: the factor
+// in PowerSpec (ResBasis/power.c:240-260), used by the sigma8
+// normalisation; one case per WhichSpectrum.  noise_osc: the factors on the
+// per-cell power phig of the Gaussian potential (ResBasis/main.c:445-455),
+// where the switch has no break, so WhichSpectrum 0 and 1 apply the linear
+// and then the log oscillation and 2 the log one only.  Basis: no factor.
+__host__ __device__ inline double power_osc(const aar_params& q, double k) {
+  if (q.variant != AAR_VARIANT_RESBASIS) return 1.0;
+  if (q.which_spectrum == 1) return 1 + q.a_res * cos(q.w_res * k + q.phi_res);
+  if (q.which_spectrum == 2) return 1 + q.a_res * cos(q.w_res * log(k) + q.phi_res);
+  return 1.0;
+}
+__host__ __device__ inline double noise_osc(const aar_params& q, double phig, double kmag) {
+  if (q.variant != AAR_VARIANT_RESBASIS) return phig;
+  if (q.which_spectrum <= 1) phig *= (1.0 + q.a_res * cos(q.w_res * kmag + q.phi_res));
+  phig *= (1.0 + q.a_res * cos(q.w_res * log(kmag) + q.phi_res));
+  return phig;
+}
+
 struct Plan {
   aar_params prm;
   std::string err;
@@ -86,6 +124,7 @@ struct Plan {
   int row_ls = 0;                // row-kernel line stride (float2) of this grid size
   void* jit = nullptr;           // run-time specialised modal row kernel (jit.cu), or null
   int jit_mode = 1;              // 0 off, 1 for N >= 256, 2 always
+  int64_t xpass_group = 1;       // tiles per item group of the multi-output x passes (passes.cuh)
   std::string jit_status = "off";
   int nterms = 0, nr_active = 0;
   // plain FP64 form
@@ -141,6 +180,9 @@ void plain_free(Plan* p);
 int fused_c2r(Plan* p, const float2* in, float* out, cudaStream_t st);
 int fused_r2c(Plan* p, const float* in, float2* out, cudaStream_t st);
 int fused_configure_xform(Plan* p);
+// row copy between row orders (row_of), ncols elements of `elem` bytes per row
+int copy_rows(Plan* p, void* dst, int64_t dst_ld, int dst_xb, const void* src, int64_t src_ld, int src_xb, int ncols,
+              size_t elem, cudaStream_t st);
 int noalloc_gaussian(Plan* p, void* d_out, cudaStream_t st);
 int jit_prepare(Plan* p);
 int jit_modal_rows(Plan* p, float2* work, int64_t fs, cudaStream_t st);

@@ -6,6 +6,7 @@
 #include <math.h>
 #include <stdint.h>
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
@@ -174,7 +175,7 @@ static int set_transfer(Plan* p, const double* k, const double* t, int n) {
         if (kr < 1e-8) return 0.0;
         double w = 3 * (sin(kr) / kr3 - cos(kr) / kr2);
         double T = cz.transfer(kk);
-        double P = 1.0 * exp(q.primordial_index * log(kk)) * T * T;
+        double P = 1.0 * exp(q.primordial_index * log(kk)) * power_osc(q, kk) * T * T;
         return 4 * kPi * kk * kk * w * w * P;
       },
       0, 500.0 * 1 / R8);
@@ -201,7 +202,8 @@ static int set_transfer(Plan* p, const double* k, const double* t, int n) {
     double fac = pow(2 * kPi / q.box, 1.5);
     for (int64_t n2 = 0; n2 < nsq; ++n2) {
       double km = kF * sqrt((double)n2), k2 = km * km;
-      amp[n2] = n2 ? (float)(sqrt(p->Anorm * exp(q.primordial_index * log(km))) * fac * p->Beta / k2) : 0.f;
+      amp[n2] = n2 ? (float)(sqrt(noise_osc(q, p->Anorm * exp(q.primordial_index * log(km)), km)) * fac * p->Beta / k2)
+                   : 0.f;
       twb[n2] = (float)(cz.transfer(km) / p->Dplus / p->Beta);
     }
     AAR_CUDA_TRY(p, cudaMemcpy(p->d_amp, amp.data(), sizeof(float) * nsq, cudaMemcpyHostToDevice));
@@ -346,8 +348,18 @@ static int create(Plan* p) {
     return set_err(p, "plain FP64 form supports even Nmesh up to 2048"), AAR_ERR_ARG;
   if (!(q.box > 0) || q.nsample <= 0) return set_err(p, "Box and Nsample must be positive"), AAR_ERR_ARG;
   if (q.seed < 0) return set_err(p, "Seed must be >= 0"), AAR_ERR_ARG;
+  if (q.variant == AAR_VARIANT_BASIS) {
+    if (q.which_spectrum != 0)
+      return set_err(p, "2LPTBasis: only WhichSpectrum 0 (the tabulated transfer function) is supported"), AAR_ERR_ARG;
+  } else if (q.variant == AAR_VARIANT_RESBASIS) {
+    if (q.which_spectrum < 0 || q.which_spectrum > 2)
+      return set_err(p, "2LPTResBasis: WhichSpectrum must be 0, 1 or 2"), AAR_ERR_ARG;
+  } else {
+    return set_err(p, "unknown variant"), AAR_ERR_ARG;
+  }
   AAR_CUDA_TRY(p, cudaGetDevice(&p->dev));
   AAR_CUDA_TRY(p, cudaDeviceGetAttribute(&p->num_sms, cudaDevAttrMultiProcessorCount, p->dev));
+  if (const char* g = getenv("AAR_XPASS_GROUP")) p->xpass_group = std::max(1LL, atoll(g));
   p->N = N;
   p->HP = ((N / 2 + 1) + 7) / 8 * 8;
   p->grid.N = N;
@@ -640,10 +652,8 @@ int aar_copy_spectrum(aar_plan* h, void* d_out, void* stream) {
   if (!h || !d_out) return AAR_ERR_ARG;
   Plan* p = &h->p;
   if (p->prm.precision != AAR_FUSED_FP32 || !p->d_phik) return set_err(p, "no FP32 spectrum in this plan"), AAR_ERR_STATE;
-  int N = p->N, H = N / 2 + 1;
-  AAR_CUDA_TRY(p, cudaMemcpy2DAsync(d_out, sizeof(float2) * H, p->d_phik, sizeof(float2) * p->HP, sizeof(float2) * H,
-                                    (size_t)N * N, cudaMemcpyDeviceToDevice, S(stream)));
-  return AAR_OK;
+  const int H = p->N / 2 + 1;
+  return copy_rows(p, d_out, H, 1, p->d_phik, p->HP, kXB, H, sizeof(float2), S(stream));
 }
 
 int aar_gaussian_spectrum_noalloc(aar_plan* h, void* d_out, void* stream) {
@@ -727,9 +737,7 @@ int aar_copy_field(aar_plan* h, int32_t which, float* d_out, void* stream) {
   if (p->prm.precision != AAR_FUSED_FP32 || !p->d_work) return set_err(p, "no FP32 fields in this plan"), AAR_ERR_STATE;
   int N = p->N;
   const float* src = (const float*)(p->d_work + (size_t)which * N * N * p->HP);
-  AAR_CUDA_TRY(p, cudaMemcpy2DAsync(d_out, sizeof(float) * N, src, sizeof(float) * 2 * p->HP, sizeof(float) * N,
-                                    (size_t)N * N, cudaMemcpyDeviceToDevice, S(stream)));
-  return AAR_OK;
+  return copy_rows(p, d_out, N, 1, src, 2 * p->HP, kXB, N, sizeof(float), S(stream));
 }
 
 // ------------------------------------------------------------- JIT rows
@@ -749,10 +757,8 @@ int aar_set_spectrum(aar_plan* h, const void* d_in, void* stream) {
   if (!h || !d_in) return AAR_ERR_ARG;
   Plan* p = &h->p;
   if (p->prm.precision != AAR_FUSED_FP32 || !p->d_phik) return set_err(p, "aar_set_spectrum is for the fused form"), AAR_ERR_ARG;
-  const int N = p->N, H = N / 2 + 1;
-  AAR_CUDA_TRY(p, cudaMemcpy2DAsync(p->d_phik, sizeof(float2) * p->HP, d_in, sizeof(float2) * H, sizeof(float2) * H,
-                                    (size_t)N * N, cudaMemcpyDeviceToDevice, S(stream)));
-  return AAR_OK;
+  const int H = p->N / 2 + 1;
+  return copy_rows(p, p->d_phik, p->HP, kXB, d_in, H, 1, H, sizeof(float2), S(stream));
 }
 
 static int adj_ready(Plan* p) {

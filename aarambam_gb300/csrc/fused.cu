@@ -68,7 +68,8 @@ struct AxisCfg {
 };
 
 // Tile indexing.  Axis 0 (x): rows n = x, other index o = y.  Axis 1 (y):
-// rows n = y, o = x.  Column w covers kz = c0 + w.
+// rows n = y, o = x.  Column w covers kz = c0 + w.  Fields are in the
+// x-blocked row order row_of(x, y, N, kXB).
 // Tile element ownership: thread t owns column w = t % W and rows
 // n = t / W + q THREADS/W, q < PER; with THREADS/W a multiple of 16 the
 // padded shared index and the global offset are a per-thread base plus a
@@ -83,12 +84,14 @@ struct TileAddr {
     w = threadIdx.x % W;
     n0 = threadIdx.x / W;
     sbase = w * C::LS + spad(n0);
+    // a thread's rows n0 + q DN keep n0 % kXB, so the offsets stay affine in q
+    static_assert(DN % kXB == 0, "row step of a tile thread must be a multiple of the x block");
     if (AXIS == 0) {
-      gbase = ((int64_t)n0 * N + o) * HP + c0 + w;
+      gbase = row_of(n0, o, N, kXB) * HP + c0 + w;
       gstep = (int64_t)DN * N * HP;
     } else {
-      gbase = ((int64_t)o * N + n0) * HP + c0 + w;
-      gstep = (int64_t)DN * HP;
+      gbase = row_of(o, n0, N, kXB) * HP + c0 + w;
+      gstep = (int64_t)DN * kXB * HP;
     }
   }
   __device__ __forceinline__ int s(int q) const {
@@ -143,12 +146,23 @@ __global__ void __launch_bounds__(256) k_modal_acc(ModalArgs a, float2* phi, con
                                                    const float* __restrict__ rtab, int rstride) {
   constexpr int K = N / 2 + 1;  // kz = 0 .. N/2 of a row
   constexpr int64_t total = (int64_t)N * N * K;
+  // the active slots and their field bases, once per block
+  __shared__ int rs[kMaxModes];
+  __shared__ const float2* base[kMaxModes];
   const int nr = dt->tl.nr;
+  if (threadIdx.x < nr) {
+    const int r = dt->tl.r_of_slot[threadIdx.x];
+    rs[threadIdx.x] = r;
+    base[threadIdx.x] = work + (int64_t)r * fs;
+  }
+  __syncthreads();
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t row = i / K;
     const int kz = (int)(i - row * K);
     const int64_t e = row * HP + kz;
-    const int kx = sidx((int)(row / N), N), ky = sidx((int)(row % N), N);
+    int x, y;
+    row_xy(row, N, kXB, x, y);
+    const int kx = sidx(x, N), ky = sidx(y, N);
     const int n2 = kx * kx + ky * ky + kz * kz;
     if (n2 == 0) {
       phi[e] = make_float2(0.f, 0.f);
@@ -157,11 +171,10 @@ __global__ void __launch_bounds__(256) k_modal_acc(ModalArgs a, float2* phi, con
     if (!keep_cell(a.g, kx, ky, kz)) continue;
     const float* rt = rtab + (int64_t)n2 * rstride;
     float sx = 0.f, sy = 0.f, cx = 0.f, cy = 0.f;
-#pragma unroll 4
+#pragma unroll 8
     for (int k = 0; k < nr; ++k) {
-      const int r = dt->tl.r_of_slot[k];
-      const float rho = __ldg(rt + r);
-      const float2 v = __ldg(work + (int64_t)r * fs + e);
+      const float rho = __ldg(rt + rs[k]);
+      const float2 v = __ldg(base[k] + e);
       const float tx = v.x * rho, ty = v.y * rho;
       const float ux = sx + tx, uy = sy + ty;
       cx += (fabsf(sx) >= fabsf(tx)) ? (sx - ux) + tx : (tx - ux) + sx;
@@ -187,7 +200,9 @@ __global__ void __launch_bounds__(256) k_scale_twb(const float2* __restrict__ ph
     const int64_t row = i / K;
     const int kz = (int)(i - row * K);
     const int64_t e = row * HP + kz;
-    const int kx = sidx((int)(row / N), N), ky = sidx((int)(row % N), N);
+    int x, y;
+    row_xy(row, N, kXB, x, y);
+    const int kx = sidx(x, N), ky = sidx(y, N);
     const float t = __ldg(twb + kx * kx + ky * ky + kz * kz);
     const float2 v = phi[e];
     out[e] = make_float2(v.x * t, v.y * t);
@@ -379,8 +394,8 @@ __device__ __forceinline__ void readout_one(const ReadArgs& a, const float* __re
     jj[d] = (i + 1 == N) ? 0 : i + 1;
   }
   const int64_t rs = 2 * (int64_t)a.HP;
-  int64_t o000 = ((int64_t)ii[0] * N + ii[1]) * rs, o010 = ((int64_t)ii[0] * N + jj[1]) * rs;
-  int64_t o100 = ((int64_t)jj[0] * N + ii[1]) * rs, o110 = ((int64_t)jj[0] * N + jj[1]) * rs;
+  int64_t o000 = row_of(ii[0], ii[1], N, kXB) * rs, o010 = row_of(ii[0], jj[1], N, kXB) * rs;
+  int64_t o100 = row_of(jj[0], ii[1], N, kXB) * rs, o110 = row_of(jj[0], jj[1], N, kXB) * rs;
   float u = fr[0], v = fr[1], w = fr[2];
   float f1 = (1 - u) * (1 - v) * (1 - w), f2 = (1 - u) * (1 - v) * w, f3 = (1 - u) * v * (1 - w),
         f4 = (1 - u) * v * w, f5 = u * (1 - v) * (1 - w), f6 = u * (1 - v) * w, f7 = u * v * (1 - w),
@@ -483,7 +498,7 @@ struct Launch {
   }
   static int modal(Plan* p, const ModalArgs& a, cudaStream_t st) {
     int64_t fs = fstride(p);
-    XinvOp<N, W> xo{a, p->d_phik, p->d_work, fs, tiles(p), p->nsq, p->HP, p->d_qtab};
+    XinvOp<N, W> xo{a, p->d_phik, p->d_work, fs, tiles(p), p->nsq, p->HP, p->d_qtab, p->xpass_group};
     int rc = run_pass<N>(p, xo, tiles(p) * a.M, st, "modal_xinv");
     if (rc) return rc;
     if ((rc = ypass<+1>(p, p->d_work, a.M, nullptr, st, "modal_ypass_inv"))) return rc;
@@ -548,7 +563,7 @@ struct Launch {
     }
     AAR_CUDA_TRY(p, cudaGetLastError());
     p->last_launches += 1;
-    LptOp<N, W, 0> ho{a, phit, p->d_work, fs, tiles(p), p->HP, 6};
+    LptOp<N, W, 0> ho{a, phit, p->d_work, fs, tiles(p), p->HP, 6, p->xpass_group};
     int rc = run_pass<N>(p, ho, tiles(p) * 6, st, "lpt_xinv_hess");
     if (rc) return rc;
     if ((rc = ypass<+1>(p, p->d_work, 6, nullptr, st, "lpt_ypass_inv_hess"))) return rc;
@@ -567,9 +582,9 @@ struct Launch {
       AxisOp<N, W, 0, -1> xs{p->d_work + 6 * fs, 0, tiles(p), p->HP, nullptr};
       if ((rc = run_pass<N>(p, xs, tiles(p), st, "lpt_xfwd_source"))) return rc;
     }
-    LptOp<N, W, 2> m2{a, p->d_phik, p->d_work, fs, tiles(p), p->HP, 6};
+    LptOp<N, W, 2> m2{a, p->d_phik, p->d_work, fs, tiles(p), p->HP, 6, p->xpass_group};
     if ((rc = run_pass<N>(p, m2, tiles(p) * 3, st, "lpt_xpsi2"))) return rc;
-    LptOp<N, W, 1> m1{a, phit, p->d_work, fs, tiles(p), p->HP, 6};
+    LptOp<N, W, 1> m1{a, phit, p->d_work, fs, tiles(p), p->HP, 6, p->xpass_group};
     if ((rc = run_pass<N>(p, m1, tiles(p) * 3, st, "lpt_xpsi1"))) return rc;
     if ((rc = ypass<+1>(p, p->d_work, 6, nullptr, st, "lpt_ypass_inv_disp"))) return rc;
     using R = RowCfg<N>;
@@ -792,29 +807,52 @@ struct Xform {
   }
 };
 
+// Row copy between row orders: row (x, y) of src (order src_xb, ld src_ld
+// elements) to row (x, y) of dst, the first ncols elements of each row.
+// Moves fields between the caller's natural [x][y] buffers and the plan's
+// x-blocked ones.
+template <class T>
+__global__ void k_copy_rows(T* __restrict__ dst, int64_t dst_ld, int dst_xb, const T* __restrict__ src, int64_t src_ld,
+                            int src_xb, int N, int ncols) {
+  const int64_t total = (int64_t)N * N * ncols;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = i / ncols;
+    const int c = (int)(i - r * ncols);
+    const int x = (int)(r / N), y = (int)(r % N);
+    dst[row_of(x, y, N, dst_xb) * dst_ld + c] = src[row_of(x, y, N, src_xb) * src_ld + c];
+  }
+}
+
+int copy_rows(Plan* p, void* dst, int64_t dst_ld, int dst_xb, const void* src, int64_t src_ld, int src_xb, int ncols,
+              size_t elem, cudaStream_t st) {
+  const unsigned nb = (unsigned)(p->num_sms * 8);
+  if (elem == sizeof(float2))
+    k_copy_rows<float2><<<nb, 256, 0, st>>>((float2*)dst, dst_ld, dst_xb, (const float2*)src, src_ld, src_xb, p->N,
+                                            ncols);
+  else
+    k_copy_rows<float><<<nb, 256, 0, st>>>((float*)dst, dst_ld, dst_xb, (const float*)src, src_ld, src_xb, p->N,
+                                           ncols);
+  AAR_CUDA_TRY(p, cudaGetLastError());
+  return AAR_OK;
+}
+
 // unnormalised FFTW-convention transforms through work slot 0
 int fused_c2r(Plan* p, const float2* in, float* out, cudaStream_t st) {
   int N = p->N, H = N / 2 + 1;
   float2* slot = p->d_work;
-  AAR_CUDA_TRY(p, cudaMemcpy2DAsync(slot, sizeof(float2) * p->HP, in, sizeof(float2) * H, sizeof(float2) * H,
-                                    (size_t)N * N, cudaMemcpyDeviceToDevice, st));
-  int rc = dispatch_n(N, [&](auto nc) { return Xform<decltype(nc)::value>::c2r(p, slot, st); });
+  int rc = copy_rows(p, slot, p->HP, kXB, in, H, 1, H, sizeof(float2), st);
   if (rc) return rc;
-  AAR_CUDA_TRY(p, cudaMemcpy2DAsync(out, sizeof(float) * N, slot, sizeof(float) * 2 * p->HP, sizeof(float) * N,
-                                    (size_t)N * N, cudaMemcpyDeviceToDevice, st));
-  return AAR_OK;
+  if ((rc = dispatch_n(N, [&](auto nc) { return Xform<decltype(nc)::value>::c2r(p, slot, st); }))) return rc;
+  return copy_rows(p, out, N, 1, slot, 2 * p->HP, kXB, N, sizeof(float), st);
 }
 
 int fused_r2c(Plan* p, const float* in, float2* out, cudaStream_t st) {
   int N = p->N, H = N / 2 + 1;
   float2* slot = p->d_work;
-  AAR_CUDA_TRY(p, cudaMemcpy2DAsync(slot, sizeof(float) * 2 * p->HP, in, sizeof(float) * N, sizeof(float) * N,
-                                    (size_t)N * N, cudaMemcpyDeviceToDevice, st));
-  int rc = dispatch_n(N, [&](auto nc) { return Xform<decltype(nc)::value>::r2c(p, slot, st); });
+  int rc = copy_rows(p, slot, 2 * p->HP, kXB, in, N, 1, N, sizeof(float), st);
   if (rc) return rc;
-  AAR_CUDA_TRY(p, cudaMemcpy2DAsync(out, sizeof(float2) * H, slot, sizeof(float2) * p->HP, sizeof(float2) * H,
-                                    (size_t)N * N, cudaMemcpyDeviceToDevice, st));
-  return AAR_OK;
+  if ((rc = dispatch_n(N, [&](auto nc) { return Xform<decltype(nc)::value>::r2c(p, slot, st); }))) return rc;
+  return copy_rows(p, out, H, 1, slot, p->HP, kXB, H, sizeof(float2), st);
 }
 
 int fused_configure_xform(Plan* p) {

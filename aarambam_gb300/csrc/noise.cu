@@ -10,7 +10,9 @@
 // Noise (main.c:382-524): one thread per (i, j) column reseeds ranlxd1 with
 // seedtable[i][j] and draws (phase, amplitude) pairs for k < N/2, skipping the
 // Nyquist indices and DC after the draws, keeping the cube/sphere cut, and
-// writing the k = 0 plane with its Hermitian partner.
+// writing the k = 0 plane with its Hermitian partner.  The fused plan's
+// spectrum is written in its x-blocked row order; the plain form and the
+// caller's buffers in the natural one.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -85,10 +87,12 @@ int launch_seedtable(Plan* p, uint32_t seed, uint32_t* d_out, cudaStream_t st) {
 // ------------------------------------------------------------ noise
 struct NoiseArgs {
   Grid g;
+  int xb;  // row order of the output: row_of(i, j, N, xb)
   int phase_flip, fixed_amp;
   // FP64 form: the reference's own formula
   double anorm, ns, fac, beta;
-  // FP32 form: amplitude per n^2 = sqrt(Anorm k^ns) fac Beta / k^2
+  aar_params prm;  // variant and ResBasis oscillation (noise_osc)
+  // FP32 form: amplitude per n^2 = sqrt(Anorm k^ns osc) fac Beta / k^2
   const float* amp;
 };
 
@@ -147,7 +151,7 @@ __global__ void k_noise(NoiseArgs a, const uint32_t* __restrict__ seedtable, voi
       double phase = __dmul_rn(__dmul_rn((double)U1 * 3.5527136788005009e-15, 2.0), kPi);
       if (a.phase_flip) phase = __dadd_rn(phase, kPi);
       double ampl = (double)U2 * 3.5527136788005009e-15;
-      double phig = a.anorm * exp(a.ns * log(km));
+      double phig = noise_osc(a.prm, a.anorm * exp(a.ns * log(km)), km);
       if (!a.fixed_amp) phig *= -log(ampl);
       phig = sqrt(phig) * a.fac * a.beta / k2;
       double sn, cs;
@@ -167,16 +171,16 @@ __global__ void k_noise(NoiseArgs a, const uint32_t* __restrict__ seedtable, voi
     }
     int64_t c1 = -1, c2 = -1;
     if (k > 0) {
-      c1 = ((int64_t)i * N + j) * HP + k;
+      c1 = row_of(i, j, N, a.xb) * HP + k;
     } else if (i == 0) {
       if (j >= N / 2) continue;
-      c1 = ((int64_t)0 * N + j) * HP;
-      c2 = ((int64_t)0 * N + (N - j)) * HP;
+      c1 = row_of(0, j, N, a.xb) * HP;
+      c2 = row_of(0, N - j, N, a.xb) * HP;
     } else {
       if (i >= N / 2) continue;
       int ii = N - i, jj = (N - j) % N;
-      c1 = ((int64_t)i * N + j) * HP;
-      c2 = ((int64_t)ii * N + jj) * HP;
+      c1 = row_of(i, j, N, a.xb) * HP;
+      c2 = row_of(ii, jj, N, a.xb) * HP;
     }
     if (FP64) {
       double2* o = (double2*)out;
@@ -190,15 +194,17 @@ __global__ void k_noise(NoiseArgs a, const uint32_t* __restrict__ seedtable, voi
   }
 }
 
-static NoiseArgs noise_args(Plan* p) {
+static NoiseArgs noise_args(Plan* p, int xb) {
   NoiseArgs a;
   a.g = p->grid;
+  a.xb = xb;
   a.phase_flip = p->prm.phase_flip == 1;
   a.fixed_amp = p->prm.fixed_amplitude != 0;
   a.anorm = p->Anorm;
   a.ns = p->prm.primordial_index;
   a.fac = pow(2 * kPi / p->prm.box, 1.5);
   a.beta = p->Beta;
+  a.prm = p->prm;
   a.amp = p->d_amp;
   return a;
 }
@@ -209,7 +215,7 @@ int launch_noise_fp32(Plan* p, const uint32_t* d_seed, float2* d_phik, cudaStrea
   int64_t cols = (int64_t)p->N * p->N;
   int bs = 128;
   { ProfScope ps_(p, "noise", st);
-  k_noise<false><<<(unsigned)((cols + bs - 1) / bs), bs, 0, st>>>(noise_args(p), d_seed, d_phik, p->HP);
+  k_noise<false><<<(unsigned)((cols + bs - 1) / bs), bs, 0, st>>>(noise_args(p, kXB), d_seed, d_phik, p->HP);
   }
   AAR_CUDA_TRY(p, cudaGetLastError());
   p->last_launches += 1;
@@ -222,7 +228,7 @@ int launch_noise_fp64(Plan* p, const uint32_t* d_seed, double2* d_phik, int hp, 
   int64_t cols = (int64_t)p->N * p->N;
   int bs = 128;
   { ProfScope ps_(p, "noise", st);
-  k_noise<true><<<(unsigned)((cols + bs - 1) / bs), bs, 0, st>>>(noise_args(p), d_seed, d_phik, hp);
+  k_noise<true><<<(unsigned)((cols + bs - 1) / bs), bs, 0, st>>>(noise_args(p, 1), d_seed, d_phik, hp);
   }
   AAR_CUDA_TRY(p, cudaGetLastError());
   p->last_launches += 1;
@@ -284,9 +290,9 @@ int noalloc_gaussian(Plan* p, void* d_out, cudaStream_t st) {
   AAR_CUDA_TRY(p, cudaMemsetAsync(d_out, 0, (fp64 ? sizeof(double2) : sizeof(float2)) * (size_t)total * hp, st));
   const unsigned nb = (unsigned)((total + 127) / 128);
   if (fp64)
-    k_noise<true><<<nb, 128, 0, st>>>(noise_args(p), seed, d_out, hp);
+    k_noise<true><<<nb, 128, 0, st>>>(noise_args(p, 1), seed, d_out, hp);
   else
-    k_noise<false><<<nb, 128, 0, st>>>(noise_args(p), seed, d_out, hp);
+    k_noise<false><<<nb, 128, 0, st>>>(noise_args(p, 1), seed, d_out, hp);
   AAR_CUDA_TRY(p, cudaGetLastError());
   p->last_launches = 2;
   return AAR_OK;

@@ -85,7 +85,21 @@ struct AxisOp {
   }
 };
 
-// First modal pass: item = tile * M + p; phi tile times q_p(n^2) (zero on
+// Item order of the x passes that write several output fields from one
+// input tile: groups of `grp` consecutive tiles, and within a group all
+// tiles of output 0, then all of output 1, ...  The blocks resident at one
+// time then write into a few fields instead of all of them (each tile of an
+// x pass touches one address per x row, N rows 4 MB apart at N = 1024), and
+// the group's input tiles stay in L2 while its outputs are produced.
+__device__ __forceinline__ void group_order(int64_t item, int64_t tiles, int nc, int64_t grp, int64_t& t, int& c) {
+  const int64_t span = grp * nc;
+  const int64_t g = item / span, r = item - g * span;
+  const int64_t gs = min(grp, tiles - g * grp);  // the last group may be short
+  c = (int)(r / gs);
+  t = g * grp + (r - (int64_t)c * gs);
+}
+
+// First modal pass: item = (tile group, p, tile) (group_order); phi tile times q_p(n^2) (zero on
 // the cut, DC and padding columns), inverse x FFT, into field p.
 template <int N, int W>
 struct XinvOp {
@@ -95,9 +109,10 @@ struct XinvOp {
   int64_t fs, tiles, nsq;
   int HP;
   const float* qtab;
+  int64_t grp;
   __device__ void coords(int64_t item, int& o, int& c0, int& p) const {
-    int64_t t = item / a.M;
-    p = (int)(item % a.M);
+    int64_t t;
+    group_order(item, tiles, a.M, grp, t, p);
     int ncol = HP / W;
     o = (int)(t / ncol);
     c0 = (int)(t % ncol) * W;
@@ -139,9 +154,8 @@ struct XinvOp {
   }
 };
 
-// 2LPT passes (MODE 0: Hessians, items tile * 6 + comp; MODE 1: ZA
-// displacements, items tile * 3 + a; MODE 2: 2LPT displacements, items
-// tile * 3 + a): the factor lpt_factor<MODE> (main.c:1180-1368) on
+// 2LPT passes (MODE 0: Hessians, 6 components; MODE 1: ZA displacements,
+// 3; MODE 2: 2LPT displacements, 3; items in group_order): the factor lpt_factor<MODE> (main.c:1180-1368) on
 // T/(D Beta) phi (MODE 0, 1: `phi` points at that product, made once by
 // k_scale_twb, so the per-|k|^2 table is not gathered nine times), or for
 // MODE 2 on the source slot already transformed along x; then the inverse x
@@ -154,10 +168,11 @@ struct LptOp {
   float2* work;
   int64_t fs, tiles;
   int HP, src_slot;
+  int64_t grp;
   static constexpr int NC = MODE == 0 ? 6 : 3;
   __device__ void coords(int64_t item, int& o, int& c0, int& comp) const {
-    int64_t t = item / NC;
-    comp = (int)(item % NC);
+    int64_t t;
+    group_order(item, tiles, NC, grp, t, comp);
     int ncol = HP / W;
     o = (int)(t / ncol);
     c0 = (int)(t % ncol) * W;

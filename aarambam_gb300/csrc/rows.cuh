@@ -19,8 +19,10 @@ __device__ __forceinline__ void cp_async_wait() {
 }
 
 
-// Row layout: complex row X[0..N/2] at field + (x N + y) HP; the real row
-// x[0..N-1] occupies the same bytes (float2 z_n = (x_{2n}, x_{2n+1})).
+// Row layout: complex row X[0..N/2] at field + m HP, m the row's memory
+// index (the plan's row order maps (x, y) to m); the real row x[0..N-1]
+// occupies the same bytes (float2 z_n = (x_{2n}, x_{2n+1})).  The row steps
+// are the same for every row, so the kernels run over memory rows.
 template <int N>
 struct RowCfg {
   static constexpr int H = N / 2;             // complex FFT length
@@ -107,7 +109,7 @@ __device__ __forceinline__ void row_r2c_post(const float2* line, float2* __restr
   }
 }
 
-// Generic row kernel.  For each row (blockIdx.x = x*N + y): c2r of `nin`
+// Generic row kernel.  For each memory row (blockIdx.x): c2r of `nin`
 // input fields (slots in_slot[]), a per-position combine step Op, r2c of
 // `nout` output lines into slots out_slot[].  One warp per line at a time.
 // THREADS = 256 with two resident blocks per SM: while one block waits at a

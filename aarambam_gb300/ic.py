@@ -19,6 +19,9 @@ from ._lib import AarError, check
 
 
 def params_from_config(cfg: dict, precision: int = _lib.AAR_FUSED_FP32, mem_limit_bytes: int = 0) -> _lib.Params:
+    """C-ABI parameters of a parameter-file dict; a dict with the A_res /
+    w_res / phi_res tags is a 2LPTResBasis set."""
+    res = "A_res" in cfg
     return _lib.Params(
         nmesh=cfg["Nmesh"], nsample=cfg["Nsample"], nmax=cfg["Nmax"], seed=cfg["Seed"], box=cfg["Box"],
         omega=cfg["Omega"], omega_lambda=cfg["OmegaLambda"], hubble_param=cfg["HubbleParam"],
@@ -27,7 +30,10 @@ def params_from_config(cfg: dict, precision: int = _lib.AAR_FUSED_FP32, mem_limi
         unit_velocity_in_cm_per_s=cfg["UnitVelocity_in_cm_per_s"],
         input_spectrum_unit_length_in_cm=cfg["InputSpectrum_UnitLength_in_cm"],
         fixed_amplitude=cfg["FixedAmplitude"], phase_flip=cfg["PhaseFlip"], sphere_mode=cfg["SphereMode"],
-        precision=precision, mem_limit_bytes=mem_limit_bytes)
+        precision=precision, mem_limit_bytes=mem_limit_bytes,
+        variant=_lib.AAR_VARIANT_RESBASIS if res else _lib.AAR_VARIANT_BASIS,
+        which_spectrum=cfg.get("WhichSpectrum", 0), a_res=cfg.get("A_res", 0.0), w_res=cfg.get("w_res", 0.0),
+        phi_res=cfg.get("phi_res", 0.0))
 
 
 def _ptr(t: torch.Tensor) -> int:

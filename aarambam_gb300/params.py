@@ -30,6 +30,12 @@ TAGS = [
 ]
 TAG_TYPES = dict(TAGS)
 
+# 2LPTResBasis adds the P(k) oscillation after SavePotentialField
+# (Aarambam/LPT/ResBasis/read_param.c:88-99)
+_at = [t for t, _ in TAGS].index("SavePotentialField") + 1
+TAGS_RESBASIS = TAGS[:_at] + [("A_res", FLOAT), ("w_res", FLOAT), ("phi_res", FLOAT)] + TAGS[_at:]
+TAG_TABLES = {"basis": TAGS, "resbasis": TAGS_RESBASIS}
+
 _FLOAT_PREFIX = re.compile(r"^\s*[+-]?((\d+\.?\d*)|(\.\d+))([eE][+-]?\d+)?")
 _INT_PREFIX = re.compile(r"^\s*[+-]?\d+")
 
@@ -62,9 +68,12 @@ def c_atoi(s: str) -> int:
     return (v + 2**31) % 2**32 - 2**31
 
 
-def parse_parameter_text(text: str, fname: str = "<text>") -> dict:
-    """Parse parameter-file text.  Returns {tag: value}; raises ParameterError."""
-    remaining = {t for t, _ in TAGS}
+def parse_parameter_text(text: str, fname: str = "<text>", variant: str = "basis") -> dict:
+    """Parse parameter-file text with the tag table of `variant` ("basis" or
+    "resbasis").  Returns {tag: value}; raises ParameterError."""
+    tags = TAG_TABLES[variant]
+    types = dict(tags)
+    remaining = {t for t, _ in tags}
     values: dict = {}
     errors = []
     # fgets(buf, 200, fd): a physical line longer than 199 characters is read in
@@ -84,11 +93,11 @@ def parse_parameter_text(text: str, fname: str = "<text>") -> dict:
             continue
         if tag in remaining:
             remaining.discard(tag)
-            kind = TAG_TYPES[tag]
+            kind = types[tag]
             values[tag] = c_atof(val) if kind == FLOAT else c_atoi(val) if kind == INT else val
         else:
             errors.append(f"Error in file {fname}:   Tag '{tag}' not allowed or multiple defined.")
-    for tag, _ in TAGS:
+    for tag, _ in tags:
         if tag in remaining:
             errors.append(f"Error. I miss a value for tag '{tag}' in parameter file '{fname}'.")
     if errors:
@@ -96,11 +105,11 @@ def parse_parameter_text(text: str, fname: str = "<text>") -> dict:
     return values
 
 
-def read_parameterfile(fname: str) -> dict:
+def read_parameterfile(fname: str, variant: str = "basis") -> dict:
     """Read a 2LPT parameter file (read_param.c:8-262)."""
     try:
         with open(fname, "r", errors="surrogateescape") as f:
             text = f.read()
     except OSError:
         raise ParameterError([f"Parameter file {fname} not found."]) from None
-    return parse_parameter_text(text, fname)
+    return parse_parameter_text(text, fname, variant)

@@ -1,13 +1,15 @@
 """Configuration and post-processing helpers with the reference's interface
-(Aarambam/utils.py): make_config_basis / make_example_config_basis build the
-2LPT parameter file text, collate_potential gathers the potential dumps,
-camb2input converts a CAMB transfer file.
+(Aarambam/utils.py): make_config_basis / make_config_resbasis and their
+make_example_config_* build the 2LPT parameter file text, collate_potential
+gathers the potential dumps, camb2input converts a CAMB transfer file.
 
 Differences, deliberately: the default OutputDir comes from TMPDIR when set
 and the system temporary directory otherwise (the reference raises KeyError
 at import without TMPDIR, utils.py:61), and collate_potential also accepts the
 single-file dumps a one-process run writes (`Gauss_potential_<Seed>`, whose
-name the reference's collate mistakes for a slab size, utils.py:327).
+name the reference's collate mistakes for a slab size, utils.py:327), and
+DEFAULT_RESBASIS_INPUTS carries Pk_mode = 1 (the reference's lacks the key,
+so its make_example_config_resbasis raises TypeError).
 """
 from __future__ import annotations
 
@@ -89,6 +91,32 @@ def make_config_basis(Nmesh, Nsample, Nmax, Lbox, FileBase, OutputDir, GlassFile
 
 def make_example_config_basis():
     return make_config_basis(**DEFAULT_BASIS_INPUTS)
+
+
+# 2LPTResBasis: the Basis file with WhichSpectrum = Pk_mode and the three
+# oscillation tags (utils.py:71-84)
+DEFAULT_RESBASIS_CONFIG = (DEFAULT_BASIS_CONFIG + """
+A_res               %(Pk_A_res)f
+w_res               %(Pk_w_res)f
+phi_res             %(Pk_phi_res)f
+""").replace("0 #Fixed to 0 because we always want to use only the Transfer Function", "%(Pk_mode)d")
+
+DEFAULT_RESBASIS_INPUTS = dict(DEFAULT_BASIS_INPUTS, Pk_A_res=0.9, Pk_w_res=2, Pk_phi_res=0.0, Pk_mode=1)
+
+
+def make_config_resbasis(Nmesh, Nsample, Nmax, Lbox, FileBase, OutputDir, GlassFile, GlassTileFac, seed, Om, Ode,
+                         h, sigma8, n_s, z_ini, Fnl, N_modes, TransferPath, AlphaPath, AiPath, SavePotentialField,
+                         NWriteoutProcesses, Pk_A_res, Pk_w_res, Pk_phi_res, Pk_mode):
+    """The 2LPTResBasis parameter-file text (utils.py:172-271).  Pk_mode is
+    WhichSpectrum: the executable applies (1 + A cos(w k + phi)) and
+    (1 + A cos(w ln k + phi)) for modes 0 and 1 and the log one only for 2
+    (its switch has no break, ResBasis/main.c:445-455)."""
+    SavePotentialField = int(SavePotentialField)
+    return DEFAULT_RESBASIS_CONFIG % locals()
+
+
+def make_example_config_resbasis():
+    return make_config_resbasis(**DEFAULT_RESBASIS_INPUTS)
 
 
 def camb2input(path):

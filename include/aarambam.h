@@ -40,6 +40,11 @@ extern "C" {
 #define AAR_FUSED_FP32 0  /* own FFTs, fused filters/products/accumulation, FP32 */
 #define AAR_PLAIN_FP64 1  /* cuFFT Z2D/D2Z + separate pointwise kernels, FP64 */
 
+/* Which executable's power spectrum the plan follows. */
+#define AAR_VARIANT_BASIS 0    /* 2LPTBasis: P(k) = Norm k^ns T^2 (LPT/Basis/power.c:240-265) */
+#define AAR_VARIANT_RESBASIS 1 /* 2LPTResBasis: P(k) with the oscillation A_res, w_res, phi_res
+                                  (LPT/ResBasis/power.c:240-260, main.c:445-455) */
+
 /* The parameter-file values the path uses (read_param.c:25-184). */
 typedef struct aar_params {
   int32_t nmesh, nsample, nmax, seed;
@@ -50,6 +55,9 @@ typedef struct aar_params {
   int32_t fixed_amplitude, phase_flip, sphere_mode;
   int32_t precision;        /* AAR_FUSED_FP32 or AAR_PLAIN_FP64 */
   int64_t mem_limit_bytes;  /* refuse plan allocations beyond this (0 = no cap) */
+  int32_t variant;          /* AAR_VARIANT_BASIS or AAR_VARIANT_RESBASIS */
+  int32_t which_spectrum;   /* WhichSpectrum: 0 for Basis; 0, 1 or 2 for ResBasis */
+  double a_res, w_res, phi_res; /* ResBasis oscillation (ResBasis/read_param.c:88-99) */
 } aar_params;
 
 /* Host scalars of the set-up: power.c:391-448 (Norm = sigma8 normalisation,

@@ -163,14 +163,26 @@ typedef struct {
   double R;
 } orc_sig_ctx;
 
-/* power.c:562-576 with PowerSpec case 0 (power.c:246-248) */
+/* PowerSpec (Basis/power.c:240-265 case 0; ResBasis/power.c:240-260, one
+   case per WhichSpectrum, T^2 applied after the switch) */
+static double orc_powerspec(const orc_params *p, double k) {
+  double power = p->Norm * exp(p->ns * log(k));
+  if (p->ResBasis && p->WhichSpectrum == 1)
+    power = p->Norm * exp(p->ns * log(k)) * (1 + p->A_res * cos(p->w_res * k + p->phi_res));
+  if (p->ResBasis && p->WhichSpectrum == 2)
+    power = p->Norm * exp(p->ns * log(k)) * (1 + p->A_res * cos(p->w_res * log(k) + p->phi_res));
+  double T = orc_transfer(p, k);
+  power *= T * T;
+  return power;
+}
+
+/* power.c:562-576 */
 static double orc_sigma2_int(double k, const void *vctx) {
   const orc_sig_ctx *c = (const orc_sig_ctx *)vctx;
   double kr = c->R * k, kr2 = kr * kr, kr3 = kr2 * kr;
   if (kr < 1e-8) return 0;
   double w = 3 * (sin(kr) / kr3 - cos(kr) / kr2);
-  double T = orc_transfer(c->p, k);
-  double P = c->p->Norm * exp(c->p->ns * log(k)) * T * T;
+  double P = orc_powerspec(c->p, k);
   return 4 * ORC_PI * k * k * w * w * P;
 }
 
@@ -516,6 +528,19 @@ void orc_gauss_potential(const orc_params *p, const uint32_t *seedtable, double 
       double k2 = kx * kx + ky * ky + kz * kz, km = sqrt(k2);
       if (orc_cut(p, kx, ky, kz, km)) continue;
       double phig = p->Anorm * exp(p->ns * log(km));
+      if (p->ResBasis) {
+        /* ResBasis/main.c:445-455: the switch has no break statements */
+        switch (p->WhichSpectrum) {
+          case 0:
+            phig *= 1.0;
+            /* fall through */
+          case 1:
+            phig *= (1.0 + p->A_res * cos(p->w_res * km + p->phi_res));
+            /* fall through */
+          case 2:
+            phig *= (1.0 + p->A_res * cos(p->w_res * log(km) + p->phi_res));
+        }
+      }
       if (!p->FixedAmplitude) phig *= -log(ampl);
       phig = sqrt(phig) * fac * p->Beta / k2;
       double re = phig * cos(phase), im = phig * sin(phase);

@@ -54,6 +54,10 @@ typedef struct {
   double kconv; /* InputSpectrum_UnitLength_in_cm / UnitLength_in_cm */
   int ntrans;
   double *logk, *logT; /* sorted, logT normalised to the first entry */
+  /* 2LPTResBasis (LPT/ResBasis): ResBasis = 1 adds the oscillation
+     A_res, w_res, phi_res selected by WhichSpectrum; 0 = 2LPTBasis */
+  int ResBasis, WhichSpectrum;
+  double A_res, w_res, phi_res;
 } orc_params;
 
 /* Returns 0 on success, nonzero error code on a bad transfer table. */

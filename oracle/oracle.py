@@ -35,7 +35,9 @@ class Params(C.Structure):
                 ("FixedAmplitude", C.c_int), ("PhaseFlip", C.c_int), ("SphereMode", C.c_int)] + \
                [(n, C.c_double) for n in ("Norm", "Anorm", "D0", "Dplus", "InitTime", "Hubble", "Beta",
                                           "vel_prefac", "vel_prefac2", "kconv")] + \
-               [("ntrans", C.c_int), ("logk", C.POINTER(C.c_double)), ("logT", C.POINTER(C.c_double))]
+               [("ntrans", C.c_int), ("logk", C.POINTER(C.c_double)), ("logT", C.POINTER(C.c_double))] + \
+               [("ResBasis", C.c_int), ("WhichSpectrum", C.c_int)] + \
+               [(n, C.c_double) for n in ("A_res", "w_res", "phi_res")]
 
 
 class Rlx(C.Structure):
@@ -100,6 +102,9 @@ class Oracle:
         p = Params(N=cfg["Nmesh"], Nsample=cfg["Nsample"], Nmax=cfg["Nmax"], Seed=cfg["Seed"], Box=cfg["Box"],
                    ns=cfg["PrimordialIndex"], Fnl=cfg["Fnl"], FixedAmplitude=cfg["FixedAmplitude"],
                    PhaseFlip=cfg["PhaseFlip"], SphereMode=cfg["SphereMode"])
+        if "A_res" in cfg:  # a 2LPTResBasis parameter set
+            p.ResBasis, p.WhichSpectrum = 1, cfg["WhichSpectrum"]
+            p.A_res, p.w_res, p.phi_res = cfg["A_res"], cfg["w_res"], cfg["phi_res"]
         rc = lib().orc_setup(C.byref(p), C.byref(c), len(k), np.ascontiguousarray(k, np.float64),
                              np.ascontiguousarray(T, np.float64))
         if rc != 0:

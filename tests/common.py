@@ -10,6 +10,8 @@ from aarambam_gb300 import gadget, tables
 HERE = os.path.dirname(os.path.abspath(__file__))
 GOLDEN = os.path.join(HERE, "golden")
 CASES = ["local_n32", "scalarI_n32_flip_fixed_cut", "scalarI12_n16_sphere", "local_n24"]
+# 2LPTResBasis outputs (oscillating P(k)): WhichSpectrum 1, 2 and 0
+RES_CASES = ["res_lin_n32", "res_log_n32", "res_both_n16"]
 
 BASE_CFG = dict(Omega=0.3, OmegaLambda=0.7, OmegaBaryon=0.0, OmegaDM_2ndSpecies=0.0, HubbleParam=0.7,
                 ShapeGamma=0.0, Sigma8=0.8, PrimordialIndex=0.965, Redshift=49.0, FixedAmplitude=0, PhaseFlip=0,

@@ -1,9 +1,10 @@
 """Golden outputs of the reference 2LPT code itself, at small grids.
 
-Builds the reference's own Aarambam/LPT/Basis sources (compiled where they lie
-in the reference checkout, against the single-process MPI / GSL-rng /
-FFTW2 stand-ins in oracle/shim, recipe `make -C oracle ref`), runs the
-resulting executable on a few small configurations and stores what it
+Builds the reference's own Aarambam/LPT/Basis and LPT/ResBasis sources
+(compiled where they lie in the reference checkout, against the
+single-process MPI / GSL-rng / FFTW2 stand-ins in oracle/shim, recipe
+`make -C oracle ref`), runs the resulting executables on a few small
+configurations and stores what they
 writes -- the Gaussian and non-Gaussian potential dumps (write_phi) and the
 Gadget snapshot -- as compressed .npz fixtures under tests/golden/ref/.
 
@@ -28,7 +29,6 @@ sys.path.insert(0, ROOT)
 from aarambam_gb300 import gadget, tables  # noqa: E402
 
 OUT = os.path.join(HERE, "ref")
-REF_BIN = os.path.join(ROOT, "oracle", "_ref", "2LPTBasis")
 
 BASE = dict(Omega=0.3, OmegaLambda=0.7, OmegaBaryon=0.0, OmegaDM_2ndSpecies=0.0, HubbleParam=0.7,
             ShapeGamma=0.0, Sigma8=0.8, PrimordialIndex=0.965, Redshift=49.0, FixedAmplitude=0, PhaseFlip=0,
@@ -49,6 +49,16 @@ CASES = {
                                  SphereMode=1, table="scalarI_m12_L1000_n512", glass=(16, 1)),
     "local_n24": dict(Nmesh=24, Nsample=24, Nmax=128, Box=500.0, Seed=99, Fnl=-50.0, N_modes=8,
                       table="local_m8_L500_n128", glass=(12, 2)),
+    # 2LPTResBasis (oscillating P(k)), one case per WhichSpectrum
+    "res_lin_n32": dict(exe="2LPTResBasis", Nmesh=32, Nsample=32, Nmax=128, Box=500.0, Seed=31, Fnl=10.0,
+                        N_modes=8, WhichSpectrum=1, A_res=0.5, w_res=30.0, phi_res=0.3,
+                        table="local_m8_L500_n128", glass=(16, 2)),
+    "res_log_n32": dict(exe="2LPTResBasis", Nmesh=32, Nsample=28, Nmax=256, Box=500.0, Seed=32, Fnl=100.0,
+                        N_modes=10, WhichSpectrum=2, A_res=0.3, w_res=10.0, phi_res=0.0, PhaseFlip=1,
+                        table="scalarI_m10_L500_n256", glass=(8, 4)),
+    "res_both_n16": dict(exe="2LPTResBasis", Nmesh=16, Nsample=16, Nmax=512, Box=1000.0, Seed=33, Fnl=100.0,
+                         N_modes=12, WhichSpectrum=0, A_res=0.9, w_res=2.0, phi_res=0.0, SphereMode=1,
+                         table="scalarI_m12_L1000_n512", glass=(16, 1)),
 }
 
 
@@ -67,13 +77,14 @@ def run_case(name, spec, tmp):
     gadget.write_glass(os.path.join(d, "glass.dat"), gadget.lattice_glass(gn, 100.0), 100.0)
     tdir = os.path.join(HERE, "tables", spec["table"])
     cfg = dict(BASE)
-    cfg.update({kk: vv for kk, vv in spec.items() if kk not in ("table", "glass")})
+    cfg.update({kk: vv for kk, vv in spec.items() if kk not in ("table", "glass", "exe")})
     cfg.update(GlassFile=os.path.join(d, "glass.dat"), GlassTileFac=tile, OutputDir=d,
                FileWithInputTransfer=os.path.join(d, "T.dat"),
                FileWithAlphaCoeff=os.path.join(tdir, "AlphaTable.dat"),
                FileWithX0Coeff=os.path.join(tdir, "AiTable.dat"))
     write_config(os.path.join(d, "cfg"), cfg)
-    res = subprocess.run([REF_BIN, os.path.join(d, "cfg")], capture_output=True, text=True, cwd=d)
+    exe = os.path.join(ROOT, "oracle", "_ref", spec.get("exe", "2LPTBasis"))
+    res = subprocess.run([exe, os.path.join(d, "cfg")], capture_output=True, text=True, cwd=d)
     if res.returncode != 0:
         raise RuntimeError(res.stdout + res.stderr)
     seed = cfg["Seed"]

@@ -3,7 +3,7 @@ import numpy as np
 import pytest
 
 from oracle import oracle as O
-from tests.common import CASES, bbks, lattice_lagrangian, load_case, rel_rms, table
+from tests.common import CASES, RES_CASES, bbks, lattice_lagrangian, load_case, rel_rms, table
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -69,7 +69,7 @@ def test_seedtable_first_values():
         assert st[i, j] == int(0x7FFFFFFF * u[d])
 
 
-@pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("name", CASES + RES_CASES)
 def test_oracle_reproduces_reference_outputs(name):
     """Oracle vs the reference's own main.c/power.c/read_glass.c built on the
     single-process stand-ins (tests/golden/make_ref_fixtures.py)."""
@@ -102,3 +102,21 @@ def test_oracle_rejects_short_transfer_table():
     k = np.logspace(-3, 2, 50)
     with pytest.raises(RuntimeError, match="1111"):
         O.Oracle(cfg, k, np.ones_like(k))
+
+
+@pytest.mark.parametrize("name", RES_CASES)
+def test_resbasis_normalisation_and_oscillation(name):
+    """ResBasis: sigma8 normalisation with the oscillating PowerSpec (the
+    reference prints Normfac), and the fixtures do depend on the oscillation:
+    the same run without it misses the reference's Gaussian potential."""
+    cfg, z = load_case(name)
+    k, t = bbks()
+    s = O.Oracle(cfg, k, t).scalars
+    normfac = float(str(z["stdout"]).split("Normfac=")[1].split(")")[0])
+    assert abs(s["Norm"] / normfac - 1) < 1e-5
+    plain = {kk: v for kk, v in cfg.items() if kk not in ("A_res", "w_res", "phi_res")}
+    plain["WhichSpectrum"] = 0
+    o = O.Oracle(plain, k, t)
+    alpha, x0 = table(cfg["table"], cfg["N_modes"])
+    r = o.run(alpha, x0, lattice_lagrangian(o, cfg["glass_n"], cfg["GlassTileFac"]))
+    assert rel_rms(r["pot_gauss"], z["pot_gauss"]) > 1e-2

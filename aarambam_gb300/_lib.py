@@ -31,6 +31,8 @@ EXPORTS = [
     "aar_last_error", "aar_plan_destroy", "aar_version",
     "aar_batch_create", "aar_batch_run", "aar_batch_launch_count", "aar_batch_last_error", "aar_batch_destroy",
     "aar_set_spectrum", "aar_adj_spectral", "aar_adj_source", "aar_adj_products", "aar_set_jit", "aar_jit_status",
+    "aar_tetra_covariance_scratch_bytes", "aar_tetra_covariance", "aar_tetra_QS", "aar_tetra_residual",
+    "aar_bordered_cond",
 ]
 AAR_ADJ_OP_ONE, AAR_ADJ_OP_GAUSS, AAR_ADJ_OP_Q, AAR_ADJ_OP_RHO = 0, 1, 2, 3
 AAR_ADJ_OP_HESS, AAR_ADJ_OP_PSI1, AAR_ADJ_OP_PSI2 = 4, 5, 6
@@ -114,6 +116,14 @@ def load(build_if_missing: bool = False):
     L.aar_adj_spectral.argtypes = [vp, i32, i32, i32, vp, vp, i32, vp]
     L.aar_adj_source.argtypes = [vp, vp, vp, vp, vp]
     L.aar_adj_products.argtypes = [vp, vp, vp, vp, vp, vp]
+    # Decomposer (device pointers; tetrapyd arguments as tetrapyd.c's)
+    tetra = [vp, vp, vp, vp, i32, vp, vp, vp, i32, vp, i32, i32]
+    L.aar_tetra_covariance_scratch_bytes.argtypes = [i32, i32]
+    L.aar_tetra_covariance_scratch_bytes.restype = C.c_size_t
+    L.aar_tetra_covariance.argtypes = [vp] + tetra + [vp, C.c_size_t, vp]
+    L.aar_tetra_QS.argtypes = [vp, vp, i32] + tetra + [vp]
+    L.aar_tetra_residual.argtypes = [vp, vp, vp, vp, i32] + tetra + [vp]
+    L.aar_bordered_cond.argtypes = [vp, vp, i32, vp, vp, i32, vp]
     L.aar_last_error.argtypes = [vp]
     L.aar_last_error.restype = C.c_char_p
     L.aar_plan_destroy.argtypes = [vp]

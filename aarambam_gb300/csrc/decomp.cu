@@ -132,7 +132,7 @@ __global__ void k_gram_reduce(const double* __restrict__ part, int nslices, int 
   const int64_t nm = nmodes;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nm * nm; e += (int64_t)gridDim.x * blockDim.x) {
     const int n = (int)(e / nm), m = (int)(e % nm);
-    if ((n / kGT) > (m / kGT)) continue;  // lower tiles are mirrors
+    if (n > m) continue;  // the lower triangle is the mirror
     double s = 0.0;
     for (int k = 0; k < nslices; ++k) s += part[(int64_t)k * nm * nm + e];
     qq[e] = s;

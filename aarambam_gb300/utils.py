@@ -1,7 +1,8 @@
 """Configuration and post-processing helpers with the reference's interface
 (Aarambam/utils.py): make_config_basis / make_config_resbasis and their
 make_example_config_* build the 2LPT parameter file text, collate_potential
-gathers the potential dumps, camb2input converts a CAMB transfer file.
+gathers the potential dumps, camb2input converts a CAMB transfer file, and
+Decomposer runs the modal decomposition that writes the coefficient tables.
 
 Differences, deliberately: the default OutputDir comes from TMPDIR when set
 and the system temporary directory otherwise (the reference raises KeyError
@@ -152,15 +153,27 @@ def collate_potential(OutputDir):
 
 
 class Decomposer:
-    """Placeholder of the reference's modal Decomposer interface
-    (utils.py:349-446).  The decomposition itself (cmbbest, OMP with CG) is
-    not part of this package; coefficient tables come from the reference
-    Decomposer and are read with aarambam_gb300.tables."""
+    """Bispectrum modal decomposition driver (utils.py:349-446): combines a
+    model mix-in (models.py, or any class with `bispectrum` /
+    `raw_bispectrum` reading self.args, e.g. the reference's own
+    Aarambam.models classes) with a basis class (default
+    basis.BasicBasisDecompose, whose dense FP64 work runs on the GPU), runs
+    it and, with `outdir`, writes AlphaTable.dat / AiTable.dat there."""
 
     def __init__(self, N_modes, n_s, Lbox, Nmax, ModeTol, MaxModeCount, **kwargs):
-        self.args = dict(N_modes=N_modes, n_s=n_s, Lbox=Lbox, Nmax=Nmax, ModeTol=ModeTol,
-                         MaxModeCount=MaxModeCount, **kwargs)
+        args = dict(N_modes=N_modes, n_s=n_s, Lbox=Lbox, Nmax=Nmax, ModeTol=ModeTol, MaxModeCount=MaxModeCount)
+        args.update(**kwargs)
+        self.args = args
 
-    def go(self, Model, Basis, outdir=None, **kwargs):
-        raise NotImplementedError("the modal decomposition runs in the reference Decomposer; "
-                                  "pass its AlphaTable.dat / AiTable.dat to the 2LPT step")
+    def go(self, Model, Basis=None, outdir=None, **kwargs):
+        if Basis is None:
+            from .basis import BasicBasisDecompose as Basis
+        inpars = self.args.copy()
+        inpars.update(**kwargs)
+        decomp = type("C", (Model, Basis), {})
+        instan = decomp(**inpars)
+        result = instan.go()
+        if outdir is not None:
+            assert os.path.exists(outdir), f"Path {outdir} does not exist"
+            instan.finalize(result, directory=outdir)
+        return result

@@ -21,6 +21,7 @@
 #ifndef AARAMBAM_H
 #define AARAMBAM_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -160,6 +161,48 @@ int aar_gaussian_spectrum_noalloc(aar_plan* plan, void* d_out, void* stream);
    data float32 [N][N][N].  The plan's first work field is used as scratch. */
 int aar_c2r(aar_plan* plan, const void* d_in, float* d_out, void* stream);
 int aar_r2c(aar_plan* plan, const float* d_in, void* d_out, void* stream);
+
+/* ---- modal decomposition (the Decomposer's dense FP64 work) ----
+   Stateless entry points on device pointers, with the arguments of the
+   reference's C kernels (Aarambam/basis/tetrapyd.h, bound from
+   cmbbest.pyx:35-47): tetrapyd points (weights, i1 >= i2 >= i3 indices into
+   the 1D k grid), 3D mode indices p1 >= p2 >= p3, and the 1D mode functions
+   mode_evals[mode_p_max][k_npts] (mode_p_max * k_npts * 8 <= 160 KiB).
+   Q_n(t) is the symmetrised product of tetrapyd.c:136-152.  Return AAR_OK,
+   AAR_ERR_ARG or AAR_ERR_CUDA. */
+
+/* Scratch bytes aar_tetra_covariance needs (per-slice partial sums). */
+size_t aar_tetra_covariance_scratch_bytes(int32_t tetra_npts, int32_t n_modes);
+
+/* cov[n][m] = sum_t w_t Q_n(t) Q_m(t), [n_modes][n_modes], symmetric.
+   Replaces compute_mode_bispectra_covariance (tetrapyd.c:107-236). */
+int aar_tetra_covariance(double* d_cov, const double* d_tetra_weights, const int32_t* d_i1, const int32_t* d_i2,
+                         const int32_t* d_i3, int32_t tetra_npts, const int32_t* d_p1, const int32_t* d_p2,
+                         const int32_t* d_p3, int32_t n_modes, const double* d_mode_evals, int32_t mode_p_max,
+                         int32_t k_npts, void* d_scratch, size_t scratch_bytes, void* stream);
+
+/* QS[s][n] = sum_t S[s][t] w_t Q_n(t), S [n_shapes][tetra_npts].
+   Replaces compute_QS (tetrapyd.c:238-305). */
+int aar_tetra_QS(double* d_QS, const double* d_S, int32_t n_shapes, const double* d_tetra_weights,
+                 const int32_t* d_i1, const int32_t* d_i2, const int32_t* d_i3, int32_t tetra_npts,
+                 const int32_t* d_p1, const int32_t* d_p2, const int32_t* d_p3, int32_t n_modes,
+                 const double* d_mode_evals, int32_t mode_p_max, int32_t k_npts, void* stream);
+
+/* R[t] = S[t] - sum_j coef[j] Q_{sel[j]}(t), j ascending: the matching-
+   pursuit residual (cmbbest.pyx:433) without storing Q. */
+int aar_tetra_residual(double* d_R, const double* d_S, const int32_t* d_sel, const double* d_coef, int32_t n_sel,
+                       const double* d_tetra_weights, const int32_t* d_i1, const int32_t* d_i2, const int32_t* d_i3,
+                       int32_t tetra_npts, const int32_t* d_p1, const int32_t* d_p2, const int32_t* d_p3,
+                       int32_t n_modes, const double* d_mode_evals, int32_t mode_p_max, int32_t k_npts,
+                       void* stream);
+
+/* Condition numbers lambda_max / lambda_min of the bordered symmetric
+   matrices [[A, b_i], [b_i^T, c_i]], i < n_cand, given the eigenvalues lam
+   (ascending, k of them) of the PSD matrix A = V diag(lam) V^T, the rows
+   Z[i] = (V^T b_i)^T [n_cand][k] and c.  Replaces the per-candidate
+   np.linalg.cond of get_cond (cmbbest.pyx:44-47, :443-446). */
+int aar_bordered_cond(double* d_cond, const double* d_lam, int32_t k, const double* d_Z, const double* d_c,
+                      int32_t n_cand, void* stream);
 
 /* ---- adjoint of the fused chain (no counterpart in the reference) ----
    Building blocks of a reverse-mode pass over white noise w -> Gaussian

@@ -71,7 +71,11 @@ def run(name, tmp):
     os.makedirs(outdir, exist_ok=True)
     t0 = time.time()
     dec = Am.utils.Decomposer(N_modes=m, n_s=ns, Lbox=lbox, Nmax=nmax, ModeTol=tol, MaxModeCount=maxc)
-    res = dec.go(getattr(Am.models, model), Am.basis.BasicBasisDecompose, outdir=outdir, **kw)
+    # Aarambam.models exports SingleField and Colliders; the resonance
+    # templates live in Aarambam.models.Resonances
+    import Aarambam.models.Resonances as Res  # noqa: E402
+    cls = getattr(Am.models, model, None) or getattr(Res, model)
+    res = dec.go(cls, Am.basis.BasicBasisDecompose, outdir=outdir, **kw)
     dt = time.time() - t0
     tab = np.loadtxt(os.path.join(outdir, "AlphaTable.dat"))
     meta = dict(model=model, N_modes=m, n_s=ns, Lbox=lbox, Nmax=nmax, ModeTol=tol, MaxModeCount=maxc,

@@ -359,7 +359,7 @@ class BasicBasisDecompose:
 
     def go(self):
         out = {}
-        out.update(self.generate_alpha())
+        out.update(self.generate_alpha(verbose=self.args.get("verbose", True)))
         out.update(self.generate_Ai())
         return out
 

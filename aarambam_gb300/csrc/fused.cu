@@ -139,7 +139,9 @@ __device__ __forceinline__ void tile_fft(float2* sm, const float2* __restrict__ 
 // cut cells keep phi as it is.  A streaming kernel: the R slot reads of a
 // thread are independent, so many are in flight per SM.  (Measured: pairs of
 // cells per thread with 16-byte loads were slower, 36.5 vs 30.8 ms at
-// 1024^3; so was the slot list as a kernel parameter, 39.0 ms.)
+// 1024^3; so was the slot list as a kernel parameter, 39.0 ms, and the rho
+// row read with 16-byte loads into registers and the slots walked with
+// compile-time indices, 38.0 ms.)
 template <int N>
 __global__ void __launch_bounds__(256) k_modal_acc(ModalArgs a, float2* phi, const float2* __restrict__ work,
                                                    int64_t fs, int HP, float fnl_n3, const DevTerms* __restrict__ dt,

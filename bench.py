@@ -52,6 +52,11 @@ BATCH_TEMPLATES = [("local_m6_L500_n256", 6, 10.0), ("equil_m9_L500_n256", 9, 10
                    ("scalarI_m10_L500_n256", 10, 100.0), ("scalarI_m13_L500_n256_mu0p5", 13, 100.0),
                    ("scalarI_m16_L500_n256_mu1p5", 16, 100.0)]
 BATCH_WORKLOADS = {"batch32_n256": (32, 256, 500.0)}
+# modal decompositions (Decomposer.go): model, N_modes, Lbox, Nmax, model keywords, reference table
+DECOMP_WORKLOADS = {
+    "decomp_logres_m20": ("LogResonance", 20, 2000.0, 1536, {"w_res": 10.0, "phi": 0.0}, "logres_w10_m20_L2000_n1536"),
+    "decomp_local_m20": ("Local", 20, 1000.0, 1024, {}, None),
+}
 
 
 def parse():
@@ -60,7 +65,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
-    ap.add_argument("--workload", default="scalarI_m20_n1024", choices=sorted(WORKLOADS) + sorted(BATCH_WORKLOADS))
+    ap.add_argument("--workload", default="scalarI_m20_n1024",
+                    choices=sorted(WORKLOADS) + sorted(BATCH_WORKLOADS) + sorted(DECOMP_WORKLOADS))
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-n", type=int, default=128)
@@ -535,11 +541,52 @@ def batch_arm(args):
         "gpu_launches": b.launches * args.steps, "clocks": clocks, "cpu_baseline": None, "e2e": None}))
 
 
+def decomp_arm(args):
+    """Modal decomposition: seconds per Decomposer.go (covariance build and
+    matching pursuit on the GPU, FP64), next to the reference Decomposer's
+    own time for the same table where it was made (its meta.json, measured on
+    an 8-core x86 host)."""
+    import torch
+    from aarambam_gb300 import _lib, models, utils
+    from aarambam_gb300.basis import BasicBasisDecompose
+    _lib.load(build_if_missing=True)
+    model, M, lbox, nmax, kw, table = DECOMP_WORKLOADS[args.workload]
+    torch.cuda.set_device(0)
+    dec = utils.Decomposer(M, 0.965, lbox, nmax, 1e-4, 150)
+    times, out, inst = [], None, None
+    for i in range(max(1, args.warmup) + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        inst = type("C", (getattr(models, model), BasicBasisDecompose), {})(**dec.args, verbose=False, **kw)
+        out = inst.go()
+        torch.cuda.synchronize()
+        if i >= max(1, args.warmup):
+            times.append(time.perf_counter() - t0)
+    ref = None
+    if table:
+        mpath = os.path.join(TABLES, table, "meta.json")
+        if os.path.exists(mpath):
+            with open(mpath) as f:
+                ref = json.load(f).get("seconds")
+    per = sum(times) / len(times)
+    print(json.dumps({
+        "metric": "seconds per modal decomposition (Decomposer.go)", "value": per, "unit": "s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * per,
+        "higher_is_better": False, "scaling": None, "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"{args.workload}: {model} {kw}, N_modes {M}, Lbox {lbox}, Nmax {nmax}, "
+                               "k_grid_size 150, ModeTol 1e-4, MaxModeCount 150",
+                   "modes": int(inst.basis.mode_indices.shape[1]), "tetrapyd_points": int(inst.basis.tetrapyd_grid_size),
+                   "pursuit_steps": len(inst.basis.omp_log), "nonzero_alpha": int(np.count_nonzero(out["AlphaTable"][:, 3]))},
+        "covariance_s": inst.basis.timings["covariance_s"],
+        "reference_decomposer_s": ref,
+        "reference_decomposer_host": "8-core x86 (the table's meta.json)" if ref else None}))
+
+
 def reference_arm(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    if args.workload not in WORKLOADS:  # batches: the reference runs one realisation per process
+    if args.workload not in WORKLOADS:  # batches / decompositions: the IC path's reference arm
         args.workload = "scalarI_m12_n256"
     cfg = make_cfg(args.workload, 1234)
     n = args.cpu_sample_n
@@ -573,5 +620,7 @@ if __name__ == "__main__":
         reference_arm(a)
     elif a.workload in BATCH_WORKLOADS:
         batch_arm(a)
+    elif a.workload in DECOMP_WORKLOADS:
+        decomp_arm(a)
     else:
         gpu_arm(a)

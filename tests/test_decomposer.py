@@ -220,3 +220,22 @@ def test_decomposer_scalarI_matches_reference_table(cuda, tmp_path):
     print("correlation: reference table", c_ref, "this run", c_got)
     assert abs(c_ref - 0.9998542847) < 1e-8  # the reference table under this basis (CPU oracle: 0.99985428472)
     assert abs(c_got - c_ref) < 2e-5
+
+
+@pytest.mark.gpu
+def test_decomposer_logresonance_m20_matches_reference_table(cuda, tmp_path):
+    """The resonant template of the 1536^3 case (LogResonance w_res = 10,
+    20 modes, Lbox 2000, Nmax 1536): the pursuit runs its 129 steps to
+    MaxModeCount and ends on the reference's 132 modes with the reference's
+    coefficients."""
+    name = "logres_w10_m20_L2000_n1536"
+    m = meta(name)
+    dec = utils.Decomposer(m["N_modes"], m["n_s"], m["Lbox"], m["Nmax"], m["ModeTol"], m["MaxModeCount"])
+    dec.go(models.LogResonance, B.BasicBasisDecompose, outdir=str(tmp_path), verbose=False, **m["model_kwargs"])
+    got = np.loadtxt(os.path.join(str(tmp_path), "AlphaTable.dat"))
+    want = golden_table(name)
+    assert np.array_equal(got[:, :3], want[:, :3])
+    assert np.array_equal(got[:, 3] != 0, want[:, 3] != 0)
+    assert np.abs(got[:, 3] - want[:, 3]).max() <= 1e-6 * np.abs(want[:, 3]).max()
+    ai = np.loadtxt(os.path.join(str(tmp_path), "AiTable.dat"))
+    assert np.allclose(ai, np.loadtxt(os.path.join(GOLDEN, "tables", name, "AiTable.dat")), rtol=1e-15, atol=1e-15)

@@ -166,6 +166,26 @@ def test_run_glass_matches_run(cuda):
     assert np.array_equal(ids.cpu().numpy(), z["ids"])
 
 
+def test_random_glass_vs_oracle(cuda):
+    """A glass that is not a lattice (uniform random positions, tiled 2^3
+    times): trilinear weights of every corner in play (read_glass.c:129-214,
+    main.c:1440-1516)."""
+    cfg = dict(SMALL[0])
+    rng = np.random.default_rng(11)
+    glass = rng.uniform(0, 100.0, (3000, 3)).astype(np.float32)
+    k, t = bbks()
+    o = O.Oracle(cfg, k, t)
+    lagr = o.tile_glass(glass, 100.0, 2)
+    r = o.run(*table(cfg["table"], cfg["N_modes"]), lagr)
+    g = gen_for(cfg)
+    pos, vel, ids = g.run_glass(torch.from_numpy(glass).cuda(), 100.0, 2)
+    d_gpu = periodic_delta(pos.cpu().numpy(), lagr, cfg["Box"])
+    d_ref = periodic_delta(r["pos"], lagr, cfg["Box"])
+    assert rel_rms(d_gpu, d_ref) < 1e-5
+    assert rel_rms(vel.cpu().numpy(), r["vel"]) < 1e-5
+    assert np.array_equal(ids.cpu().numpy(), np.arange(1, len(lagr) + 1))
+
+
 def test_run_host_matches_device(cuda):
     cfg = SMALL[1]
     r = oracle_run(key(cfg))

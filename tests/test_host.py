@@ -155,7 +155,7 @@ def test_potential_dump_layout(tmp_path):
 def test_c_abi_library_exports_every_declared_symbol():
     build()
     hdr = open(os.path.join(ROOT, "include", "aarambam.h")).read()
-    declared = set(re.findall(r"^\s*(?:int|void|const char\*)\s+(aar_[a-z0-9_]+)\s*\(", hdr, re.M))
+    declared = set(re.findall(r"^\s*(?:int|void|size_t|const char\*)\s+(aar_[A-Za-z0-9_]+)\s*\(", hdr, re.M))
     assert declared == set(_lib.EXPORTS)
     L = ctypes.CDLL(LIB)
     for name in declared:
@@ -210,3 +210,20 @@ def test_skip_ahead_window_integer():
             V = (V + MOD * d) // B
         assert digs[:12] == seq[t:t + 12]
         assert (digs[7] - digs[0] - digs[12]) % B == car[t + 11]
+
+
+def test_multi_file_glass(tmp_path):
+    """A glass split over files base.0, base.1 (find_files, read_glass.c:226-260)."""
+    rng = np.random.default_rng(2)
+    a = rng.uniform(0, 100, (40, 3)).astype(np.float32)
+    b = rng.uniform(0, 100, (24, 3)).astype(np.float32)
+    base = str(tmp_path / "glass")
+    for i, part in enumerate((a, b)):
+        h = gadget.make_header(npart=[0, len(part), 0, 0, 0, 0], npartTotal=[0, 64, 0, 0, 0, 0], num_files=2,
+                               BoxSize=100.0)
+        with open(f"{base}.{i}", "wb") as f:
+            gadget._write_record(f, h.tobytes())
+            gadget._write_record(f, part.astype("<f4").tobytes())
+    assert gadget.glass_files(base) == [f"{base}.0", f"{base}.1"]
+    pos, h = gadget.read_glass(base)
+    assert np.array_equal(pos, np.concatenate([a, b])) and int(h["num_files"]) == 2

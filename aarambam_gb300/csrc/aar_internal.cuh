@@ -111,6 +111,7 @@ struct Plan {
   float* d_amp = nullptr;     // per n^2 noise amplitude
   float* d_twb = nullptr;     // per n^2 T(k) / (Dplus Beta)
   float* d_sinc = nullptr;    // per grid index: CIC window sin(x)/x
+  float* d_isinc2 = nullptr;  // per grid index: 1 / (sin(x)/x)^2
   float* d_qtab = nullptr;    // [M][nsq] field filters q_p per n^2
   float* d_rtab = nullptr;    // [nsq][rtab_stride] radial parts rho_r per n^2 (r fastest)
   int rtab_stride = 0;

@@ -234,7 +234,7 @@ static void plan_release(Plan* p) {
   p->prof.clear();
   for (auto e : p->event_pool) cudaEventDestroy(e);
   p->event_pool.clear();
-  void* ptrs[] = {p->d_phik, p->d_work, p->d_seed, p->d_twN, p->d_twH, p->d_amp, p->d_twb, p->d_rlxpow, p->d_terms, p->d_io, p->d_qtab, p->d_rtab, p->d_sinc, p->d_adj_scratch};
+  void* ptrs[] = {p->d_phik, p->d_work, p->d_seed, p->d_twN, p->d_twH, p->d_amp, p->d_twb, p->d_rlxpow, p->d_terms, p->d_io, p->d_qtab, p->d_rtab, p->d_sinc, p->d_isinc2, p->d_adj_scratch};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   p->d_phik = p->d_work = nullptr;
@@ -243,6 +243,7 @@ static void plan_release(Plan* p) {
   p->d_amp = p->d_twb = nullptr;
   p->d_rlxpow = p->d_terms = nullptr;
   p->d_qtab = p->d_rtab = nullptr;
+  p->d_sinc = p->d_isinc2 = nullptr;
   p->d_io = nullptr;
   p->io_cap = 0;
   p->d_adj_scratch = nullptr;
@@ -263,7 +264,7 @@ static bool pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
 static int alloc_fused(Plan* p, int M) {
   int N = p->N;
   size_t fbytes = sizeof(float2) * (size_t)N * N * p->HP;
-  int nwork = M == 0 ? 1 : std::max(M, 8);
+  int nwork = M == 0 ? 1 : std::max(M, 9);  // the 2LPT schedule uses slots 0..8
   if (p->d_work && p->nwork >= nwork) return AAR_OK;
   if (p->d_work) {
     cudaFree(p->d_work);
@@ -414,6 +415,19 @@ static int create(Plan* p) {
     }
     if ((rc = plan_alloc(p, (void**)&p->d_sinc, sizeof(float) * N))) return rc;
     AAR_CUDA_TRY(p, cudaMemcpy(p->d_sinc, sinc.data(), sizeof(float) * N, cudaMemcpyHostToDevice));
+    // its inverse square, the per-axis CIC deconvolution factor of the
+    // separable 2LPT passes
+    std::vector<float> is2(N);
+    for (int i = 0; i < N; ++i) {
+      double kv = sidx(i, N) * 2 * kPi / q.box, f = 1;
+      if (kv != 0) {
+        f = (kv * q.box / 2) / N;
+        f = sin(f) / f;
+      }
+      is2[i] = (float)(1.0 / (f * f));
+    }
+    if ((rc = plan_alloc(p, (void**)&p->d_isinc2, sizeof(float) * N))) return rc;
+    AAR_CUDA_TRY(p, cudaMemcpy(p->d_isinc2, is2.data(), sizeof(float) * N, cudaMemcpyHostToDevice));
   }
   return AAR_OK;
 }

@@ -235,6 +235,7 @@ struct ModalRowOp {
   // resident rows per SM: shared memory holds two at 1024^3 with 20 modes;
   // below that registers decide (three rows: 80 registers, no spill)
   static constexpr int min_blocks(int n) { return n >= 1024 ? 2 : 3; }
+  static constexpr bool kZfac = false;
   static constexpr bool kPairs = true;
   int M, nr;
   int r_of_slot[kMaxModes];
@@ -295,7 +296,11 @@ struct ModalRowOp {
 struct SourceRowOp {
   static constexpr int min_blocks(int) { return 4; }  // seven lines per row
   static constexpr bool kPairs = true;
+  static constexpr bool kZfac = true;  // z factors of the Hessians (1, 1, kz, 1, kz, kz^2)
   int out;
+  float kF;
+  const float* isinc2;
+  __device__ ZFac zfac(int l) const { return ZFac{l == 2 || l == 4 ? 1 : l == 5 ? 2 : 0, kF, isinc2}; }
   __device__ int nin() const { return 6; }
   __device__ int in_slot(int l) const { return l; }
   __device__ int nout() const { return 1; }
@@ -316,10 +321,17 @@ struct SourceRowOp {
   }
 };
 
-// plain c2r of one field per blockIdx.y (slot = first + blockIdx.y)
+// c2r of one field per blockIdx.y (slot = first + blockIdx.y), each with
+// its z factor (ZFac type ztype[blockIdx.y]; 0 = plain c2r)
+struct ZTypes {
+  int t[6];
+  float kF;
+  const float* isinc2;
+};
 template <int N>
 __global__ void __launch_bounds__(256) k_rows_c2r(float2* work, int64_t fs, int HP, int first, int64_t nrows,
-                                                  const float2* __restrict__ twN, const float2* __restrict__ twH) {
+                                                  const float2* __restrict__ twN, const float2* __restrict__ twH,
+                                                  ZTypes zt) {
   using C = RowCfg<N>;
   constexpr int H = C::H;
   extern __shared__ float2 sm[];
@@ -330,7 +342,8 @@ __global__ void __launch_bounds__(256) k_rows_c2r(float2* work, int64_t fs, int 
   bool act = row < nrows && sub < C::LPW;
   float2* line = sm + (warp * C::LPW + sub) * C::LS;
   float2* f = work + (int64_t)(first + blockIdx.y) * fs + (act ? row : 0) * HP;
-  if (act) row_c2r_pre<N>(f, line, t, C::T, twN);
+  const ZFac zf{blockIdx.y < 6 ? zt.t[blockIdx.y] : 0, zt.kF, zt.isinc2};
+  if (act) row_c2r_pre<N>(f, line, t, C::T, twN, zf);
   __syncwarp();
   line_fft_smem<H, C::T, +1>(line, t, twH, act);
   if (act)
@@ -396,27 +409,42 @@ __device__ __forceinline__ void readout_one(const ReadArgs& a, const float* __re
     jj[d] = (i + 1 == N) ? 0 : i + 1;
   }
   const int64_t rs = 2 * (int64_t)a.HP;
-  int64_t o000 = row_of(ii[0], ii[1], N, kXB) * rs, o010 = row_of(ii[0], jj[1], N, kXB) * rs;
-  int64_t o100 = row_of(jj[0], ii[1], N, kXB) * rs, o110 = row_of(jj[0], jj[1], N, kXB) * rs;
   float u = fr[0], v = fr[1], w = fr[2];
-  float f1 = (1 - u) * (1 - v) * (1 - w), f2 = (1 - u) * (1 - v) * w, f3 = (1 - u) * v * (1 - w),
-        f4 = (1 - u) * v * w, f5 = u * (1 - v) * (1 - w), f6 = u * (1 - v) * w, f7 = u * v * (1 - w),
-        f8 = u * v * w;
-  int k0 = ii[2], k1 = jj[2];
-  for (int ax = 0; ax < 3; ++ax) {
-    const float* d1 = F + ax * a.fs;
-    const float* d2 = F + (3 + ax) * a.fs;
-    float dis = d1[o000 + k0] * f1 + d1[o000 + k1] * f2 + d1[o010 + k0] * f3 + d1[o010 + k1] * f4 +
+  float dis[3], dis2[3];
+  if (u == 0.f && v == 0.f && w == 0.f) {
+    // on a grid point (a regular lattice whose spacing Box/N is a binary
+    // fraction): weights f1 = 1, f2..f8 = 0, so the 8-point sum is the one
+    // corner value exactly (finite fields) and the other 7 loads are skipped
+    const int64_t o = row_of(ii[0], ii[1], N, kXB) * rs + ii[2];
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+      dis[ax] = F[ax * a.fs + o];
+      dis2[ax] = F[(3 + ax) * a.fs + o];
+    }
+  } else {
+    int64_t o000 = row_of(ii[0], ii[1], N, kXB) * rs, o010 = row_of(ii[0], jj[1], N, kXB) * rs;
+    int64_t o100 = row_of(jj[0], ii[1], N, kXB) * rs, o110 = row_of(jj[0], jj[1], N, kXB) * rs;
+    float f1 = (1 - u) * (1 - v) * (1 - w), f2 = (1 - u) * (1 - v) * w, f3 = (1 - u) * v * (1 - w),
+          f4 = (1 - u) * v * w, f5 = u * (1 - v) * (1 - w), f6 = u * (1 - v) * w, f7 = u * v * (1 - w),
+          f8 = u * v * w;
+    int k0 = ii[2], k1 = jj[2];
+    for (int ax = 0; ax < 3; ++ax) {
+      const float* d1 = F + ax * a.fs;
+      const float* d2 = F + (3 + ax) * a.fs;
+      dis[ax] = d1[o000 + k0] * f1 + d1[o000 + k1] * f2 + d1[o010 + k0] * f3 + d1[o010 + k1] * f4 +
                 d1[o100 + k0] * f5 + d1[o100 + k1] * f6 + d1[o110 + k0] * f7 + d1[o110 + k1] * f8;
-    float dis2 = d2[o000 + k0] * f1 + d2[o000 + k1] * f2 + d2[o010 + k0] * f3 + d2[o010 + k1] * f4 +
+      dis2[ax] = d2[o000 + k0] * f1 + d2[o000 + k1] * f2 + d2[o010 + k0] * f3 + d2[o010 + k1] * f4 +
                  d2[o100 + k0] * f5 + d2[o100 + k1] * f6 + d2[o110 + k0] * f7 + d2[o110 + k1] * f8;
-    dis2 *= a.inv_n3;
-    float d = dis - (3.f / 7.f) * dis2;
+    }
+  }
+  for (int ax = 0; ax < 3; ++ax) {
+    const float d1 = dis[ax], d2 = dis2[ax] * a.inv_n3;
+    float d = d1 - (3.f / 7.f) * d2;
     float x = p[ax] + d;
     if (x < 0.f) x += a.box;
     if (x >= a.box) x -= a.box;
     op[ax] = x;
-    ov[ax] = dis * a.vp1 - (3.f / 7.f) * dis2 * a.vp2;
+    ov[ax] = d1 * a.vp1 - (3.f / 7.f) * d2 * a.vp2;
   }
 }
 
@@ -556,6 +584,12 @@ struct Launch {
     p->last_launches += 1;
     return AAR_OK;
   }
+  // 2LPT (main.c:1180-1431).  Work slots: 7 = T/(D Beta) phi; Hessians
+  // d_ab in 0..5 (00 01 02 11 12 22) via x outputs P = -kF^2 kx^2 phi_T -> 0,
+  // Q = -kF^2 kx phi_T -> 8, R = -kF^2 phi_T -> 6 and the y fan-out (xy, yz:
+  // ky; yy: ky^2); the source rows apply the z factors (xz, yz: kz; zz:
+  // kz^2) and write S to 6; psi1 (0..2) and psi2 (3..5) likewise from x
+  // outputs in 0, 8 (psi1) and 3, 7 (psi2).
   static int lpt(Plan* p, const LptArgs& a, cudaStream_t st) {
     int64_t fs = fstride(p);
     float2* phit = p->d_work + 7 * fs;  // T/(D Beta) phi, read by the Hessian and psi1 passes
@@ -565,12 +599,15 @@ struct Launch {
     }
     AAR_CUDA_TRY(p, cudaGetLastError());
     p->last_launches += 1;
-    LptOp<N, W, 0> ho{a, phit, p->d_work, fs, tiles(p), p->HP, 6, p->xpass_group};
-    int rc = run_pass<N>(p, ho, tiles(p) * 6, st, "lpt_xinv_hess");
-    if (rc) return rc;
-    if ((rc = ypass<+1>(p, p->d_work, 6, nullptr, st, "lpt_ypass_inv_hess"))) return rc;
+    int rc;
+    {
+      LptXOp<N, W, 0> ho{a, phit, p->d_work, fs, tiles(p), p->HP, {0, 8, 6}, p->xpass_group};
+      if ((rc = run_pass<N>(p, ho, tiles(p) * 3, st, "lpt_xinv_hess"))) return rc;
+      YFanOp<N, W> yf{a, p->d_work, fs, tiles(p), p->HP, {0, 8, 8, 6, 6, 6}, {0, 1, 2, 3, 4, 5}, {0, 1, 0, 2, 1, 0}, 1};
+      if ((rc = run_pass<N>(p, yf, tiles(p) * 6, st, "lpt_ypass_inv_hess"))) return rc;
+    }
     size_t sm_rows = sizeof(float2) * (size_t)7 * RowCfg<N>::LS;
-    SourceRowOp op{6};
+    SourceRowOp op{6, a.m.g.kF, a.isinc2};
     {
       ProfScope ps_(p, "lpt_rows_source", st);
       k_rows<N, SourceRowOp><<<(unsigned)((int64_t)N * N), kRowThreads, sm_rows, st>>>(op, p->d_work, fs, p->HP, p->d_twN,
@@ -579,24 +616,28 @@ struct Launch {
     AAR_CUDA_TRY(p, cudaGetLastError());
     p->last_launches += 1;
     if ((rc = ypass<-1>(p, p->d_work + 6 * fs, 1, nullptr, st, "lpt_ypass_fwd_source"))) return rc;
-    // forward x of the source in place, psi2 from it, then psi1 from phi
+    // forward x of the source in place with -1/k^2, then the displacement x passes
     {
-      AxisOp<N, W, 0, -1> xs{p->d_work + 6 * fs, 0, tiles(p), p->HP, nullptr};
+      XfwdInvK2Op<N, W> xs{p->d_work + 6 * fs, tiles(p), p->HP, a.m.g.kF};
       if ((rc = run_pass<N>(p, xs, tiles(p), st, "lpt_xfwd_source"))) return rc;
     }
-    LptOp<N, W, 2> m2{a, p->d_phik, p->d_work, fs, tiles(p), p->HP, 6, p->xpass_group};
-    if ((rc = run_pass<N>(p, m2, tiles(p) * 3, st, "lpt_xpsi2"))) return rc;
-    LptOp<N, W, 1> m1{a, phit, p->d_work, fs, tiles(p), p->HP, 6, p->xpass_group};
-    if ((rc = run_pass<N>(p, m1, tiles(p) * 3, st, "lpt_xpsi1"))) return rc;
-    if ((rc = ypass<+1>(p, p->d_work, 6, nullptr, st, "lpt_ypass_inv_disp"))) return rc;
+    {
+      LptXOp<N, W, 1> m1{a, phit, p->d_work, fs, tiles(p), p->HP, {0, 8, 0}, p->xpass_group};
+      if ((rc = run_pass<N>(p, m1, tiles(p) * 2, st, "lpt_xpsi1"))) return rc;
+      LptXOp<N, W, 1> m2{a, p->d_work + 6 * fs, p->d_work, fs, tiles(p), p->HP, {3, 7, 0}, p->xpass_group};
+      if ((rc = run_pass<N>(p, m2, tiles(p) * 2, st, "lpt_xpsi2"))) return rc;
+      YFanOp<N, W> yf{a, p->d_work, fs, tiles(p), p->HP, {0, 8, 8, 3, 7, 7}, {0, 1, 2, 3, 4, 5}, {3, 4, 3, 3, 4, 3}, 1};
+      if ((rc = run_pass<N>(p, yf, tiles(p) * 6, st, "lpt_ypass_inv_disp"))) return rc;
+    }
     using R = RowCfg<N>;
     int lines_per_block = 8 * R::LPW;
     int64_t nrows = (int64_t)N * N;
     dim3 grid((unsigned)((nrows + lines_per_block - 1) / lines_per_block), 6);
+    const ZTypes zt{{3, 3, 4, 3, 3, 4}, a.m.g.kF, a.isinc2};
     {
       ProfScope ps_(p, "lpt_rows_c2r", st);
       k_rows_c2r<N><<<grid, 256, sizeof(float2) * lines_per_block * R::LS, st>>>(p->d_work, fs, p->HP, 0, nrows,
-                                                                                p->d_twN, p->d_twH);
+                                                                                p->d_twN, p->d_twH, zt);
     }
     AAR_CUDA_TRY(p, cudaGetLastError());
     p->last_launches += 1;
@@ -694,6 +735,7 @@ LptArgs lpt_args(Plan* p) {
   a.inv_Dbeta = (float)(1.0 / (p->Dplus * p->Beta));
   a.twb = p->d_twb;
   a.sinc = p->d_sinc;
+  a.isinc2 = p->d_isinc2;
   a.box_over_2n = (float)(p->prm.box / 2 / p->N);
   return a;
 }
@@ -785,7 +827,8 @@ struct Xform {
     dim3 g2((unsigned)((nrows + lpb - 1) / lpb), 1);
     {
       ProfScope ps_(p, "xform_rows", st);
-      k_rows_c2r<N><<<g2, 256, sizeof(float2) * lpb * R::LS, st>>>(slot, 0, p->HP, 0, nrows, p->d_twN, p->d_twH);
+      k_rows_c2r<N><<<g2, 256, sizeof(float2) * lpb * R::LS, st>>>(slot, 0, p->HP, 0, nrows, p->d_twN, p->d_twH,
+                                                                  ZTypes{{0, 0, 0, 0, 0, 0}, 0.f, nullptr});
     }
     AAR_CUDA_TRY(p, cudaGetLastError());
     p->last_launches += 1;

@@ -42,6 +42,7 @@ static std::string gen_source(int N, int M, int minb, int pairs, const TermList&
   s += "struct JitRowOp {\n";
   s += "  static constexpr int min_blocks(int) { return " + std::to_string(minb) + "; }\n";
   s += "  static constexpr bool kPairs = " + std::string(pairs ? "true" : "false") + ";\n";
+  s += "  static constexpr bool kZfac = false;\n";
   s += "  __device__ int nin() const { return " + std::to_string(M) + "; }\n";
   s += "  __device__ int in_slot(int l) const { return l; }\n";
   s += "  __device__ int nout() const { return " + std::to_string(tl.nr) + "; }\n";

@@ -154,22 +154,25 @@ struct XinvOp {
   }
 };
 
-// 2LPT passes (MODE 0: Hessians, 6 components; MODE 1: ZA displacements,
-// 3; MODE 2: 2LPT displacements, 3; items in group_order): the factor lpt_factor<MODE> (main.c:1180-1368) on
-// T/(D Beta) phi (MODE 0, 1: `phi` points at that product, made once by
-// k_scale_twb, so the per-|k|^2 table is not gathered nine times), or for
-// MODE 2 on the source slot already transformed along x; then the inverse x
-// FFT.  Outputs: Hessians to slots 0..5, psi1 to slots 0..2, psi2
-// to slots 3..5.
-template <int N, int W, int MODE>
-struct LptOp {
+// 2LPT x passes.  The spectral factors of main.c:1180-1368 are products of
+// one factor per axis, except 1/k^2 of psi2, which the forward x pass of the
+// source applies (XfwdInvK2Op); so an x pass writes one field per distinct
+// x factor and a fan-out y pass (YFanOp) and the c2r rows (ZFac) apply the
+// rest.  KIND 0, Hessians d_ab = -k_a k_b T/(D Beta) phi: x factors -kF^2 kx^2,
+// -kF^2 kx, -kF^2 (3 outputs).  KIND 1, displacements i k_a smth on
+// T/(D Beta) phi (psi1) or on -S/k^2 (psi2), smth = [sinc_x sinc_y sinc_z]^-2:
+// x factors i kF kx / sinc_x^2 and i / sinc_x^2 (2 outputs).  Items in
+// group_order over the outputs.
+template <int N, int W, int KIND>
+struct LptXOp {
   LptArgs a;
-  const float2* phi;
+  const float2* src;
   float2* work;
   int64_t fs, tiles;
-  int HP, src_slot;
+  int HP;
+  int out[3];
   int64_t grp;
-  static constexpr int NC = MODE == 0 ? 6 : 3;
+  static constexpr int NC = KIND == 0 ? 3 : 2;
   __device__ void coords(int64_t item, int& o, int& c0, int& comp) const {
     int64_t t;
     group_order(item, tiles, NC, grp, t, comp);
@@ -180,11 +183,8 @@ struct LptOp {
   __device__ void load(float2* b, int64_t item) const {
     int o, c0, comp;
     coords(item, o, c0, comp);
-    const float2* src = MODE == 2 ? work + (int64_t)src_slot * fs : phi;
     tile_load_async<N, W, 0>(b, src, HP, o, c0);
   }
-  // the spectral factor of component comp per value of the first FFT stage:
-  // real for MODE 0, imaginary for MODE 1 and 2 (stored as its imaginary part)
   struct Early {
     float f[AxisCfg<N, W>::E];
   };
@@ -192,30 +192,128 @@ struct LptOp {
     using C = AxisCfg<N, W>;
     int o, c0, comp;
     coords(item, o, c0, comp);
-    const int ky = sidx(o, N);
+    const float kF = a.m.g.kF;
 #pragma unroll
     for (int i = 0; i < C::E; ++i) {
       int n, w;
       const bool own = fft_owned<N, W>(i, n, w);
-      const int kz = c0 + w, kx = sidx(n, N);
-      const int n2 = kx * kx + ky * ky + kz * kz;
+      const float kx = (float)sidx(n, N);
       float f = 0.f;
-      if (own && kz <= N / 2) {
-        const float2 g = lpt_factor<MODE, false>(a, comp, n, o, kz, kx, ky, n2);
-        f = MODE == 0 ? g.x : g.y;
+      if (own && c0 + w <= N / 2) {
+        if (KIND == 0) {
+          f = comp == 0 ? -kF * kF * kx * kx : comp == 1 ? -kF * kF * kx : -kF * kF;
+        } else {
+          const float is2 = __ldg(a.isinc2 + n);
+          f = comp == 0 ? kF * kx * is2 : is2;
+        }
       }
       r.f[i] = f;
     }
   }
   __device__ bool pre(float2*, int64_t, const Early&) const { return false; }
   __device__ void body(float2* b, int64_t, const float2* tw, const Early& r) const {
-    tile_fft<N, W, +1, MODE == 0 ? 1 : 2>(b, tw, r.f);
+    tile_fft<N, W, +1, KIND == 0 ? 1 : 2>(b, tw, r.f);
     __syncthreads();
   }
   __device__ void store(const float2* b, int64_t item) const {
     int o, c0, comp;
     coords(item, o, c0, comp);
-    tile_store<N, W, 0>(b, work + (int64_t)(MODE == 2 ? 3 + comp : comp) * fs, HP, o, c0);
+    tile_store<N, W, 0>(b, work + (int64_t)out[comp] * fs, HP, o, c0);
+  }
+};
+
+// Inverse y pass fanning fields out: item (tile, c), c < NC: field in[c]
+// times the y factor type[c] (axis_factor), inverse y FFT, into out[c].
+// Outputs never alias an input that another item still reads (an in-place
+// output reads only its own input).
+template <int N, int W>
+struct YFanOp {
+  static constexpr int NC = 6;
+  LptArgs a;
+  float2* work;
+  int64_t fs, tiles;
+  int HP;
+  int in[NC], out[NC], type[NC];
+  int64_t grp;
+  __device__ void coords(int64_t item, int& o, int& c0, int& c) const {
+    int64_t t;
+    group_order(item, tiles, NC, grp, t, c);
+    int ncol = HP / W;
+    o = (int)(t / ncol);
+    c0 = (int)(t % ncol) * W;
+  }
+  __device__ void load(float2* b, int64_t item) const {
+    int o, c0, c;
+    coords(item, o, c0, c);
+    tile_load_async<N, W, 1>(b, work + (int64_t)in[c] * fs, HP, o, c0);
+  }
+  struct Early {
+    float f[AxisCfg<N, W>::E];
+  };
+  __device__ void early(Early& r, int64_t item) const {
+    using C = AxisCfg<N, W>;
+    int o, c0, c;
+    coords(item, o, c0, c);
+    const int ty = type[c];
+#pragma unroll
+    for (int i = 0; i < C::E; ++i) {
+      int n, w;
+      fft_owned<N, W>(i, n, w);
+      r.f[i] = axis_factor(ty, sidx(n, N), a.m.g.kF, a.isinc2, n);
+    }
+  }
+  __device__ bool pre(float2*, int64_t, const Early&) const { return false; }
+  __device__ void body(float2* b, int64_t, const float2* tw, const Early& r) const {
+    tile_fft<N, W, +1, 1>(b, tw, r.f);
+    __syncthreads();
+  }
+  __device__ void store(const float2* b, int64_t item) const {
+    int o, c0, c;
+    coords(item, o, c0, c);
+    tile_store<N, W, 1>(b, work + (int64_t)out[c] * fs, HP, o, c0);
+  }
+};
+
+// Forward x pass of the 2LPT source in place, then S <- -S / (kF^2 |k|^2)
+// (0 at k = 0): the non-separable part of psi2 = -i k_a / k^2 S smth
+// (main.c:1356-1363).
+template <int N, int W>
+struct XfwdInvK2Op {
+  float2* f;
+  int64_t tiles;
+  int HP;
+  float kF;
+  __device__ void coords(int64_t item, int& o, int& c0) const {
+    int ncol = HP / W;
+    o = (int)(item / ncol);
+    c0 = (int)(item % ncol) * W;
+  }
+  __device__ void load(float2* b, int64_t item) const {
+    int o, c0;
+    coords(item, o, c0);
+    tile_load_async<N, W, 0>(b, f, HP, o, c0);
+  }
+  struct Early {};
+  __device__ void early(Early&, int64_t) const {}
+  __device__ bool pre(float2*, int64_t, const Early&) const { return false; }
+  __device__ void body(float2* b, int64_t, const float2* tw, const Early&) const {
+    tile_fft<N, W, -1>(b, tw);
+    __syncthreads();
+  }
+  __device__ void store(const float2* b, int64_t item) const {
+    using C = AxisCfg<N, W>;
+    int o, c0;
+    coords(item, o, c0);
+    const TileAddr<N, W, 0> ta(HP, o, c0);
+    const int ky = sidx(o, N), kz = c0 + ta.w;
+#pragma unroll 4
+    for (int q = 0; q < C::PER; ++q) {
+      const int kx = sidx(ta.n0 + q * TileAddr<N, W, 0>::DN, N);
+      const int n2 = kx * kx + ky * ky + kz * kz;
+      const float g = n2 ? -1.f / (kF * kF * (float)n2) : 0.f;
+      const float2 v = b[ta.s(q)];
+      f[ta.g(q)] = make_float2(v.x * g, v.y * g);
+    }
   }
 };
 

@@ -19,6 +19,26 @@ __device__ __forceinline__ void cp_async_wait() {
 }
 
 
+// Per-axis real factor of the 2LPT y pass and c2r rows (index k along the
+// axis; y uses the signed index, z the column index kz = 0..N/2): 0: 1,
+// 1: k, 2: k^2, 3: 1/sinc^2, 4: kF k / sinc^2 (isinc2 = 1/sinc^2 per grid
+// index gi).
+__device__ __forceinline__ float axis_factor(int type, int k, float kF, const float* __restrict__ isinc2, int gi) {
+  if (type == 0) return 1.f;
+  if (type == 1) return (float)k;
+  if (type == 2) return (float)k * (float)k;
+  const float is2 = __ldg(isinc2 + gi);
+  return type == 3 ? is2 : kF * (float)k * is2;
+}
+
+// z factor of a row's spectrum, applied as the c2r pre-step reads X_k
+struct ZFac {
+  int type;  // axis_factor type, 0 = none
+  float kF;
+  const float* isinc2;
+  __device__ __forceinline__ float at(int k) const { return axis_factor(type, k, kF, isinc2, k); }
+};
+
 // Row layout: complex row X[0..N/2] at field + m HP, m the row's memory
 // index (the plan's row order maps (x, y) to m); the real row x[0..N-1]
 // occupies the same bytes (float2 z_n = (x_{2n}, x_{2n+1})).  The row steps
@@ -35,11 +55,15 @@ struct RowCfg {
 // inverse half-length FFT (FFTW c2r semantics: Im X_0, Im X_{N/2} dropped)
 template <int N>
 __device__ __forceinline__ void row_c2r_pre(const float2* __restrict__ X, float2* line, int t, int T,
-                                            const float2* __restrict__ twN) {
+                                            const float2* __restrict__ twN, ZFac zf = ZFac{0, 0.f, nullptr}) {
   constexpr int H = N / 2;
   for (int k = t; k <= H / 2; k += T) {
     int k2 = H - k;
     float2 a = X[k], b = X[k2];
+    if (zf.type) {
+      a = cscale(a, zf.at(k));
+      b = cscale(b, zf.at(k2));
+    }
     if (k == 0) {
       a.y = 0.f;
       b.y = 0.f;
@@ -66,11 +90,16 @@ __device__ __forceinline__ void row_c2r_pre(const float2* __restrict__ X, float2
 // The same pre-step in place, on X_0..X_{N/2} already staged in `line`
 // (element k at spad(k)): each lane rewrites the pair (k, H - k) it reads.
 template <int N>
-__device__ __forceinline__ void row_c2r_pre_inplace(float2* line, int t, int T, const float2* __restrict__ twN) {
+__device__ __forceinline__ void row_c2r_pre_inplace(float2* line, int t, int T, const float2* __restrict__ twN,
+                                                    ZFac zf = ZFac{0, 0.f, nullptr}) {
   constexpr int H = N / 2;
   for (int k = t; k <= H / 2; k += T) {
     int k2 = H - k;
     float2 a = line[spad(k)], b = line[spad(k2)];
+    if (zf.type) {
+      a = cscale(a, zf.at(k));
+      b = cscale(b, zf.at(k2));
+    }
     if (k == 0) {
       a.y = 0.f;
       b.y = 0.f;
@@ -142,7 +171,10 @@ __device__ __forceinline__ void rows_body(const Op& op, float2* work, int64_t fs
     int l = l0 + sub;
     bool act = l < op.nin() && sub < C::LPW;
     float2* line = sm + (act ? l : 0) * C::LS;
-    if (act) row_c2r_pre_inplace<N>(line, t, C::T, twN);
+    if (act) {
+      if constexpr (Op::kZfac) row_c2r_pre_inplace<N>(line, t, C::T, twN, op.zfac(l));
+      else row_c2r_pre_inplace<N>(line, t, C::T, twN);
+    }
     __syncwarp();
     line_fft_smem<H, C::T, +1>(line, t, twH, act);
   }

@@ -29,6 +29,7 @@ struct LptArgs {
   float inv_Dbeta;    // 1 / (Dplus Beta)
   const float* twb;   // per n^2: T(k) / (Dplus Beta)
   const float* sinc;  // per grid index: sin(x)/x, x = k Box / 2N (1 at k = 0)
+  const float* isinc2;  // per grid index: 1 / sinc^2
   float box_over_2n;
 };
 

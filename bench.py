@@ -169,9 +169,11 @@ def alg_bytes(name: str, N: int, M: int, R: int, npart: int) -> float:
         "seedtable": 4.0 * N * N, "noise": F + 4.0 * N * N,
         "modal_xinv": (1 + M) * F, "modal_ypass_inv": 2 * M * F, "modal_rows": (M + R) * F,
         "modal_ypass_fwd": 2 * R * F, "modal_xfwd": 2 * R * F, "modal_acc": (R + 2) * F,
-        "lpt_scale_twb": 2 * F, "lpt_xinv_hess": 7 * F, "lpt_ypass_inv_hess": 12 * F, "lpt_rows_source": 7 * F,
-        "lpt_ypass_fwd_source": 2 * F, "lpt_xfwd_source": 2 * F, "lpt_xpsi2": 4 * F, "lpt_xpsi1": 4 * F,
-        "lpt_ypass_inv_disp": 12 * F,
+        # 2LPT: x passes write one field per distinct x factor (Hessians 3,
+        # displacements 2 + 2) and the y passes fan them out to 6
+        "lpt_scale_twb": 2 * F, "lpt_xinv_hess": 4 * F, "lpt_ypass_inv_hess": 9 * F, "lpt_rows_source": 7 * F,
+        "lpt_ypass_fwd_source": 2 * F, "lpt_xfwd_source": 2 * F, "lpt_xpsi2": 3 * F, "lpt_xpsi1": 3 * F,
+        "lpt_ypass_inv_disp": 10 * F,
         "lpt_rows_c2r": 12 * F, "readout": 6 * 4.0 * N ** 3 + 36.0 * npart,
     }
     return table.get(name, float("nan"))

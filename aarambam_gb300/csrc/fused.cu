@@ -493,7 +493,7 @@ static int run_pass(Plan* p, const Op& op, int64_t nitems, cudaStream_t st, cons
   constexpr int W = 8;
   using A = AxisCfg<N, W>;
   auto kern = k_pass<N, W, Op>;
-  const size_t smem = A::SMEM;
+  const size_t smem = A::SMEM + ExtraSmem<Op>::value;
   AAR_CUDA_TRY(p, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   if (nitems < 1) return AAR_OK;
   if (nitems > 0x7fffffff) return set_err(p, std::string(name) + ": too many work items"), AAR_ERR_ARG;

@@ -132,20 +132,33 @@ __device__ __forceinline__ void tile_fft(float2* sm, const float2* __restrict__ 
   line_fft_smem<N, C::T, SIGN, 0, SCALE>(sm + (act ? line : 0) * C::LS, t, tw, act, 1 + (act ? line : 0), sc);
 }
 
+// rho_n(k) of the accumulation evaluated per cell (main.c:825-860):
+// k^(s (n-3)) for n <= 3, (P_{n-1}(kbar) - X0[n-1]) / k^2 above, with
+// kbar = -1 + 2 (k^s - kmin^s)/(kmax^s - kmin^s); kmin = kF, so
+// k^s - kmin^s = kmin^s expm1(s ln(sqrt(n^2))) (no cancellation near kmin),
+// and P_l by the Bonnet recurrence P_l = A_l kbar P_{l-1} - B_l P_{l-2}.
+struct RhoArgs {
+  float s, c1, log2kF, inv_kF2;  // c1 = 2 kmin^s / (kmax^s - kmin^s)
+  float x0[kMaxModes];
+  float A[kMaxModes], B[kMaxModes];  // (2l-1)/l, (l-1)/l
+};
+
 // Last modal step, after the forward x transform of every active slot r:
-// acc = sum_r rho_r(k) g_r(k) (per-|k|^2 table, Neumaier-compensated in
-// registers), then phi <- phi + fnl_n3 * acc, DC = 0 (main.c:1101-1126).
+// acc = sum_r rho_r(k) g_r(k) (rho_r computed per cell in FP32, RhoArgs;
+// Neumaier-compensated in registers), then phi <- phi + fnl_n3 * acc,
+// DC = 0 (main.c:1101-1126).
 // One thread per half-spectrum element (padding columns are not touched);
 // cut cells keep phi as it is.  A streaming kernel: the R slot reads of a
 // thread are independent, so many are in flight per SM.  (Measured: pairs of
 // cells per thread with 16-byte loads were slower, 36.5 vs 30.8 ms at
 // 1024^3; so was the slot list as a kernel parameter, 39.0 ms, and the rho
 // row read with 16-byte loads into registers and the slots walked with
-// compile-time indices, 38.0 ms.)
+// compile-time indices, 38.0 ms.  Gathering rho_r from a per-|k|^2 table,
+// one load per slot, left the kernel waiting on those loads: 31.4 ms.)
 template <int N>
 __global__ void __launch_bounds__(256) k_modal_acc(ModalArgs a, float2* phi, const float2* __restrict__ work,
                                                    int64_t fs, int HP, float fnl_n3, const DevTerms* __restrict__ dt,
-                                                   const float* __restrict__ rtab, int rstride) {
+                                                   const RhoArgs ra) {
   constexpr int K = N / 2 + 1;  // kz = 0 .. N/2 of a row
   constexpr int64_t total = (int64_t)N * N * K;
   // the active slots and their field bases, once per block
@@ -171,12 +184,29 @@ __global__ void __launch_bounds__(256) k_modal_acc(ModalArgs a, float2* phi, con
       continue;
     }
     if (!keep_cell(a.g, kx, ky, kz)) continue;
-    const float* rt = rtab + (int64_t)n2 * rstride;
+    const float lnn2 = logf((float)n2);
+    const float kbar = -1.f + ra.c1 * expm1f(0.5f * ra.s * lnn2);
+    const float L = ra.log2kF + lnn2 * 0.72134752044448170368f;  // log2 k = log2 kF + ln(n2) / (2 ln 2)
+    const float inv_k2 = ra.inv_kF2 / (float)n2;
+    float P0 = 1.f, P1 = kbar;  // P_{deg-1}, P_deg
+    int deg = 1;
     float sx = 0.f, sy = 0.f, cx = 0.f, cy = 0.f;
-#pragma unroll 8
+#pragma unroll 4
     for (int k = 0; k < nr; ++k) {
-      const float rho = __ldg(rt + rs[k]);
+      const int r = rs[k];
       const float2 v = __ldg(base[k] + e);
+      float rho;
+      if (r <= 3) {
+        rho = r == 3 ? 1.f : exp2f(ra.s * (float)(r - 3) * L);
+      } else {
+        while (deg < r - 1) {
+          ++deg;
+          const float Pn = ra.A[deg] * kbar * P1 - ra.B[deg] * P0;
+          P0 = P1;
+          P1 = Pn;
+        }
+        rho = (P1 - ra.x0[r - 1]) * inv_k2;
+      }
       const float tx = v.x * rho, ty = v.y * rho;
       const float ux = sx + tx, uy = sy + ty;
       cx += (fabsf(sx) >= fabsf(tx)) ? (sx - ux) + tx : (tx - ux) + sx;
@@ -506,6 +536,23 @@ static int run_pass(Plan* p, const Op& op, int64_t nitems, cudaStream_t st, cons
   return AAR_OK;
 }
 
+static RhoArgs rho_args(const Plan* p) {
+  RhoArgs r{};
+  const double ns = p->prm.primordial_index, box = p->prm.box;
+  const double kF = 2 * kPi / box, kmin = kF, kmax = kF * p->prm.nmax;
+  const double sx = (4 - ns) / 3, kmin_s = pow(kmin, sx), kmax_s = pow(kmax, sx);
+  r.s = (float)sx;
+  r.c1 = (float)(2 * kmin_s / (kmax_s - kmin_s));
+  r.log2kF = (float)log2(kF);
+  r.inv_kF2 = (float)(1 / (kF * kF));
+  for (int n = 0; n < kMaxModes; ++n) r.x0[n] = n < (int)p->x0.size() ? (float)p->x0[n] : 0.f;
+  for (int l = 1; l < kMaxModes; ++l) {
+    r.A[l] = (float)((2.0 * l - 1) / l);
+    r.B[l] = (float)((l - 1.0) / l);
+  }
+  return r;
+}
+
 template <int N>
 struct Launch {
   static constexpr int W = 8;
@@ -577,8 +624,7 @@ struct Launch {
     {
       ProfScope ps_(p, "modal_acc", st);
       k_modal_acc<N><<<(unsigned)(p->num_sms * 8), 256, 0, st>>>(a, p->d_phik, p->d_work, fs, p->HP, fnl_n3,
-                                                             (const DevTerms*)p->d_terms, p->d_rtab,
-                                                             p->rtab_stride);
+                                                             (const DevTerms*)p->d_terms, rho_args(p));
     }
     AAR_CUDA_TRY(p, cudaGetLastError());
     p->last_launches += 1;

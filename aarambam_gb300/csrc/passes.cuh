@@ -141,15 +141,46 @@ struct XinvOp {
     coords(item, o, c0, p);
     const int ky = sidx(o, N);
     const float* q = qtab + (int64_t)p * nsq;
+    if constexpr (C::E == 32 && stage_radix(N, C::E, 0) == 32 && C::THREADS == W * C::T && 32 % C::T == 0) {
+      // value i of lane t is line element n = t + T i.  For n >= N/2 the
+      // filter depends on |kx| = N - n, which is element 31 - i of lane
+      // (T - t) % T of the same line (same ky, kz): each lane gathers its
+      // 16 values below N/2 and takes the other 16 from its partner by
+      // shuffle (lane t = 0 pairs with itself one place off: it gathers all).
+      const int t = threadIdx.x % C::T, w = threadIdx.x / C::T;
+      const int kz = c0 + w;
+      const bool col = kz <= N / 2;
+      float g[16];
 #pragma unroll
-    for (int i = 0; i < C::E; ++i) {
-      int n, w;
-      const bool own = fft_owned<N, W>(i, n, w);
-      int kz = c0 + w, kx = sidx(n, N);
-      int n2 = kx * kx + ky * ky + kz * kz;
-      float f = 0.f;
-      if (own && kz <= N / 2 && n2 != 0 && keep_cell(a.g, kx, ky, kz)) f = __ldg(q + n2);
-      r.f[i] = f;
+      for (int i = 0; i < 16; ++i) {
+        const int kx = t + C::T * i;  // < N/2
+        const int n2 = kx * kx + ky * ky + kz * kz;
+        g[i] = col && n2 != 0 && keep_cell(a.g, kx, ky, kz) ? __ldg(q + n2) : 0.f;
+        r.f[i] = g[i];
+      }
+      const int lane = threadIdx.x & 31;
+      const int src = (lane - t) + (C::T - t) % C::T;
+#pragma unroll
+      for (int j = 0; j < 16; ++j) r.f[16 + j] = __shfl_sync(0xffffffffu, g[15 - j], src);
+      if (t == 0) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int kx = sidx(C::T * (16 + j), N);
+          const int n2 = kx * kx + ky * ky + kz * kz;
+          r.f[16 + j] = col && keep_cell(a.g, kx, ky, kz) ? __ldg(q + n2) : 0.f;
+        }
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < C::E; ++i) {
+        int n, w;
+        const bool own = fft_owned<N, W>(i, n, w);
+        int kz = c0 + w, kx = sidx(n, N);
+        int n2 = kx * kx + ky * ky + kz * kz;
+        float f = 0.f;
+        if (own && kz <= N / 2 && n2 != 0 && keep_cell(a.g, kx, ky, kz)) f = __ldg(q + n2);
+        r.f[i] = f;
+      }
     }
   }
   __device__ bool pre(float2*, int64_t, const Early&) const { return false; }

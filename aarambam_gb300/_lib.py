@@ -32,7 +32,7 @@ EXPORTS = [
     "aar_batch_create", "aar_batch_run", "aar_batch_launch_count", "aar_batch_last_error", "aar_batch_destroy",
     "aar_set_spectrum", "aar_adj_spectral", "aar_adj_source", "aar_adj_products", "aar_set_jit", "aar_jit_status",
     "aar_tetra_covariance_scratch_bytes", "aar_tetra_covariance", "aar_tetra_QS", "aar_tetra_residual",
-    "aar_bordered_cond",
+    "aar_bordered_cond", "aar_autotune",
 ]
 AAR_ADJ_OP_ONE, AAR_ADJ_OP_GAUSS, AAR_ADJ_OP_Q, AAR_ADJ_OP_RHO = 0, 1, 2, 3
 AAR_ADJ_OP_HESS, AAR_ADJ_OP_PSI1, AAR_ADJ_OP_PSI2 = 4, 5, 6
@@ -110,6 +110,7 @@ def load(build_if_missing: bool = False):
     L.aar_batch_destroy.argtypes = [vp]
     L.aar_batch_destroy.restype = None
     L.aar_set_jit.argtypes = [vp, i32]
+    L.aar_autotune.argtypes = [vp, C.c_char_p, i32, vp]
     L.aar_jit_status.argtypes = [vp]
     L.aar_jit_status.restype = C.c_char_p
     L.aar_set_spectrum.argtypes = [vp, vp, vp]

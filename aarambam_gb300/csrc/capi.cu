@@ -766,6 +766,86 @@ int aar_set_jit(aar_plan* h, int32_t mode) {
 
 const char* aar_jit_status(const aar_plan* h) { return h ? h->p.jit_status.c_str() : "null plan"; }
 
+// ------------------------------------------------------------- autotuner
+// Times the field stages (noise, modal, 2LPT) of this plan on its device for
+// each schedule candidate and keeps the fastest: row kernel generic or
+// NVRTC-specialised with 2 or 3 resident blocks per SM, and the item
+// grouping of the multi-output x passes (1, one y row of tiles, four rows).
+// Each candidate runs twice (the first run compiles and warms up); the
+// second is timed with CUDA events on the stream.  The plan's spectrum and
+// fields are overwritten, as by a realisation.
+int aar_autotune(aar_plan* h, char* report, int32_t len, void* stream) {
+  if (!h) return AAR_ERR_ARG;
+  Plan* p = &h->p;
+  int rc = ready(p);
+  if (rc) return rc;
+  if (p->prm.precision != AAR_FUSED_FP32) return set_err(p, "the autotuner is for the fused form"), AAR_ERR_ARG;
+  cudaStream_t st = S(stream);
+  struct Cand {
+    int jit, minb;
+    int64_t grp;
+    float ms;
+  };
+  const int64_t row_tiles = p->HP / 8;
+  std::vector<Cand> cands;
+  for (int j = 0; j < 3; ++j)
+    for (int64_t g : {(int64_t)1, row_tiles, 4 * row_tiles})
+      cands.push_back(Cand{j == 0 ? 0 : 2, j == 2 ? 3 : 2, g, -1.f});
+  const int saved_mode = p->jit_mode, saved_minb = p->jit_minb;
+  const int64_t saved_grp = p->xpass_group;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  AAR_CUDA_TRY(p, cudaEventCreate(&e0));
+  AAR_CUDA_TRY(p, cudaEventCreate(&e1));
+  int best = -1;
+  for (size_t i = 0; i < cands.size() && rc == AAR_OK; ++i) {
+    Cand& c = cands[i];
+    p->jit_mode = c.jit;
+    p->jit_minb = c.minb;
+    p->xpass_group = c.grp;
+    if ((rc = jit_prepare(p))) break;
+    if (c.jit && p->jit == nullptr) continue;  // NVRTC unavailable: no such candidate
+    for (int rep = 0; rep < 2 && rc == AAR_OK; ++rep) {
+      if (rep == 1 && (rc = (cudaEventRecord(e0, st) == cudaSuccess ? AAR_OK : AAR_ERR_CUDA))) break;
+      if ((rc = run_noise(p, st)) || (rc = fused_modal(p, st)) || (rc = fused_lpt(p, st))) break;
+      if (rep == 1 && cudaEventRecord(e1, st) != cudaSuccess) rc = AAR_ERR_CUDA;
+    }
+    if (rc) break;
+    if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&c.ms, e0, e1) != cudaSuccess) {
+      rc = AAR_ERR_CUDA;
+      break;
+    }
+    if (best < 0 || c.ms < cands[best].ms) best = (int)i;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc == AAR_ERR_CUDA) cudaGetLastError(), set_err(p, "autotune: a CUDA call failed");
+  if (rc || best < 0) {
+    p->jit_mode = saved_mode;
+    p->jit_minb = saved_minb;
+    p->xpass_group = saved_grp;
+    jit_prepare(p);
+    return rc ? rc : (set_err(p, "autotune: no candidate ran"), AAR_ERR_STATE);
+  }
+  p->jit_mode = cands[best].jit;
+  p->jit_minb = cands[best].minb;
+  p->xpass_group = cands[best].grp;
+  if ((rc = jit_prepare(p))) return rc;
+  ++p->generation;
+  if (report && len > 0) {
+    std::string out;
+    char line[160];
+    for (size_t i = 0; i < cands.size(); ++i) {
+      const Cand& c = cands[i];
+      snprintf(line, sizeof(line), "%s rows=%s minb=%d group=%lld %.3f ms\n", (int)i == best ? "*" : " ",
+               c.jit ? "nvrtc" : "generic", c.jit ? c.minb : 0, (long long)c.grp, c.ms);
+      out += line;
+    }
+    if ((int)out.size() + 1 > len) return set_err(p, "autotune report buffer too small"), AAR_ERR_ARG;
+    memcpy(report, out.c_str(), out.size() + 1);
+  }
+  return AAR_OK;
+}
+
 // ------------------------------------------------------------- adjoint
 int aar_set_spectrum(aar_plan* h, const void* d_in, void* stream) {
   if (!h || !d_in) return AAR_ERR_ARG;

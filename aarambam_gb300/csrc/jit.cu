@@ -101,7 +101,7 @@ int jit_prepare(Plan* p) {
   const Term* ft = (const Term*)(p->host_terms.data() + sizeof(TermList));
   std::vector<Term> terms(ft, ft + tl.nterms);
   const int N = p->N, M = p->M;
-  const int minb = N >= 1024 ? 2 : 3;
+  const int minb = p->jit_minb > 0 ? p->jit_minb : (N >= 1024 ? 2 : 3);
   const int regcap = 65536 / (kRowThreadsHost * minb);
   const int pairs = 2 * 2 * M + 16 <= regcap * 3 / 4;  // f values of two positions fit the register budget
   std::string key = std::to_string(N) + ":" + std::to_string(M) + ":" + std::to_string(minb) + ":" +

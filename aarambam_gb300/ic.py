@@ -119,6 +119,15 @@ class ICGenerator:
     def jit_status(self) -> str:
         return self.L.aar_jit_status(self.h).decode()
 
+    def autotune(self) -> str:
+        """Time the candidate schedules of this plan on its GPU and keep the
+        fastest (aar_autotune); returns the per-candidate report.  The plan's
+        spectrum and fields are overwritten."""
+        buf = C.create_string_buffer(4096)
+        with torch.cuda.device(self.device):
+            check(self.L, self.h, self.L.aar_autotune(self.h, buf, len(buf), self._stream()))
+        return buf.value.decode()
+
     def set_seed(self, seed: int) -> None:
         check(self.L, self.h, self.L.aar_set_seed(self.h, int(seed)))
         self.cfg["Seed"] = int(seed)

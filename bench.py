@@ -68,6 +68,7 @@ def parse():
     ap.add_argument("--workload", default="scalarI_m20_n1024",
                     choices=sorted(WORKLOADS) + sorted(BATCH_WORKLOADS) + sorted(DECOMP_WORKLOADS))
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default schedule (no aar_autotune)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-n", type=int, default=128)
     ap.add_argument("--plain", action="store_true", help="also time the plain FP64 cuFFT form (1 step)")
@@ -349,6 +350,8 @@ def gpu_arm(args):
     alpha, x0, k, t = load_tables(cfg["table"], M)
     R = active_r(alpha)
     gen = ICGenerator(cfg, alpha, x0, k, t)
+    # the plan's schedule, chosen by timing the candidates on this GPU
+    tuned = [] if args.no_autotune else [l for l in gen.autotune().splitlines() if l.strip()]
     lagr = lattice_positions(N, cfg["Box"], dev)
     npart = lagr.shape[0]
     pos = torch.empty_like(lagr)
@@ -473,7 +476,8 @@ def gpu_arm(args):
                                       f"z=49", "nmesh": N, "n_modes": M, "l2": "working set >> L2 (no flush)",
                           "parallelism": "replicas" if world > 1 else "single GPU"},
                "roofline": roofline, "path_roofline": path_roof, "cpu_baseline": cpu, "e2e": e2e, "plain_fp64": plain,
-               "gpu_launches": launches, "clocks": clocks, "precision_vs_fp64_oracle": precision, "kernels": kernels}
+               "gpu_launches": launches, "clocks": clocks, "precision_vs_fp64_oracle": precision, "kernels": kernels,
+               "schedule": tuned}
         print(json.dumps(out))
     if world > 1:
         dist.destroy_process_group()

@@ -263,6 +263,15 @@ void aar_batch_destroy(aar_batch* batch);
 int aar_set_jit(aar_plan* plan, int32_t mode);
 const char* aar_jit_status(const aar_plan* plan);
 
+/* Schedule autotuner (no counterpart in the reference): times the field
+   stages of this plan on its device for each candidate schedule -- the row
+   kernel generic or NVRTC-specialised with 2 or 3 resident blocks per SM,
+   and the item grouping of the multi-output x passes -- and keeps the
+   fastest for the plan's later runs.  Needs tables and transfer function;
+   overwrites the plan's spectrum and fields.  `report` (may be NULL)
+   receives one line per candidate, the chosen one marked '*'. */
+int aar_autotune(aar_plan* plan, char* report, int32_t len, void* stream);
+
 /* Per-kernel timing: when enabled, CUDA events are recorded on the launching
    stream around every kernel; aar_profile_report synchronises the device and
    writes "kernel,launches,total_ms" lines for everything recorded since the

@@ -59,3 +59,31 @@ def test_jit_vs_oracle_small(cuda):
     N = cfg["Nmesh"]
     assert rel_rms((got - gauss) * N**3, (want - wg) * N**3) < 2e-4  # the non-Gaussian part alone
     assert rel_rms(got, want) < 1e-6
+
+
+def test_autotune_picks_a_schedule_and_keeps_results(cuda):
+    """The autotuner times nine schedules (row kernel generic / NVRTC with 2
+    or 3 blocks per SM x three x-pass item groupings), keeps the fastest, and
+    the particles afterwards agree with the default schedule's."""
+    import torch
+    from tests.common import bbks, make_cfg, table
+    from aarambam_gb300.ic import ICGenerator
+    cfg = make_cfg(128, 500.0, 5, 10.0, 10, "scalarI_m10_L500_n256", 256)
+    g = ICGenerator(cfg, *table("scalarI_m10_L500_n256", 10), *bbks())
+    n = torch.arange(128, device="cuda", dtype=torch.float32) * (500.0 / 128)
+    x, y, z = torch.meshgrid(n, n, n, indexing="ij")
+    lagr = torch.stack([x.reshape(-1), y.reshape(-1), z.reshape(-1)], 1).contiguous()
+    pos0, vel0 = g.run(lagr)
+    rep = g.autotune()
+    lines = [l for l in rep.splitlines() if l.strip()]
+    assert len(lines) == 9 and sum(l.startswith("*") for l in lines) == 1
+    pos1, vel1 = g.run(lagr)
+    d0 = (pos0 - lagr).double()
+    d1 = (pos1 - lagr).double()
+    d0 -= 500.0 * torch.round(d0 / 500.0)
+    d1 -= 500.0 * torch.round(d1 / 500.0)
+    # generic and NVRTC row kernels order the term sums differently: FP32
+    # rounding, far inside the 1e-5 displacement bound against FP64
+    err = float(torch.linalg.vector_norm(d1 - d0) / torch.linalg.vector_norm(d0))
+    print(rep, "displacement change", err)
+    assert err < 1e-5

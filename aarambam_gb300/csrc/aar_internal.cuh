@@ -150,6 +150,11 @@ struct Plan {
   int64_t io_cap = 0;
   cudaStream_t copy_stream = nullptr;  // side stream of the host-to-device copy
   cudaEvent_t copy_start = nullptr, copy_done = nullptr;
+  // device-to-host of the particles, chunk by chunk behind the read-out
+  static constexpr int kOutChunks = 8;
+  int out_chunks = kOutChunks;  // chunks of the host read-out (1: one copy after the read-out)
+  cudaStream_t out_stream[2] = {nullptr, nullptr};
+  cudaEvent_t chunk_read[kOutChunks] = {}, out_done[2] = {nullptr, nullptr};
 };
 
 // Records CUDA events around the kernels launched in its scope (when the

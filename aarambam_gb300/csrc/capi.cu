@@ -254,6 +254,16 @@ static void plan_release(Plan* p) {
   if (p->copy_start) cudaEventDestroy(p->copy_start);
   p->copy_stream = nullptr;
   p->copy_done = p->copy_start = nullptr;
+  for (int i = 0; i < 2; ++i) {
+    if (p->out_stream[i]) cudaStreamDestroy(p->out_stream[i]);
+    if (p->out_done[i]) cudaEventDestroy(p->out_done[i]);
+    p->out_stream[i] = nullptr;
+    p->out_done[i] = nullptr;
+  }
+  for (int i = 0; i < Plan::kOutChunks; ++i) {
+    if (p->chunk_read[i]) cudaEventDestroy(p->chunk_read[i]);
+    p->chunk_read[i] = nullptr;
+  }
   plain_free(p);
 }
 
@@ -361,6 +371,7 @@ static int create(Plan* p) {
   AAR_CUDA_TRY(p, cudaGetDevice(&p->dev));
   AAR_CUDA_TRY(p, cudaDeviceGetAttribute(&p->num_sms, cudaDevAttrMultiProcessorCount, p->dev));
   if (const char* g = getenv("AAR_XPASS_GROUP")) p->xpass_group = std::max(1LL, atoll(g));
+  if (const char* g = getenv("AAR_OUT_CHUNKS")) p->out_chunks = std::min(std::max(1, atoi(g)), (int)Plan::kOutChunks);
   p->N = N;
   p->HP = ((N / 2 + 1) + 7) / 8 * 8;
   p->grid.N = N;
@@ -652,7 +663,34 @@ int aar_run_host(aar_plan* h, const float* h_lagr, int64_t npart, float* h_pos, 
     if ((rc = fused_modal(p, st))) return rc;
     if ((rc = fused_lpt(p, st))) return rc;
     AAR_CUDA_TRY(p, cudaStreamWaitEvent(st, p->copy_done, 0));
-    if ((rc = fused_readout(p, d_in, npart, d_pos, d_vel, st))) return rc;
+    // read-out in chunks; each chunk's Pos/Vel go to the host on one of two
+    // side streams while the next chunks are read out
+    if (!p->out_stream[0]) {
+      for (int i = 0; i < 2; ++i) {
+        AAR_CUDA_TRY(p, cudaStreamCreateWithFlags(&p->out_stream[i], cudaStreamNonBlocking));
+        AAR_CUDA_TRY(p, cudaEventCreateWithFlags(&p->out_done[i], cudaEventDisableTiming));
+      }
+      for (int i = 0; i < Plan::kOutChunks; ++i)
+        AAR_CUDA_TRY(p, cudaEventCreateWithFlags(&p->chunk_read[i], cudaEventDisableTiming));
+    }
+    const int nchunk = npart >= (int64_t)p->out_chunks * 65536 ? p->out_chunks : 1;
+    for (int c = 0; c < nchunk; ++c) {
+      const int64_t a = npart * c / nchunk, b = npart * (c + 1) / nchunk, cnt = b - a;
+      if ((rc = fused_readout(p, d_in + 3 * a, cnt, d_pos + 3 * a, d_vel + 3 * a, st))) return rc;
+      if (cnt == 0) continue;
+      cudaStream_t os = p->out_stream[c & 1];
+      AAR_CUDA_TRY(p, cudaEventRecord(p->chunk_read[c], st));
+      AAR_CUDA_TRY(p, cudaStreamWaitEvent(os, p->chunk_read[c], 0));
+      const size_t cb = sizeof(float) * 3 * (size_t)cnt;
+      AAR_CUDA_TRY(p, cudaMemcpyAsync(h_pos + 3 * a, d_pos + 3 * a, cb, cudaMemcpyDeviceToHost, os));
+      AAR_CUDA_TRY(p, cudaMemcpyAsync(h_vel + 3 * a, d_vel + 3 * a, cb, cudaMemcpyDeviceToHost, os));
+    }
+    for (int i = 0; i < 2; ++i) {
+      AAR_CUDA_TRY(p, cudaEventRecord(p->out_done[i], p->out_stream[i]));
+      AAR_CUDA_TRY(p, cudaStreamWaitEvent(st, p->out_done[i], 0));
+    }
+    AAR_CUDA_TRY(p, cudaStreamSynchronize(st));
+    return AAR_OK;
   }
   if (npart > 0) {
     AAR_CUDA_TRY(p, cudaMemcpyAsync(h_pos, d_pos, bytes, cudaMemcpyDeviceToHost, st));

@@ -126,6 +126,7 @@ struct Plan {
   void* jit = nullptr;           // run-time specialised modal row kernel (jit.cu), or null
   int jit_mode = 1;              // 0 off, 1 for N >= 256, 2 always
   int jit_minb = 0;              // resident row blocks per SM of the NVRTC kernel (0: by N)
+  int jit_threads = 0;           // threads per block of the NVRTC row kernel (0: 256)
   int64_t xpass_group = 1;       // tiles per item group of the multi-output x passes (passes.cuh)
   std::string jit_status = "off";
   int nterms = 0, nr_active = 0;

@@ -807,7 +807,9 @@ const char* aar_jit_status(const aar_plan* h) { return h ? h->p.jit_status.c_str
 // ------------------------------------------------------------- autotuner
 // Times the field stages (noise, modal, 2LPT) of this plan on its device for
 // each schedule candidate and keeps the fastest: row kernel generic or
-// NVRTC-specialised with 2 or 3 resident blocks per SM, and the item
+// NVRTC-specialised with 2 or 3 resident blocks per SM of 256 threads or 2
+// of 320 (ten warps: one round of line transforms fewer when the plan has
+// 17 to 20 modes), and the item
 // grouping of the multi-output x passes (1, one y row of tiles, four rows).
 // Each candidate runs twice (the first run compiles and warms up); the
 // second is timed with CUDA events on the stream.  The plan's spectrum and
@@ -820,16 +822,19 @@ int aar_autotune(aar_plan* h, char* report, int32_t len, void* stream) {
   if (p->prm.precision != AAR_FUSED_FP32) return set_err(p, "the autotuner is for the fused form"), AAR_ERR_ARG;
   cudaStream_t st = S(stream);
   struct Cand {
-    int jit, minb;
+    int jit, minb, threads;
     int64_t grp;
     float ms;
   };
   const int64_t row_tiles = p->HP / 8;
+  // (row kernel, blocks per SM, threads per block); 320 threads only where
+  // ten warps take the M input lines in fewer rounds than eight
+  std::vector<int3> rows = {{0, 2, 256}, {2, 2, 256}, {2, 3, 256}};
+  if ((p->M + 9) / 10 < (p->M + 7) / 8) rows.push_back({2, 2, 320});
   std::vector<Cand> cands;
-  for (int j = 0; j < 3; ++j)
-    for (int64_t g : {(int64_t)1, row_tiles, 4 * row_tiles})
-      cands.push_back(Cand{j == 0 ? 0 : 2, j == 2 ? 3 : 2, g, -1.f});
-  const int saved_mode = p->jit_mode, saved_minb = p->jit_minb;
+  for (const int3& r : rows)
+    for (int64_t g : {(int64_t)1, row_tiles, 4 * row_tiles}) cands.push_back(Cand{r.x, r.y, r.z, g, -1.f});
+  const int saved_mode = p->jit_mode, saved_minb = p->jit_minb, saved_threads = p->jit_threads;
   const int64_t saved_grp = p->xpass_group;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   AAR_CUDA_TRY(p, cudaEventCreate(&e0));
@@ -839,6 +844,7 @@ int aar_autotune(aar_plan* h, char* report, int32_t len, void* stream) {
     Cand& c = cands[i];
     p->jit_mode = c.jit;
     p->jit_minb = c.minb;
+    p->jit_threads = c.threads;
     p->xpass_group = c.grp;
     if ((rc = jit_prepare(p))) break;
     if (c.jit && p->jit == nullptr) continue;  // NVRTC unavailable: no such candidate
@@ -860,12 +866,14 @@ int aar_autotune(aar_plan* h, char* report, int32_t len, void* stream) {
   if (rc || best < 0) {
     p->jit_mode = saved_mode;
     p->jit_minb = saved_minb;
+    p->jit_threads = saved_threads;
     p->xpass_group = saved_grp;
     jit_prepare(p);
     return rc ? rc : (set_err(p, "autotune: no candidate ran"), AAR_ERR_STATE);
   }
   p->jit_mode = cands[best].jit;
   p->jit_minb = cands[best].minb;
+  p->jit_threads = cands[best].threads;
   p->xpass_group = cands[best].grp;
   if ((rc = jit_prepare(p))) return rc;
   ++p->generation;
@@ -874,8 +882,8 @@ int aar_autotune(aar_plan* h, char* report, int32_t len, void* stream) {
     char line[160];
     for (size_t i = 0; i < cands.size(); ++i) {
       const Cand& c = cands[i];
-      snprintf(line, sizeof(line), "%s rows=%s minb=%d group=%lld %.3f ms\n", (int)i == best ? "*" : " ",
-               c.jit ? "nvrtc" : "generic", c.jit ? c.minb : 0, (long long)c.grp, c.ms);
+      snprintf(line, sizeof(line), "%s rows=%s minb=%d threads=%d group=%lld %.3f ms\n", (int)i == best ? "*" : " ",
+               c.jit ? "nvrtc" : "generic", c.jit ? c.minb : 0, c.threads, (long long)c.grp, c.ms);
       out += line;
     }
     if ((int)out.size() + 1 > len) return set_err(p, "autotune report buffer too small"), AAR_ERR_ARG;

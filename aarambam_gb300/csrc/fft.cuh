@@ -228,15 +228,17 @@ __device__ __forceinline__ void unroll_br(F&& f) {
 // One Stockham stage on the values a lane holds: v[b*R + r] = x[j + r N/R],
 // j = t + T b.  On return v[b*R + r] = y[(j/Ns) Ns R + j%Ns + r Ns].  When Ns
 // divides T the twiddle exponent k = j mod Ns = t mod Ns is the same for
-// every group b, so the R - 1 twiddles are loaded once per stage.
-template <int N, int T, int R, int Ns, int SIGN>
+// every group b, so the R - 1 twiddles are loaded once per stage.  The table
+// tw holds exp(-2 pi i m / (N TWS)); TWS > 1 reads a longer line's table
+// with stride TWS.
+template <int N, int T, int R, int Ns, int SIGN, int TWS = 1>
 __device__ __forceinline__ void stage_compute(float2* v, int t, const float2* __restrict__ tw) {
   constexpr int E = N / T;
   if constexpr (Ns > 1 && T % Ns == 0 && E / R > 1) {
     const int k = t % Ns;
     float2 w[R];
 #pragma unroll
-    for (int r = 1; r < R; ++r) w[r] = tw_load<SIGN>(tw, r * k * (N / (Ns * R)));
+    for (int r = 1; r < R; ++r) w[r] = tw_load<SIGN>(tw, r * k * (N / (Ns * R)) * TWS);
 #pragma unroll
     for (int b = 0; b < E / R; ++b) {
 #pragma unroll
@@ -250,7 +252,8 @@ __device__ __forceinline__ void stage_compute(float2* v, int t, const float2* __
       if constexpr (Ns > 1) {
         int k = j % Ns;
 #pragma unroll
-        for (int r = 1; r < R; ++r) v[b * R + r] = cmul(v[b * R + r], tw_load<SIGN>(tw, r * k * (N / (Ns * R))));
+        for (int r = 1; r < R; ++r)
+          v[b * R + r] = cmul(v[b * R + r], tw_load<SIGN>(tw, r * k * (N / (Ns * R)) * TWS));
       }
       DFT<R, SIGN>::run(v + b * R);
     }
@@ -292,7 +295,8 @@ __device__ __forceinline__ void line_sync(int bar_id) {
 // SCALE multiplies the values of the first stage as they are loaded (line
 // element t + T b + r N/R sits at v[b R + r]) by sc[b R + r] (SCALE 1) or by
 // i sc[b R + r] (SCALE 2): a per-element filter folded into the transform.
-template <int N, int T, int SIGN, int S = 0, int SCALE = 0>
+// TWS: twiddle-table stride (tw of a line TWS times longer).
+template <int N, int T, int SIGN, int S = 0, int SCALE = 0, int TWS = 1>
 __device__ __forceinline__ void line_fft_smem(float2* s, int t, const float2* __restrict__ tw, bool act,
                                               int bar_id = 1, const float* sc = nullptr) {
   constexpr int E = N / T;
@@ -309,11 +313,11 @@ __device__ __forceinline__ void line_fft_smem(float2* s, int t, const float2* __
     }
     line_sync<T>(bar_id);
     if (act) {
-      stage_compute<N, T, R, Ns, SIGN>(v, t, tw);
+      stage_compute<N, T, R, Ns, SIGN, TWS>(v, t, tw);
       stage_store<N, T, R, Ns>(v, s, t);
     }
     line_sync<T>(bar_id);
-    line_fft_smem<N, T, SIGN, S + 1, 0>(s, t, tw, act, bar_id);
+    line_fft_smem<N, T, SIGN, S + 1, 0, TWS>(s, t, tw, act, bar_id);
   }
 }
 

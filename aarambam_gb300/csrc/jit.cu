@@ -31,9 +31,11 @@ struct JitState {
   std::string key;        // N, M and the term structure the module was made for
   size_t smem = 0;
   int nterms = 0;
+  int threads = kRowThreadsHost;  // block size the module was compiled for
 };
 
-static std::string gen_source(int N, int M, int minb, int pairs, const TermList& tl, const std::vector<Term>& terms) {
+static std::string gen_source(int N, int M, int minb, int threads, int pairs, const TermList& tl,
+                              const std::vector<Term>& terms) {
   std::string s;
   // kCoef at global scope: its symbol name is not mangled (cudaLibraryGetGlobal)
   s += "#include \"rows.cuh\"\n";
@@ -69,10 +71,11 @@ static std::string gen_source(int N, int M, int minb, int pairs, const TermList&
     s += "#pragma unroll\n      for (int i = 0; i < K; ++i) sm[" + std::to_string(r) + " * LS + pos[i]] = a[i];\n    }\n";
   }
   s += "  }\n};\n}  // namespace aar\n";
-  s += "extern \"C\" __global__ void __launch_bounds__(aar::kRowThreads, " + std::to_string(minb) +
+  s += "extern \"C\" __global__ void __launch_bounds__(" + std::to_string(threads) + ", " + std::to_string(minb) +
        ") aar_modal_rows_jit(float2* work, long long fs, int HP, const float2* __restrict__ twN, "
        "const float2* __restrict__ twH) {\n";
-  s += "  aar::rows_body<" + std::to_string(N) + ">(aar::JitRowOp{}, work, fs, HP, twN, twH);\n}\n";
+  s += "  aar::rows_body<" + std::to_string(N) + ", aar::JitRowOp, " + std::to_string(threads) +
+       ">(aar::JitRowOp{}, work, fs, HP, twN, twH);\n}\n";
   return s;
 }
 
@@ -102,17 +105,18 @@ int jit_prepare(Plan* p) {
   std::vector<Term> terms(ft, ft + tl.nterms);
   const int N = p->N, M = p->M;
   const int minb = p->jit_minb > 0 ? p->jit_minb : (N >= 1024 ? 2 : 3);
-  const int regcap = 65536 / (kRowThreadsHost * minb);
+  const int threads = p->jit_threads > 0 ? p->jit_threads : kRowThreadsHost;
+  const int regcap = 65536 / (threads * minb);
   const int pairs = 2 * 2 * M + 16 <= regcap * 3 / 4;  // f values of two positions fit the register budget
   std::string key = std::to_string(N) + ":" + std::to_string(M) + ":" + std::to_string(minb) + ":" +
-                    std::to_string(pairs) + ":";
+                    std::to_string(threads) + ":" + std::to_string(pairs) + ":";
   for (const Term& t : terms) key += std::to_string(t.p) + "," + std::to_string(t.q) + "," + std::to_string(t.r) + ";";
   std::vector<float> coef(terms.size());
   for (size_t i = 0; i < terms.size(); ++i) coef[i] = terms[i].c;
   JitState* j = (JitState*)p->jit;
   if (!j || j->key != key) {
     jit_free(p);
-    const std::string src = gen_source(N, M, minb, pairs, tl, terms);
+    const std::string src = gen_source(N, M, minb, threads, pairs, tl, terms);
     nvrtcProgram prog;
     const char* hdrs[2] = {kEmbedFft, kEmbedRows};
     const char* names[2] = {"fft.cuh", "rows.cuh"};
@@ -153,6 +157,7 @@ int jit_prepare(Plan* p) {
     }
     j->key = key;
     j->nterms = (int)terms.size();
+    j->threads = threads;
     p->jit = j;
   }
   j->smem = sizeof(float2) * (size_t)(M + 1) * p->row_ls;
@@ -176,7 +181,7 @@ int jit_modal_rows(Plan* p, float2* work, int64_t fs, cudaStream_t st) {
   {
     ProfScope ps_(p, "modal_rows", st);
     AAR_CUDA_TRY(p, cudaLaunchKernel((const void*)j->kern, dim3((unsigned)((int64_t)p->N * p->N)),
-                                     dim3(kRowThreadsHost), args, j->smem, st));
+                                     dim3(j->threads), args, j->smem, st));
   }
   p->last_launches += 1;
   return AAR_OK;

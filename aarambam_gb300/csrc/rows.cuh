@@ -138,6 +138,104 @@ __device__ __forceinline__ void row_r2c_post(const float2* line, float2* __restr
   }
 }
 
+// ---------------------------------------------------------------------
+// Rows of N = 1024 (half-length H = 512) fold the radix-2 step of the
+// half-length transform into the c2r pre-step and the r2c post-step, so a
+// line takes two shared-memory stages (two H/2-point transforms of radix
+// 16 x 16 on the half-warps) instead of three (16 x 16 x 2).  Lane `lane`
+// of the warp owns the quads of positions k, h-k, h+k, H-k (h = H/2,
+// k = lane + 32 i <= H/4); the quads partition 0..H, so the steps work in
+// place without a barrier.
+//
+// Inverse: Z_n from X (the pre-step), then decimation in frequency:
+// u_n = Z_n + Z_{n+h} to position n and (Z_n - Z_{n+h}) e^{2 pi i n/H} to
+// n + h, n < h.  Inverse h-point transforms of the two halves leave z_{2m}
+// at m and z_{2m+1} at h + m (z_n = (x_{2n}, x_{2n+1})): the line's samples
+// in a permuted order, which the pointwise combine does not see.
+// Forward, from that order: E_k (first half) and O_k (second half) after
+// the h-point transforms, Z_k = E_k + e^{-2 pi i k/H} O_k and Z_{k+h} =
+// E_k - e^{-2 pi i k/H} O_k, then the post-step X_k from Z_k, Z_{H-k}.
+template <int N>
+struct RowFold {
+  static constexpr bool value = N == 1024;
+};
+
+// Z_j of the c2r pre-step from a = X_j, b = X_{H-j}, w = e^{+2 pi i j/N}:
+// E + i O with E = a + conj b, O = (a - conj b) w
+__device__ __forceinline__ float2 pre1(float2 a, float2 b, float2 w) {
+  const float2 e = make_float2(a.x + b.x, a.y - b.y);
+  const float2 o = cmul(make_float2(a.x - b.x, a.y + b.y), w);
+  return make_float2(e.x - o.y, e.y + o.x);
+}
+// X_j of the r2c post-step from z = Z_j, zr = Z_{H-j}, w = e^{-2 pi i j/N}
+__device__ __forceinline__ float2 post1(float2 z, float2 zr, float2 w) {
+  const float2 e = make_float2(0.5f * (z.x + zr.x), 0.5f * (z.y - zr.y));
+  const float2 od = cmul(make_float2(0.5f * (z.x - zr.x), 0.5f * (z.y + zr.y)), w);
+  return make_float2(e.x + od.y, e.y - od.x);
+}
+
+template <int N>
+__device__ __forceinline__ void row_c2r_pre_fold(float2* line, int lane, const float2* __restrict__ twN,
+                                                 const float2* __restrict__ twH, ZFac zf) {
+  constexpr int H = N / 2, h = H / 2, Q = H / 4;
+  for (int k = lane; k <= Q; k += 32) {
+    const float2 wk = __ldg(twN + k);  // e^{-2 pi i k/N}
+    const float2 vk = __ldg(twH + k);  // e^{-2 pi i k/H}
+    float2 a = line[spad(k)], b = line[spad(H - k)], c = line[spad(h - k)], d = line[spad(h + k)];
+    if (zf.type) {
+      a = cscale(a, zf.at(k));
+      b = cscale(b, zf.at(H - k));
+      c = cscale(c, zf.at(h - k));
+      d = cscale(d, zf.at(h + k));
+    }
+    if (k == 0) {  // FFTW c2r: Im X_0, Im X_{N/2} dropped
+      a.y = 0.f;
+      b.y = 0.f;
+    }
+    // e^{+2 pi i j/N} at j = k, H-k, h-k, h+k: conj w, -w, i w, i conj w
+    const float2 zk = pre1(a, b, make_float2(wk.x, -wk.y));
+    const float2 zHk = pre1(b, a, make_float2(-wk.x, -wk.y));
+    const float2 zhm = pre1(c, d, make_float2(-wk.y, wk.x));
+    const float2 zhp = k == 0 ? zhm : pre1(d, c, make_float2(wk.y, wk.x));
+    // butterflies n = k and n = h - k; e^{2 pi i n/H}: conj v, -v
+    line[spad(k)] = cadd(zk, zhp);
+    line[spad(h + k)] = cmul(csub(zk, zhp), make_float2(vk.x, -vk.y));
+    if (k != 0 && k != Q) {
+      line[spad(h - k)] = cadd(zhm, zHk);
+      line[spad(H - k)] = cmul(csub(zhm, zHk), make_float2(-vk.x, -vk.y));
+    }
+  }
+}
+
+template <int N>
+__device__ __forceinline__ void row_r2c_post_fold(const float2* line, float2* __restrict__ X, int lane,
+                                                  const float2* __restrict__ twN, const float2* __restrict__ twH) {
+  constexpr int H = N / 2, h = H / 2, Q = H / 4;
+  for (int k = lane; k <= Q; k += 32) {
+    const float2 wk = __ldg(twN + k);
+    const float2 vk = __ldg(twH + k);
+    const float2 ek = line[spad(k)], ok = cmul(line[spad(h + k)], vk);
+    const float2 zk = cadd(ek, ok), zhp = csub(ek, ok);
+    if (k == 0) {
+      // Z_0 = E_0 + O_0 = Z_H, Z_h = E_0 - O_0
+      X[0] = post1(zk, zk, wk);
+      X[H] = post1(zk, zk, make_float2(-1.f, 0.f));
+      X[h] = post1(zhp, zhp, make_float2(0.f, -1.f));
+      continue;
+    }
+    // Z_{h-k} = E_{h-k} - conj(v) O_{h-k}, Z_{H-k} = E_{h-k} + conj(v) O_{h-k}
+    const float2 em = line[spad(h - k)], om = cmul(line[spad(H - k)], make_float2(vk.x, -vk.y));
+    const float2 zhm = csub(em, om), zHk = cadd(em, om);
+    // e^{-2 pi i j/N} at j = k, H-k, h-k, h+k: w, -conj w, -i conj w, -i w
+    X[k] = post1(zk, zHk, wk);
+    X[H - k] = post1(zHk, zk, make_float2(-wk.x, wk.y));
+    if (k != Q) {
+      X[h - k] = post1(zhm, zhp, make_float2(-wk.y, -wk.x));
+      X[h + k] = post1(zhp, zhm, make_float2(wk.y, -wk.x));
+    }
+  }
+}
+
 // Generic row kernel.  For each memory row (blockIdx.x): c2r of `nin`
 // input fields (slots in_slot[]), a per-position combine step Op, r2c of
 // `nout` output lines into slots out_slot[].  One warp per line at a time.
@@ -145,7 +243,7 @@ __device__ __forceinline__ void row_r2c_post(const float2* line, float2* __restr
 // phase barrier (its last round of lines keeps only some warps busy) the
 // other block's warps issue.
 constexpr int kRowThreads = 256;
-template <int N, class Op>
+template <int N, class Op, int THREADS = kRowThreads>
 __device__ __forceinline__ void rows_body(const Op& op, float2* work, int64_t fs, int HP,
                                           const float2* __restrict__ twN, const float2* __restrict__ twH) {
   using C = RowCfg<N>;
@@ -153,7 +251,7 @@ __device__ __forceinline__ void rows_body(const Op& op, float2* work, int64_t fs
   extern __shared__ float2 sm[];
   int64_t row = blockIdx.x;
   int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  constexpr int nwarps = kRowThreads / 32;
+  constexpr int nwarps = THREADS / 32;
   int sub = lane / C::T, t = lane % C::T;
   // phase 0: stage X_0..X_{N/2} of every input line at once (one exposed
   // memory latency per row instead of one per line; staging round by round
@@ -161,11 +259,41 @@ __device__ __forceinline__ void rows_body(const Op& op, float2* work, int64_t fs
   for (int l = 0; l < op.nin(); ++l) {
     const float2* X = work + (int64_t)op.in_slot(l) * fs + row * HP;
     float2* line = sm + l * C::LS;
-    for (int k = threadIdx.x; k <= H; k += kRowThreads) cp_async8(line + spad(k), X + k);
+    for (int k = threadIdx.x; k <= H; k += THREADS) cp_async8(line + spad(k), X + k);
   }
   cp_async_commit();
   cp_async_wait<0>();
   __syncthreads();
+  if constexpr (RowFold<N>::value) {
+    static_assert(C::T == 32 && H == 512, "folded rows: one warp per 512-point half line");
+    constexpr int h = H / 2, HO = h + h / 16;  // spad(h + i) = spad(i) + HO
+    const int half = lane >> 4, t16 = lane & 15;
+    for (int l = warp; l < op.nin(); l += nwarps) {
+      float2* line = sm + l * C::LS;
+      if constexpr (Op::kZfac) row_c2r_pre_fold<N>(line, lane, twN, twH, op.zfac(l));
+      else row_c2r_pre_fold<N>(line, lane, twN, twH, ZFac{0, 0.f, nullptr});
+      __syncwarp();
+      line_fft_smem<h, 16, +1, 0, 0, 2>(line + half * HO, t16, twH, true);
+    }
+    __syncthreads();
+    for (int n = threadIdx.x; n < H; n += (Op::kPairs ? 2 : 1) * THREADS) {
+      if (Op::kPairs && n + THREADS < H) {
+        const int pos[2] = {spad(n), spad(n + THREADS)};
+        op.template combine<2>(sm, pos, C::LS);
+      } else {
+        const int pos[1] = {spad(n)};
+        op.template combine<1>(sm, pos, C::LS);
+      }
+    }
+    __syncthreads();
+    for (int l = warp; l < op.nout(); l += nwarps) {
+      float2* line = sm + op.out_line(l) * C::LS;
+      line_fft_smem<h, 16, -1, 0, 0, 2>(line + half * HO, t16, twH, true);
+      row_r2c_post_fold<N>(line, work + (int64_t)op.out_slot(l) * fs + row * HP, lane, twN, twH);
+      __syncwarp();
+    }
+    return;
+  }
   // phase 1: inverse transforms
   for (int l0 = warp * C::LPW; l0 < op.nin(); l0 += nwarps * C::LPW) {
     int l = l0 + sub;
@@ -180,9 +308,9 @@ __device__ __forceinline__ void rows_body(const Op& op, float2* work, int64_t fs
   }
   __syncthreads();
   // phase 2: per position combine (in place in the line buffers)
-  for (int n = threadIdx.x; n < H; n += (Op::kPairs ? 2 : 1) * kRowThreads) {
-    if (Op::kPairs && n + kRowThreads < H) {
-      const int pos[2] = {spad(n), spad(n + kRowThreads)};
+  for (int n = threadIdx.x; n < H; n += (Op::kPairs ? 2 : 1) * THREADS) {
+    if (Op::kPairs && n + THREADS < H) {
+      const int pos[2] = {spad(n), spad(n + THREADS)};
       op.template combine<2>(sm, pos, C::LS);
     } else {
       const int pos[1] = {spad(n)};

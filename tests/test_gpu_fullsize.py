@@ -78,3 +78,48 @@ def test_fused_vs_plain_fp64_512(cuda):
     want = dspl(pp)
     err = torch.linalg.vector_norm(dspl(pf) - want) / torch.linalg.vector_norm(want)
     assert float(err) < 1e-5
+
+
+def test_fused_vs_plain_fp64_1024(cuda):
+    """The 1024^3 bench workload (20-mode ScalarI table): fused FP32 particles
+    through the NVRTC row kernel and through the generic one, against the
+    plain FP64 GPU form.  Rows of N = 1024 fold the radix-2 step of the
+    half-length transform into the c2r pre- and r2c post-steps, so this is
+    the one size that runs those steps."""
+    N = 1024
+    tab, M = "scalarI_m20_L1000_n1024", 20
+    cfg = make_cfg(N, 1000.0, 77, 100.0, M, tab, 1024)
+    a, x0 = table(tab, M)
+    k, t = bbks()
+    g = torch.arange(N, device=cuda, dtype=torch.float32) * (1000.0 / N)
+    gx, gy, gz = torch.meshgrid(g, g, g, indexing="ij")
+    lagr = torch.stack([gx.reshape(-1), gy.reshape(-1), gz.reshape(-1)], 1).contiguous()
+    del gx, gy, gz
+    gf = ICGenerator(cfg, a, x0, k, t)
+    assert gf.jit_status == "on"
+    pj, _ = gf.run(lagr)
+    gf.set_jit(0)
+    pg, _ = gf.run(lagr)
+    gf.close()
+    del gf
+    torch.cuda.empty_cache()
+    gp = ICGenerator(cfg, a, x0, k, t, precision="fp64")
+    pp, _ = gp.run(lagr)
+    gp.close()
+    del gp
+    torch.cuda.empty_cache()
+
+    def rel(p):
+        num = den = 0.0
+        for s in range(0, lagr.shape[0], 1 << 25):
+            sl = slice(s, s + (1 << 25))
+            L = lagr[sl].double()
+            w = pp[sl].double() - L
+            w -= 1000.0 * torch.round(w / 1000.0)
+            d = p[sl].double() - L
+            d -= 1000.0 * torch.round(d / 1000.0)
+            num += float(torch.sum((d - w) ** 2))
+            den += float(torch.sum(w ** 2))
+        return (num / den) ** 0.5
+    assert rel(pj) < 1e-5
+    assert rel(pg) < 1e-5

@@ -62,9 +62,11 @@ def test_jit_vs_oracle_small(cuda):
 
 
 def test_autotune_picks_a_schedule_and_keeps_results(cuda):
-    """The autotuner times nine schedules (row kernel generic / NVRTC with 2
-    or 3 blocks per SM x three x-pass item groupings), keeps the fastest, and
-    the particles afterwards agree with the default schedule's."""
+    """The autotuner times its schedules (row kernel generic / NVRTC with 2
+    or 3 blocks per SM of 256 threads / NVRTC with 2 blocks of 320 threads
+    when ten warps need fewer rounds over the M = 10 input lines than eight,
+    x three x-pass item groupings), keeps the fastest, and the particles
+    afterwards agree with the default schedule's."""
     import torch
     from tests.common import bbks, make_cfg, table
     from aarambam_gb300.ic import ICGenerator
@@ -76,7 +78,8 @@ def test_autotune_picks_a_schedule_and_keeps_results(cuda):
     pos0, vel0 = g.run(lagr)
     rep = g.autotune()
     lines = [l for l in rep.splitlines() if l.strip()]
-    assert len(lines) == 9 and sum(l.startswith("*") for l in lines) == 1
+    assert len(lines) == 12 and sum(l.startswith("*") for l in lines) == 1
+    assert sum("threads=320" in l for l in lines) == 3
     pos1, vel1 = g.run(lagr)
     d0 = (pos0 - lagr).double()
     d1 = (pos1 - lagr).double()

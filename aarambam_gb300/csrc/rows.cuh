@@ -174,14 +174,22 @@ __device__ __forceinline__ float2 post1(float2 z, float2 zr, float2 w) {
   return make_float2(e.x + od.y, e.y - od.x);
 }
 
-template <int N>
+// X from the line buffer (in place, GLOBAL false) or from the row in global
+// memory (GLOBAL true, `src`)
+template <int N, bool GLOBAL = false>
 __device__ __forceinline__ void row_c2r_pre_fold(float2* line, int lane, const float2* __restrict__ twN,
-                                                 const float2* __restrict__ twH, ZFac zf) {
+                                                 const float2* __restrict__ twH, ZFac zf,
+                                                 const float2* __restrict__ src = nullptr) {
   constexpr int H = N / 2, h = H / 2, Q = H / 4;
   for (int k = lane; k <= Q; k += 32) {
     const float2 wk = __ldg(twN + k);  // e^{-2 pi i k/N}
     const float2 vk = __ldg(twH + k);  // e^{-2 pi i k/H}
-    float2 a = line[spad(k)], b = line[spad(H - k)], c = line[spad(h - k)], d = line[spad(h + k)];
+    float2 a, b, c, d;
+    if constexpr (GLOBAL) {
+      a = src[k], b = src[H - k], c = src[h - k], d = src[h + k];
+    } else {
+      a = line[spad(k)], b = line[spad(H - k)], c = line[spad(h - k)], d = line[spad(h + k)];
+    }
     if (zf.type) {
       a = cscale(a, zf.at(k));
       b = cscale(b, zf.at(H - k));

@@ -42,10 +42,11 @@ def _stale(obj: str, src: str) -> bool:
 
 def _embed_headers() -> None:
     """_build/jit_embed.h: the device headers the run-time specialised row
-    kernel is compiled from (jit.cu), as raw string literals."""
+    and accumulation kernels are compiled from (jit.cu), as raw string
+    literals."""
     out = os.path.join(OUT, "jit_embed.h")
-    parts = ["// generated by build.py from csrc/fft.cuh and csrc/rows.cuh\n#pragma once\n"]
-    for var, name in (("kEmbedFft", "fft.cuh"), ("kEmbedRows", "rows.cuh")):
+    parts = ["// generated by build.py from csrc/fft.cuh, csrc/rows.cuh and csrc/cells.cuh\n#pragma once\n"]
+    for var, name in (("kEmbedFft", "fft.cuh"), ("kEmbedRows", "rows.cuh"), ("kEmbedCells", "cells.cuh")):
         with open(os.path.join(CSRC, name)) as f:
             text = f.read()
         if ")AARJIT\"" in text:

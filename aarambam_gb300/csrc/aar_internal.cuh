@@ -8,61 +8,11 @@
 #include <vector>
 
 #include "../../include/aarambam.h"
+#include "cells.cuh"
 
 namespace aar {
 
 constexpr int kRowThreadsHost = 256;  // block size of the row kernels (rows.cuh kRowThreads)
-constexpr double kPi = 3.14159265358979323846;  // PI as the reference defines it
-
-// signed wavenumber index of grid index i (main.c:410-423): N/2 -> -N/2
-__host__ __device__ __forceinline__ int sidx(int i, int N) { return i < N / 2 ? i : i - N; }
-
-// Row order of the fused form's fields.  A field (complex half-spectrum or
-// real) is N^2 rows of HP complex / 2 HP real values, one row per (x, y);
-// the row of (x, y) is row_of(x, y, N, xb), i.e. x is split into blocks of
-// xb: [x / xb][y][x % xb].  With xb = kXB the N rows of an x line lie in
-// N / kXB groups of kXB rows 4*HP bytes apart, instead of N rows N*HP*8 bytes
-// apart: measured on GB300 at N = 1024, a tile copy with the x-pass pattern
-// ran at 3.4 TB/s in natural order and 6.7 TB/s blocked (xb = 4 to 64),
-// while the y-pass pattern stayed at 7.0-7.2 TB/s for xb <= 8.  xb = 1 is
-// the natural [x][y] order of the reference and of the C-ABI's buffers.
-constexpr int kXB = 4;
-__host__ __device__ __forceinline__ int64_t row_of(int x, int y, int N, int xb) {
-  return ((int64_t)(x / xb) * N + y) * xb + x % xb;
-}
-__host__ __device__ __forceinline__ void row_xy(int64_t m, int N, int xb, int& x, int& y) {
-  const int64_t q = m / xb;
-  x = (int)((q / N) * xb + m % xb);
-  y = (int)(q % N);
-}
-
-// Geometry and scalars of one plan, passed by value to kernels.
-struct Grid {
-  int N;       // Nmesh
-  int HP;      // padded half-spectrum row length (complex entries), >= N/2+1
-  int kcut;    // cube mode: keep |k index| <= kcut on every axis
-  int sphere;  // SphereMode
-  int nsq_bnd; // sphere mode: (Nsample/2)^2, the only n^2 whose keep depends on rounding
-  int nsample_half;
-  double box;
-  float kF;    // 2 pi / Box
-};
-
-// Keep / cut decision of the reference (main.c:428-441, :591-604), exact.
-// Cube mode reduces to an integer bound on each axis (host-computed).  In
-// sphere mode only n^2 == (Nsample/2)^2 sits on the rounding boundary; those
-// cells repeat the reference's FP64 expression with unfused operations.
-__device__ __forceinline__ bool keep_cell(const Grid& g, int kx, int ky, int kz) {
-  if (!g.sphere) return abs(kx) <= g.kcut && abs(ky) <= g.kcut && abs(kz) <= g.kcut;
-  int n2 = kx * kx + ky * ky + kz * kz;
-  if (n2 != g.nsq_bnd) return n2 < g.nsq_bnd;
-  double fx = __ddiv_rn(__dmul_rn((double)(2 * kx), kPi), g.box);
-  double fy = __ddiv_rn(__dmul_rn((double)(2 * ky), kPi), g.box);
-  double fz = __ddiv_rn(__dmul_rn((double)(2 * kz), kPi), g.box);
-  double k2 = __dadd_rn(__dadd_rn(__dmul_rn(fx, fx), __dmul_rn(fy, fy)), __dmul_rn(fz, fz));
-  double km = __dsqrt_rn(k2);
-  return !(__ddiv_rn(__dmul_rn(km, g.box), __dmul_rn(2.0, kPi)) > (double)g.nsample_half);
-}
 
 // Host twin of keep_cell's cube bound.
 int host_kcut(int nsample, double box);
@@ -194,6 +144,10 @@ int copy_rows(Plan* p, void* dst, int64_t dst_ld, int dst_xb, const void* src, i
 int noalloc_gaussian(Plan* p, void* d_out, cudaStream_t st);
 int jit_prepare(Plan* p);
 int jit_modal_rows(Plan* p, float2* work, int64_t fs, cudaStream_t st);
+// the specialised modal accumulation of the same module; false when the
+// plan has none (the generic k_modal_acc runs)
+bool jit_has_acc(const Plan* p);
+int jit_modal_acc(Plan* p, float2* phi, const float2* work, float fnl_n3, const RhoArgs& ra, cudaStream_t st);
 void jit_free(Plan* p);
 int adj_spectral(Plan* p, int op, int comp, int mode, const float2* in, float2* out, int accumulate,
                  cudaStream_t st);

@@ -132,17 +132,6 @@ __device__ __forceinline__ void tile_fft(float2* sm, const float2* __restrict__ 
   line_fft_smem<N, C::T, SIGN, 0, SCALE>(sm + (act ? line : 0) * C::LS, t, tw, act, 1 + (act ? line : 0), sc);
 }
 
-// rho_n(k) of the accumulation evaluated per cell (main.c:825-860):
-// k^(s (n-3)) for n <= 3, (P_{n-1}(kbar) - X0[n-1]) / k^2 above, with
-// kbar = -1 + 2 (k^s - kmin^s)/(kmax^s - kmin^s); kmin = kF, so
-// k^s - kmin^s = kmin^s expm1(s ln(sqrt(n^2))) (no cancellation near kmin),
-// and P_l by the Bonnet recurrence P_l = A_l kbar P_{l-1} - B_l P_{l-2}.
-struct RhoArgs {
-  float s, c1, log2kF, inv_kF2;  // c1 = 2 kmin^s / (kmax^s - kmin^s)
-  float x0[kMaxModes];
-  float A[kMaxModes], B[kMaxModes];  // (2l-1)/l, (l-1)/l
-};
-
 // Last modal step, after the forward x transform of every active slot r:
 // acc = sum_r rho_r(k) g_r(k) (rho_r computed per cell in FP32, RhoArgs;
 // Neumaier-compensated in registers), then phi <- phi + fnl_n3 * acc,
@@ -637,6 +626,7 @@ struct Launch {
       if ((rc = run_pass<N>(p, xf, p->nr_active * tiles(p), st, "modal_xfwd"))) return rc;
     }
     float fnl_n3 = (float)(p->prm.fnl / ((double)N * N * N));
+    if (jit_has_acc(p)) return jit_modal_acc(p, p->d_phik, p->d_work, fnl_n3, rho_args(p), st);
     {
       ProfScope ps_(p, "modal_acc", st);
       k_modal_acc<N><<<(unsigned)(p->num_sms * 8), 256, 0, st>>>(a, p->d_phik, p->d_work, fs, p->HP, fnl_n3,

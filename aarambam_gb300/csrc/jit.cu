@@ -19,7 +19,7 @@
 #include <vector>
 
 #include "aar_internal.cuh"
-#include "jit_embed.h"  // kEmbedFft, kEmbedRows (generated by build.py)
+#include "jit_embed.h"  // kEmbedFft, kEmbedRows, kEmbedCells (generated by build.py)
 #include "spectral.cuh"
 
 namespace aar {
@@ -32,6 +32,9 @@ struct JitState {
   size_t smem = 0;
   int nterms = 0;
   int threads = kRowThreadsHost;  // block size the module was compiled for
+  cudaKernel_t acc = nullptr;      // aar_modal_acc_jit, or null
+  int acc_blocks = 0;              // its resident blocks per SM
+  int64_t acc_fs = 0;              // field stride it was compiled for
 };
 
 static std::string gen_source(int N, int M, int minb, int threads, int pairs, const TermList& tl,
@@ -79,6 +82,56 @@ static std::string gen_source(int N, int M, int minb, int threads, int pairs, co
   return s;
 }
 
+// The modal accumulation of k_modal_acc (fused.cu) for this plan's active
+// slots: the slot list, the recurrence steps between slots and the field
+// offsets are compile-time, so the slot loop is straight-line code whose
+// loads all issue before the sums (the generic kernel reads the slot list
+// from shared memory and walks it with a runtime loop).  Same arithmetic in
+// the same order as the generic kernel.
+static std::string gen_acc(int N, int HP, const TermList& tl) {
+  const long long fs = (long long)N * N * HP;
+  std::string s;
+  s += "extern \"C\" __global__ void __launch_bounds__(256) aar_modal_acc_jit(aar::Grid g, float2* phi, "
+       "const float2* __restrict__ work, float fnl_n3, aar::RhoArgs ra) {\n";
+  s += "  constexpr int N = " + std::to_string(N) + ", K = N / 2 + 1, HP = " + std::to_string(HP) + ";\n";
+  s += "  constexpr long long total = (long long)N * N * K;\n";
+  s += "  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;"
+       " i += (long long)gridDim.x * blockDim.x) {\n";
+  s += "    const long long row = i / K;\n    const int kz = (int)(i - row * K);\n    const long long e = row * HP + kz;\n";
+  s += "    int x, y;\n    aar::row_xy(row, N, aar::kXB, x, y);\n";
+  s += "    const int kx = aar::sidx(x, N), ky = aar::sidx(y, N);\n    const int n2 = kx * kx + ky * ky + kz * kz;\n";
+  s += "    if (n2 == 0) {\n      phi[e] = make_float2(0.f, 0.f);\n      continue;\n    }\n";
+  s += "    if (!aar::keep_cell(g, kx, ky, kz)) continue;\n";
+  s += "    const float2* w = work + e;\n";
+  for (int j = 0; j < tl.nr; ++j)
+    s += "    const float2 v" + std::to_string(j) + " = __ldg(w + " + std::to_string((long long)tl.r_of_slot[j] * fs) +
+         "LL);\n";
+  s += "    const float lnn2 = logf((float)n2);\n";
+  s += "    const float kbar = -1.f + ra.c1 * expm1f(0.5f * ra.s * lnn2);\n";
+  s += "    const float L = ra.log2kF + lnn2 * 0.72134752044448170368f;\n";
+  s += "    const float inv_k2 = ra.inv_kF2 / (float)n2;\n";
+  s += "    float P0 = 1.f, P1 = kbar, Pn, rho;\n    float sx = 0.f, sy = 0.f, cx = 0.f, cy = 0.f;\n";
+  int deg = 1;
+  for (int j = 0; j < tl.nr; ++j) {
+    const int r = tl.r_of_slot[j];
+    if (r <= 3) {
+      s += r == 3 ? "    rho = 1.f;\n" : "    rho = exp2f(ra.s * (float)(" + std::to_string(r - 3) + ") * L);\n";
+    } else {
+      for (; deg < r - 1; ) {
+        ++deg;
+        const std::string d = std::to_string(deg);
+        s += "    Pn = ra.A[" + d + "] * kbar * P1 - ra.B[" + d + "] * P0;\n    P0 = P1;\n    P1 = Pn;\n";
+      }
+      s += "    rho = (P1 - ra.x0[" + std::to_string(r - 1) + "]) * inv_k2;\n";
+    }
+    s += "    aar::neumaier_add(sx, cx, v" + std::to_string(j) + ".x * rho);\n";
+    s += "    aar::neumaier_add(sy, cy, v" + std::to_string(j) + ".y * rho);\n";
+  }
+  s += "    float2 ph = phi[e];\n    ph.x += fnl_n3 * (sx + cx);\n    ph.y += fnl_n3 * (sy + cy);\n    phi[e] = ph;\n";
+  s += "  }\n}\n";
+  return s;
+}
+
 static void jit_release(JitState* j) {
   if (!j) return;
   if (j->lib) cudaLibraryUnload(j->lib);
@@ -116,11 +169,12 @@ int jit_prepare(Plan* p) {
   JitState* j = (JitState*)p->jit;
   if (!j || j->key != key) {
     jit_free(p);
-    const std::string src = gen_source(N, M, minb, threads, pairs, tl, terms);
+    const std::string src = "#include \"cells.cuh\"\n" + gen_source(N, M, minb, threads, pairs, tl, terms) +
+                            gen_acc(N, p->HP, tl);
     nvrtcProgram prog;
-    const char* hdrs[2] = {kEmbedFft, kEmbedRows};
-    const char* names[2] = {"fft.cuh", "rows.cuh"};
-    if (nvrtcCreateProgram(&prog, src.c_str(), "aar_modal_rows_jit.cu", 2, hdrs, names) != NVRTC_SUCCESS) {
+    const char* hdrs[3] = {kEmbedFft, kEmbedRows, kEmbedCells};
+    const char* names[3] = {"fft.cuh", "rows.cuh", "cells.cuh"};
+    if (nvrtcCreateProgram(&prog, src.c_str(), "aar_modal_rows_jit.cu", 3, hdrs, names) != NVRTC_SUCCESS) {
       p->jit_status = "nvrtcCreateProgram failed";
       return AAR_OK;
     }
@@ -158,6 +212,14 @@ int jit_prepare(Plan* p) {
     j->key = key;
     j->nterms = (int)terms.size();
     j->threads = threads;
+    // the accumulation kernel is optional: without it the generic one runs
+    if (cudaLibraryGetKernel(&j->acc, j->lib, "aar_modal_acc_jit") != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&j->acc_blocks, (const void*)j->acc, 256, 0) != cudaSuccess ||
+        j->acc_blocks < 1) {
+      cudaGetLastError();
+      j->acc = nullptr;
+    }
+    j->acc_fs = (int64_t)N * N * p->HP;
     p->jit = j;
   }
   j->smem = sizeof(float2) * (size_t)(M + 1) * p->row_ls;
@@ -182,6 +244,25 @@ int jit_modal_rows(Plan* p, float2* work, int64_t fs, cudaStream_t st) {
     ProfScope ps_(p, "modal_rows", st);
     AAR_CUDA_TRY(p, cudaLaunchKernel((const void*)j->kern, dim3((unsigned)((int64_t)p->N * p->N)),
                                      dim3(j->threads), args, j->smem, st));
+  }
+  p->last_launches += 1;
+  return AAR_OK;
+}
+
+bool jit_has_acc(const Plan* p) {
+  const JitState* j = (const JitState*)p->jit;
+  return j && j->acc && j->acc_fs == (int64_t)p->N * p->N * p->HP;
+}
+
+int jit_modal_acc(Plan* p, float2* phi, const float2* work, float fnl_n3, const RhoArgs& ra, cudaStream_t st) {
+  JitState* j = (JitState*)p->jit;
+  Grid g = p->grid;
+  RhoArgs r = ra;
+  void* args[] = {&g, &phi, &work, &fnl_n3, &r};
+  {
+    ProfScope ps_(p, "modal_acc", st);
+    AAR_CUDA_TRY(p, cudaLaunchKernel((const void*)j->acc, dim3((unsigned)(p->num_sms * j->acc_blocks)), dim3(256), args,
+                                     0, st));
   }
   p->last_launches += 1;
   return AAR_OK;

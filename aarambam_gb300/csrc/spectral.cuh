@@ -10,7 +10,6 @@ struct Term {      // one product f_p f_q with coefficient c into g_r
   float c;
 };
 
-constexpr int kMaxModes = 32;
 constexpr int kMaxTerms = 2048;
 
 struct TermList {

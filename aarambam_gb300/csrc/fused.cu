@@ -483,6 +483,9 @@ __device__ __forceinline__ void readout_one(const ReadArgs& a, const float* __re
   }
 }
 
+// One particle per thread.  (Measured at 1024^3 on a lattice: four
+// particles per thread with 16-byte loads and stores, 79 registers and three
+// blocks per SM, 27.0 vs 19.6 ms.)
 __global__ void __launch_bounds__(256, 6) k_readout(ReadArgs a, const float* __restrict__ F, const float* __restrict__ lagr, int64_t np,
                           float* pos, float* vel) {
   int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;

@@ -254,9 +254,9 @@ int aar_batch_launch_count(const aar_batch* batch);
 const char* aar_batch_last_error(const aar_batch* batch);
 void aar_batch_destroy(aar_batch* batch);
 
-/* Run-time specialised modal row kernel (no counterpart in the reference):
-   mode 0 off, 1 (default) for Nmesh >= 256, 2 always.  The kernel is
-   compiled with NVRTC for the plan's alpha-term structure when the tables
+/* Run-time specialised modal row and accumulation kernels (no counterpart
+   in the reference): mode 0 off, 1 (default) for Nmesh >= 256, 2 always.
+   Both are compiled with NVRTC for the plan's alpha-term structure when the tables
    are set (a new table with the same nonzero pattern only updates its
    coefficients); when compiling or loading fails the generic kernel stays
    in use and aar_jit_status says why ("on", "off" or the reason). */
@@ -265,7 +265,8 @@ const char* aar_jit_status(const aar_plan* plan);
 
 /* Schedule autotuner (no counterpart in the reference): times the field
    stages of this plan on its device for each candidate schedule -- the row
-   kernel generic or NVRTC-specialised with 2 or 3 resident blocks per SM,
+   kernel generic or NVRTC-specialised with 2 or 3 resident blocks per SM of
+   256 threads (or 2 of 320 where ten warps need fewer rounds over the modes),
    and the item grouping of the multi-output x passes -- and keeps the
    fastest for the plan's later runs.  Needs tables and transfer function;
    overwrites the plan's spectrum and fields.  `report` (may be NULL)

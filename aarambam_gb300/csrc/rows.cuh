@@ -247,9 +247,10 @@ __device__ __forceinline__ void row_r2c_post_fold(const float2* line, float2* __
 // Generic row kernel.  For each memory row (blockIdx.x): c2r of `nin`
 // input fields (slots in_slot[]), a per-position combine step Op, r2c of
 // `nout` output lines into slots out_slot[].  One warp per line at a time.
-// THREADS = 256 with two resident blocks per SM: while one block waits at a
-// phase barrier (its last round of lines keeps only some warps busy) the
-// other block's warps issue.
+// THREADS = 256 (the library's kernels; the NVRTC kernel may use 320) with
+// two resident blocks per SM: while one block waits at a phase barrier (its
+// last round of lines keeps only some warps busy) the other block's warps
+// issue.
 constexpr int kRowThreads = 256;
 template <int N, class Op, int THREADS = kRowThreads>
 __device__ __forceinline__ void rows_body(const Op& op, float2* work, int64_t fs, int HP,

@@ -264,23 +264,27 @@ __device__ __forceinline__ void rows_body(const Op& op, float2* work, int64_t fs
   int sub = lane / C::T, t = lane % C::T;
   // phase 0: stage X_0..X_{N/2} of every input line at once (one exposed
   // memory latency per row instead of one per line; staging round by round
-  // with a barrier per round measured slower: 148 vs 141 ms at 1024^3)
-  for (int l = 0; l < op.nin(); ++l) {
-    const float2* X = work + (int64_t)op.in_slot(l) * fs + row * HP;
-    float2* line = sm + l * C::LS;
-    for (int k = threadIdx.x; k <= H; k += THREADS) cp_async8(line + spad(k), X + k);
+  // with a barrier per round measured slower: 148 vs 141 ms at 1024^3).
+  // The folded rows read X in their pre-step straight from global memory.
+  if constexpr (!RowFold<N>::value) {
+    for (int l = 0; l < op.nin(); ++l) {
+      const float2* X = work + (int64_t)op.in_slot(l) * fs + row * HP;
+      float2* line = sm + l * C::LS;
+      for (int k = threadIdx.x; k <= H; k += THREADS) cp_async8(line + spad(k), X + k);
+    }
+    cp_async_commit();
+    cp_async_wait<0>();
+    __syncthreads();
   }
-  cp_async_commit();
-  cp_async_wait<0>();
-  __syncthreads();
   if constexpr (RowFold<N>::value) {
     static_assert(C::T == 32 && H == 512, "folded rows: one warp per 512-point half line");
     constexpr int h = H / 2, HO = h + h / 16;  // spad(h + i) = spad(i) + HO
     const int half = lane >> 4, t16 = lane & 15;
     for (int l = warp; l < op.nin(); l += nwarps) {
       float2* line = sm + l * C::LS;
-      if constexpr (Op::kZfac) row_c2r_pre_fold<N>(line, lane, twN, twH, op.zfac(l));
-      else row_c2r_pre_fold<N>(line, lane, twN, twH, ZFac{0, 0.f, nullptr});
+      const float2* X = work + (int64_t)op.in_slot(l) * fs + row * HP;
+      if constexpr (Op::kZfac) row_c2r_pre_fold<N, true>(line, lane, twN, twH, op.zfac(l), X);
+      else row_c2r_pre_fold<N, true>(line, lane, twN, twH, ZFac{0, 0.f, nullptr}, X);
       __syncwarp();
       line_fft_smem<h, 16, +1, 0, 0, 2>(line + half * HO, t16, twH, true);
     }

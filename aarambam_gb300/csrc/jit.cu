@@ -158,7 +158,12 @@ int jit_prepare(Plan* p) {
   std::vector<Term> terms(ft, ft + tl.nterms);
   const int N = p->N, M = p->M;
   const int minb = p->jit_minb > 0 ? p->jit_minb : (N >= 1024 ? 2 : 3);
-  const int threads = p->jit_threads > 0 ? p->jit_threads : kRowThreadsHost;
+  // default block size: 320 threads (ten warps) at N = 1024 where they take
+  // the M input lines in fewer rounds than eight warps (measured at 1024^3,
+  // 20 modes: 362 vs 372 ms per step); the autotuner may choose otherwise
+  const int threads = p->jit_threads > 0                                   ? p->jit_threads
+                      : (N >= 1024 && (M + 9) / 10 < (M + 7) / 8) ? 320
+                                                                       : kRowThreadsHost;
   const int regcap = 65536 / (threads * minb);
   const int pairs = 2 * 2 * M + 16 <= regcap * 3 / 4;  // f values of two positions fit the register budget
   std::string key = std::to_string(N) + ":" + std::to_string(M) + ":" + std::to_string(minb) + ":" +

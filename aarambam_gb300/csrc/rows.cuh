@@ -46,7 +46,10 @@ struct ZFac {
 template <int N>
 struct RowCfg {
   static constexpr int H = N / 2;             // complex FFT length
-  static constexpr int T = lanes_for(H);
+  // 16 values per lane from H = 256 up (two stages of 16 x 16 at H = 256,
+  // measured 6.2 vs 7.3 ms for the modal rows at 512^3; at H = 128 eight
+  // lanes per line made the 256^3 batch slower, 139 vs 127 ms)
+  static constexpr int T = H == 256 ? 16 : lanes_for(H);
   static constexpr int LPW = 32 / T;
   static constexpr int LS = spad_len(H);
 };

@@ -20,13 +20,15 @@ AAR_ERR_TRANSFER = 1111
 AAR_ERR_TRANSFER_DUP = 777
 AAR_FUSED_FP32 = 0
 AAR_PLAIN_FP64 = 1
+AAR_PLAIN_FP64_REGROUPED = 2
 AAR_VARIANT_BASIS = 0
 AAR_VARIANT_RESBASIS = 1
 
 # every symbol include/aarambam.h declares
 EXPORTS = [
     "aar_plan_create", "aar_set_tables", "aar_set_transfer", "aar_get_scalars", "aar_set_seed", "aar_run",
-    "aar_run_glass", "aar_run_host", "aar_seedtable", "aar_stage_noise", "aar_stage_modal", "aar_stage_lpt",
+    "aar_run_glass", "aar_run_host", "aar_run_glass_host", "aar_run_glass_host_async", "aar_wait_host_copies",
+    "aar_plan_prepare", "aar_plan_device_bytes", "aar_seedtable", "aar_stage_noise", "aar_stage_modal", "aar_stage_lpt",
     "aar_stage_readout", "aar_stage_readout_glass", "aar_copy_spectrum", "aar_copy_field", "aar_gaussian_spectrum_noalloc", "aar_c2r", "aar_r2c", "aar_last_launch_count", "aar_profile_enable", "aar_profile_report",
     "aar_last_error", "aar_plan_destroy", "aar_version",
     "aar_batch_create", "aar_batch_run", "aar_batch_launch_count", "aar_batch_last_error", "aar_batch_destroy",
@@ -89,6 +91,12 @@ def load(build_if_missing: bool = False):
     L.aar_run.argtypes = [vp, vp, i64, vp, vp, vp]
     L.aar_run_glass.argtypes = [vp, vp, i64, C.c_double, i32, vp, vp, vp, vp]
     L.aar_run_host.argtypes = [vp, vp, i64, vp, vp, vp]
+    L.aar_run_glass_host.argtypes = [vp, vp, i64, C.c_double, i32, vp, vp, vp, vp]
+    L.aar_run_glass_host_async.argtypes = [vp, vp, i64, C.c_double, i32, vp, vp, vp, vp]
+    L.aar_wait_host_copies.argtypes = [vp]
+    L.aar_plan_prepare.argtypes = [vp]
+    L.aar_plan_device_bytes.argtypes = [vp]
+    L.aar_plan_device_bytes.restype = i64
     L.aar_seedtable.argtypes = [vp, vp, vp]
     for n in ("aar_stage_noise", "aar_stage_modal", "aar_stage_lpt"):
         getattr(L, n).argtypes = [vp, vp]

@@ -106,6 +106,18 @@ struct Plan {
   int out_chunks = kOutChunks;  // chunks of the host read-out (1: one copy after the read-out)
   cudaStream_t out_stream[2] = {nullptr, nullptr};
   cudaEvent_t chunk_read[kOutChunks] = {}, out_done[2] = {nullptr, nullptr};
+  // host-buffer glass runs: device glass, full-size Pos/Vel/ID staging, and
+  // per chunk the event after its copy-out (the next read-out of the chunk
+  // waits for it)
+  float* d_glass = nullptr;
+  int64_t glass_cap = 0;
+  double* d_gscale = nullptr;  // glass_prepare: 3 nglass + tile products (read_glass.c:129-214)
+  int64_t gscale_cap = 0;
+  float* d_gout = nullptr;  // [npart][3] pos, then [npart][3] vel, then npart int32 ids
+  int64_t gout_cap = 0;
+  int64_t gout_last = -1;   // particle count of the last host-buffer glass call
+  static constexpr int kGlassChunks = 16;
+  cudaEvent_t gchunk_read[kGlassChunks] = {}, gchunk_free[kGlassChunks] = {};
 };
 
 // Records CUDA events around the kernels launched in its scope (when the
@@ -131,10 +143,20 @@ int fused_prepare(Plan* p);
 int fused_modal(Plan* p, cudaStream_t st);
 int fused_lpt(Plan* p, cudaStream_t st);
 int fused_readout(Plan* p, const float* d_lagr, int64_t npart, float* d_pos, float* d_vel, cudaStream_t st);
-int fused_readout_glass(Plan* p, const float* d_glass, int64_t nglass, double glass_box, int tile, float* d_pos,
-                        float* d_vel, int* d_ids, cudaStream_t st);
+// glass_prepare makes the per-glass-particle and per-tile products of the
+// Lagrangian positions (plan-owned scratch); fused_readout_glass then reads
+// out particles n0 <= n < n1 (n1 < 0: all)
+int glass_prepare(Plan* p, const float* d_glass, int64_t nglass, double glass_box, int tile, cudaStream_t st);
+int fused_readout_glass(Plan* p, int64_t nglass, int tile, float* d_pos, float* d_vel, int* d_ids, cudaStream_t st,
+                        int64_t n0 = 0, int64_t n1 = -1);
 int plain_run(Plan* p, const float* d_lagr, int64_t npart, float* d_pos, float* d_vel, cudaStream_t st);
+int plain_setup(Plan* p);
+int plain_copy_field(Plan* p, int which, double* out, cudaStream_t st);
+int plain_copy_spectrum(Plan* p, void* out, cudaStream_t st);
 void plain_free(Plan* p);
+inline bool is_plain(const aar_params& q) {
+  return q.precision == AAR_PLAIN_FP64 || q.precision == AAR_PLAIN_FP64_REGROUPED;
+}
 int fused_c2r(Plan* p, const float2* in, float* out, cudaStream_t st);
 int fused_r2c(Plan* p, const float* in, float2* out, cudaStream_t st);
 int fused_configure_xform(Plan* p);

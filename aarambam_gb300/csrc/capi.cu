@@ -193,8 +193,11 @@ static int set_transfer(Plan* p, const double* k, const double* t, int n) {
             p->D0;
   p->have_transfer = true;
 
-  // per-n^2 tables for the FP32 form: noise amplitude and T / (D Beta)
+  // per-n^2 tables for the FP32 form: noise amplitude and T / (D Beta),
+  // rewritten with synchronous copies (ordered only against the legacy
+  // stream): runs in flight on other streams finish first
   if (p->prm.precision == AAR_FUSED_FP32) {
+    AAR_CUDA_TRY(p, cudaDeviceSynchronize());
     int N = p->N;
     int64_t nsq = 3LL * (N / 2) * (N / 2) + 1;
     std::vector<float> amp(nsq), twb(nsq);
@@ -264,6 +267,19 @@ static void plan_release(Plan* p) {
     if (p->chunk_read[i]) cudaEventDestroy(p->chunk_read[i]);
     p->chunk_read[i] = nullptr;
   }
+  for (int i = 0; i < Plan::kGlassChunks; ++i) {
+    if (p->gchunk_read[i]) cudaEventDestroy(p->gchunk_read[i]);
+    if (p->gchunk_free[i]) cudaEventDestroy(p->gchunk_free[i]);
+    p->gchunk_read[i] = p->gchunk_free[i] = nullptr;
+  }
+  if (p->d_glass) cudaFree(p->d_glass);
+  if (p->d_gout) cudaFree(p->d_gout);
+  if (p->d_gscale) cudaFree(p->d_gscale);
+  p->d_gscale = nullptr;
+  p->gscale_cap = 0;
+  p->d_glass = nullptr;
+  p->d_gout = nullptr;
+  p->glass_cap = p->gout_cap = 0;
   plain_free(p);
 }
 
@@ -351,11 +367,10 @@ static int create(Plan* p) {
   const aar_params& q = p->prm;
   int N = q.nmesh;
   if (q.nsample > q.nmax) return set_err(p, "Nmax must be >= Nsample (main.c:200)"), AAR_ERR_NMAX;
-  if (q.precision != AAR_FUSED_FP32 && q.precision != AAR_PLAIN_FP64)
-    return set_err(p, "unknown precision"), AAR_ERR_ARG;
+  if (q.precision != AAR_FUSED_FP32 && !is_plain(q)) return set_err(p, "unknown precision"), AAR_ERR_ARG;
   if (q.precision == AAR_FUSED_FP32 && !(pow2(N) && N >= 16 && N <= 1024))
     return set_err(p, "fused FP32 form supports Nmesh = 16..1024, powers of two"), AAR_ERR_ARG;
-  if (q.precision == AAR_PLAIN_FP64 && !(N >= 4 && N % 2 == 0 && N <= 2048))
+  if (is_plain(q) && !(N >= 4 && N % 2 == 0 && N <= 2048))
     return set_err(p, "plain FP64 form supports even Nmesh up to 2048"), AAR_ERR_ARG;
   if (!(q.box > 0) || q.nsample <= 0) return set_err(p, "Box and Nsample must be positive"), AAR_ERR_ARG;
   if (q.seed < 0) return set_err(p, "Seed must be >= 0"), AAR_ERR_ARG;
@@ -492,6 +507,8 @@ const char* aar_last_error(const aar_plan* h) { return h ? h->p.err.c_str() : "n
 
 int aar_last_launch_count(const aar_plan* h) { return h ? h->p.last_launches : 0; }
 
+int64_t aar_plan_device_bytes(const aar_plan* h) { return h ? (int64_t)h->p.used_bytes : 0; }
+
 int aar_set_tables(aar_plan* h, const double* alpha, const double* x0, int32_t M) {
   if (!h) return AAR_ERR_ARG;
   Plan* p = &h->p;
@@ -502,6 +519,10 @@ int aar_set_tables(aar_plan* h, const double* alpha, const double* x0, int32_t M
   for (int i = 0; i < M; ++i)
     if (!isfinite(x0[i])) return set_err(p, "non-finite X0 coefficient"), AAR_ERR_ARG;
   ++p->generation;
+  // the term list and the NVRTC module's coefficients are rewritten below
+  // with synchronous copies that are ordered only against the legacy stream:
+  // wait for runs still in flight on other streams (or in batch graphs)
+  AAR_CUDA_TRY(p, cudaDeviceSynchronize());
   p->alpha.assign(alpha, alpha + n3);
   p->x0.assign(x0, x0 + M);
   p->M = M;
@@ -516,6 +537,15 @@ int aar_set_tables(aar_plan* h, const double* alpha, const double* x0, int32_t M
   }
   p->have_tables = true;
   return AAR_OK;
+}
+
+int aar_plan_prepare(aar_plan* h) {
+  if (!h) return AAR_ERR_ARG;
+  Plan* p = &h->p;
+  int rc = ready(p);
+  if (rc) return rc;
+  if (is_plain(p->prm)) return plain_setup(p);
+  return AAR_OK;  // the fused form allocates its fields with the tables
 }
 
 int aar_set_transfer(aar_plan* h, const double* k, const double* t, int32_t n) {
@@ -590,7 +620,9 @@ int aar_stage_readout_glass(aar_plan* h, const float* d_glass, int64_t nglass, d
   Plan* p = &h->p;
   if (p->prm.precision != AAR_FUSED_FP32) return set_err(p, "stage calls are for the fused form"), AAR_ERR_ARG;
   p->last_launches = 0;
-  return fused_readout_glass(p, d_glass, nglass, glass_box, tile, d_pos, d_vel, d_ids, S(stream));
+  int rc = glass_prepare(p, d_glass, nglass, glass_box, tile, S(stream));
+  if (rc) return rc;
+  return fused_readout_glass(p, nglass, tile, d_pos, d_vel, d_ids, S(stream));
 }
 
 int aar_run(aar_plan* h, const float* d_lagr, int64_t npart, float* d_pos, float* d_vel, void* stream) {
@@ -600,7 +632,7 @@ int aar_run(aar_plan* h, const float* d_lagr, int64_t npart, float* d_pos, float
   if (rc) return rc;
   p->last_launches = 0;
   cudaStream_t st = S(stream);
-  if (p->prm.precision == AAR_PLAIN_FP64) return plain_run(p, d_lagr, npart, d_pos, d_vel, st);
+  if (is_plain(p->prm)) return plain_run(p, d_lagr, npart, d_pos, d_vel, st);
   if ((rc = run_noise(p, st))) return rc;
   if ((rc = fused_modal(p, st))) return rc;
   if ((rc = fused_lpt(p, st))) return rc;
@@ -619,7 +651,31 @@ int aar_run_glass(aar_plan* h, const float* d_glass, int64_t nglass, double glas
   if ((rc = run_noise(p, st))) return rc;
   if ((rc = fused_modal(p, st))) return rc;
   if ((rc = fused_lpt(p, st))) return rc;
-  return fused_readout_glass(p, d_glass, nglass, glass_box, tile, d_pos, d_vel, d_ids, st);
+  if ((rc = glass_prepare(p, d_glass, nglass, glass_box, tile, st))) return rc;
+  return fused_readout_glass(p, nglass, tile, d_pos, d_vel, d_ids, st);
+}
+
+static int run_glass_host(Plan* p, const float* h_glass, int64_t nglass, double glass_box, int tile, float* h_pos,
+                          float* h_vel, int32_t* h_ids, cudaStream_t st, bool sync);
+
+int aar_run_glass_host(aar_plan* h, const float* h_glass, int64_t nglass, double glass_box, int32_t tile,
+                       float* h_pos, float* h_vel, int32_t* h_ids, void* stream) {
+  if (!h || nglass < 0 || tile < 1 || !(glass_box > 0)) return AAR_ERR_ARG;
+  return run_glass_host(&h->p, h_glass, nglass, glass_box, tile, h_pos, h_vel, h_ids, S(stream), true);
+}
+
+int aar_run_glass_host_async(aar_plan* h, const float* h_glass, int64_t nglass, double glass_box, int32_t tile,
+                             float* h_pos, float* h_vel, int32_t* h_ids, void* stream) {
+  if (!h || nglass < 0 || tile < 1 || !(glass_box > 0)) return AAR_ERR_ARG;
+  return run_glass_host(&h->p, h_glass, nglass, glass_box, tile, h_pos, h_vel, h_ids, S(stream), false);
+}
+
+int aar_wait_host_copies(aar_plan* h) {
+  if (!h) return AAR_ERR_ARG;
+  Plan* p = &h->p;
+  for (int i = 0; i < 2; ++i)
+    if (p->out_done[i]) AAR_CUDA_TRY(p, cudaEventSynchronize(p->out_done[i]));
+  return AAR_OK;
 }
 
 int aar_run_host(aar_plan* h, const float* h_lagr, int64_t npart, float* h_pos, float* h_vel, void* stream) {
@@ -642,7 +698,7 @@ int aar_run_host(aar_plan* h, const float* h_lagr, int64_t npart, float* h_pos, 
   float* d_in = p->d_io;
   float* d_pos = d_in + 3 * (size_t)npart;
   float* d_vel = d_pos + 3 * (size_t)npart;
-  if (p->prm.precision == AAR_PLAIN_FP64) {
+  if (is_plain(p->prm)) {
     if (npart > 0) AAR_CUDA_TRY(p, cudaMemcpyAsync(d_in, h_lagr, bytes, cudaMemcpyHostToDevice, st));
     if ((rc = aar_run(h, d_in, npart, d_pos, d_vel, stream))) return rc;
   } else {
@@ -700,9 +756,96 @@ int aar_run_host(aar_plan* h, const float* h_lagr, int64_t npart, float* h_pos, 
   return AAR_OK;
 }
 
+// Host-buffer glass run (aar_run_glass_host / _async).  Read-out in chunks
+// of particles; chunk c goes to the host on side stream c % 2 as soon as it
+// is read out.  Chunk c's staging is reused by the next call only after the
+// event recorded behind its copy (gchunk_free[c]): a never-recorded event is
+// already complete, so the first call waits for nothing.
+static int run_glass_host(Plan* p, const float* h_glass, int64_t nglass, double glass_box, int tile, float* h_pos,
+                          float* h_vel, int32_t* h_ids, cudaStream_t st, bool sync) {
+  int rc = ready(p);
+  if (rc) return rc;
+  if (p->prm.precision != AAR_FUSED_FP32) return set_err(p, "aar_run_glass_host is for the fused form"), AAR_ERR_ARG;
+  const int64_t t3 = (int64_t)tile * tile * tile;
+  const int64_t npart = nglass * t3;
+  if (npart > 0 && (!h_glass || !h_pos || !h_vel)) return set_err(p, "null host buffer"), AAR_ERR_ARG;
+  if (nglass > p->glass_cap) {
+    // the previous call's read-out may still read the old glass buffer
+    AAR_CUDA_TRY(p, cudaStreamSynchronize(st));
+    if (p->d_glass) cudaFree(p->d_glass), p->used_bytes -= sizeof(float) * 3 * (size_t)p->glass_cap;
+    p->d_glass = nullptr;
+    p->glass_cap = 0;
+    if ((rc = plan_alloc(p, (void**)&p->d_glass, sizeof(float) * 3 * (size_t)nglass))) return rc;
+    p->glass_cap = nglass;
+  }
+  const size_t per = sizeof(float) * 6 + sizeof(int32_t);
+  if (npart > p->gout_cap) {
+    // staging still being copied out by an earlier asynchronous call
+    AAR_CUDA_TRY(p, cudaDeviceSynchronize());
+    if (p->d_gout) cudaFree(p->d_gout), p->used_bytes -= per * (size_t)p->gout_cap;
+    p->d_gout = nullptr;
+    p->gout_cap = 0;
+    if ((rc = plan_alloc(p, (void**)&p->d_gout, per * (size_t)npart))) return rc;
+    p->gout_cap = npart;
+  }
+  if (!p->out_stream[0]) {
+    for (int i = 0; i < 2; ++i) {
+      AAR_CUDA_TRY(p, cudaStreamCreateWithFlags(&p->out_stream[i], cudaStreamNonBlocking));
+      AAR_CUDA_TRY(p, cudaEventCreateWithFlags(&p->out_done[i], cudaEventDisableTiming));
+    }
+    for (int i = 0; i < Plan::kOutChunks; ++i)
+      AAR_CUDA_TRY(p, cudaEventCreateWithFlags(&p->chunk_read[i], cudaEventDisableTiming));
+  }
+  if (!p->gchunk_read[0])
+    for (int i = 0; i < Plan::kGlassChunks; ++i) {
+      AAR_CUDA_TRY(p, cudaEventCreateWithFlags(&p->gchunk_read[i], cudaEventDisableTiming));
+      AAR_CUDA_TRY(p, cudaEventCreateWithFlags(&p->gchunk_free[i], cudaEventDisableTiming));
+    }
+  float* d_pos = p->d_gout;
+  float* d_vel = d_pos + 3 * (size_t)npart;
+  int32_t* d_ids = h_ids ? (int32_t*)(d_vel + 3 * (size_t)npart) : nullptr;
+  p->last_launches = 0;
+  // the chunk hand-over assumes the previous call's staging layout; with
+  // another particle count, wait for all of its copies first
+  if (npart != p->gout_last && p->out_done[0])
+    for (int i = 0; i < 2; ++i) AAR_CUDA_TRY(p, cudaStreamWaitEvent(st, p->out_done[i], 0));
+  p->gout_last = npart;
+  if (nglass > 0)
+    AAR_CUDA_TRY(p, cudaMemcpyAsync(p->d_glass, h_glass, sizeof(float) * 3 * (size_t)nglass, cudaMemcpyHostToDevice, st));
+  if ((rc = run_noise(p, st))) return rc;
+  if ((rc = fused_modal(p, st))) return rc;
+  if ((rc = fused_lpt(p, st))) return rc;
+  if ((rc = glass_prepare(p, p->d_glass, nglass, glass_box, tile, st))) return rc;
+  const int nchunk = npart >= (int64_t)Plan::kGlassChunks * 65536 ? Plan::kGlassChunks : 1;
+  for (int c = 0; c < nchunk; ++c) {
+    const int64_t a = npart * c / nchunk, b = npart * (c + 1) / nchunk, cnt = b - a;
+    if (cnt == 0) continue;
+    AAR_CUDA_TRY(p, cudaStreamWaitEvent(st, p->gchunk_free[c], 0));
+    if ((rc = fused_readout_glass(p, nglass, tile, d_pos, d_vel, d_ids, st, a, b))) return rc;
+    cudaStream_t os = p->out_stream[c & 1];
+    AAR_CUDA_TRY(p, cudaEventRecord(p->gchunk_read[c], st));
+    AAR_CUDA_TRY(p, cudaStreamWaitEvent(os, p->gchunk_read[c], 0));
+    const size_t cb = sizeof(float) * 3 * (size_t)cnt;
+    AAR_CUDA_TRY(p, cudaMemcpyAsync(h_pos + 3 * a, d_pos + 3 * a, cb, cudaMemcpyDeviceToHost, os));
+    AAR_CUDA_TRY(p, cudaMemcpyAsync(h_vel + 3 * a, d_vel + 3 * a, cb, cudaMemcpyDeviceToHost, os));
+    if (h_ids)
+      AAR_CUDA_TRY(p, cudaMemcpyAsync(h_ids + a, d_ids + a, sizeof(int32_t) * (size_t)cnt, cudaMemcpyDeviceToHost, os));
+    AAR_CUDA_TRY(p, cudaEventRecord(p->gchunk_free[c], os));
+  }
+  // the copies stay on the side streams: the caller's stream goes on with
+  // the next realisation while they run (aar_wait_host_copies waits for them)
+  for (int i = 0; i < 2; ++i) AAR_CUDA_TRY(p, cudaEventRecord(p->out_done[i], p->out_stream[i]));
+  if (sync) {
+    AAR_CUDA_TRY(p, cudaStreamSynchronize(st));
+    for (int i = 0; i < 2; ++i) AAR_CUDA_TRY(p, cudaEventSynchronize(p->out_done[i]));
+  }
+  return AAR_OK;
+}
+
 int aar_copy_spectrum(aar_plan* h, void* d_out, void* stream) {
   if (!h || !d_out) return AAR_ERR_ARG;
   Plan* p = &h->p;
+  if (is_plain(p->prm)) return plain_copy_spectrum(p, d_out, S(stream));
   if (p->prm.precision != AAR_FUSED_FP32 || !p->d_phik) return set_err(p, "no FP32 spectrum in this plan"), AAR_ERR_STATE;
   const int H = p->N / 2 + 1;
   return copy_rows(p, d_out, H, 1, p->d_phik, p->HP, kXB, H, sizeof(float2), S(stream));
@@ -783,9 +926,10 @@ int aar_profile_report(aar_plan* h, char* buf, int32_t len) {
   return AAR_OK;
 }
 
-int aar_copy_field(aar_plan* h, int32_t which, float* d_out, void* stream) {
+int aar_copy_field(aar_plan* h, int32_t which, void* d_out, void* stream) {
   if (!h || !d_out || which < 0 || which > 5) return AAR_ERR_ARG;
   Plan* p = &h->p;
+  if (is_plain(p->prm)) return plain_copy_field(p, which, (double*)d_out, S(stream));
   if (p->prm.precision != AAR_FUSED_FP32 || !p->d_work) return set_err(p, "no FP32 fields in this plan"), AAR_ERR_STATE;
   int N = p->N;
   const float* src = (const float*)(p->d_work + (size_t)which * N * N * p->HP);
@@ -836,6 +980,9 @@ int aar_autotune(aar_plan* h, char* report, int32_t len, void* stream) {
     for (int64_t g : {(int64_t)1, row_tiles, 4 * row_tiles}) cands.push_back(Cand{r.x, r.y, r.z, g, -1.f});
   const int saved_mode = p->jit_mode, saved_minb = p->jit_minb, saved_threads = p->jit_threads;
   const int64_t saved_grp = p->xpass_group;
+  // every candidate may unload and reload the NVRTC module (jit_prepare), so
+  // graphs captured before this call are stale whatever the outcome
+  ++p->generation;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   AAR_CUDA_TRY(p, cudaEventCreate(&e0));
   AAR_CUDA_TRY(p, cudaEventCreate(&e1));
@@ -876,7 +1023,6 @@ int aar_autotune(aar_plan* h, char* report, int32_t len, void* stream) {
   p->jit_threads = cands[best].threads;
   p->xpass_group = cands[best].grp;
   if ((rc = jit_prepare(p))) return rc;
-  ++p->generation;
   if (report && len > 0) {
     std::string out;
     char line[160];

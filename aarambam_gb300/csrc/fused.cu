@@ -500,23 +500,32 @@ __global__ void __launch_bounds__(256, 6) k_readout(ReadArgs a, const float* __r
   }
 }
 
-// Lagrangian position of particle n from a glass tiled tile^3 times
-// (read_glass.c:129-214): FP64 with unfused operations, rounded to float.
-__global__ void k_readout_glass(ReadArgs a, const float* __restrict__ F, const float* __restrict__ glass,
-                                int64_t nglass, double glass_box, int tile, double box_over_tile, float* pos,
-                                float* vel, int* ids) {
-  int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  int64_t np = nglass * tile * tile * tile;
-  if (n >= np) return;
+// Lagrangian positions from a glass tiled tile^3 times (read_glass.c:129-214):
+// Pos = glass / glass_box * (Box / tile) + t * (Box / tile) in FP64 with
+// unfused operations, rounded to float.  The two products depend only on
+// the glass particle and on the tile index, so k_glass_scale makes them once
+// per call (3 nglass + tile doubles) and a particle costs one FP64 add per
+// axis (GB300's FP64 rate is a small fraction of its FP32 rate).
+__global__ void k_glass_scale(const float* __restrict__ glass, int64_t nglass, double glass_box, int tile,
+                              double box_over_tile, double* __restrict__ gs) {
+  const int64_t n = 3 * nglass + tile;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    gs[i] = i < 3 * nglass ? __dmul_rn(__ddiv_rn((double)glass[i], glass_box), box_over_tile)
+                           : __dmul_rn((double)(i - 3 * nglass), box_over_tile);
+}
+
+// Particles n0 <= n < n1 (indices of the whole tiled set, particle order of
+// read_glass.c:181-214: tile index outer, glass index inner).
+__global__ void k_readout_glass(ReadArgs a, const float* __restrict__ F, const double* __restrict__ gs,
+                                int64_t nglass, int tile, float* pos, float* vel, int* ids, int64_t n0, int64_t n1) {
+  int64_t n = n0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= n1) return;
   int64_t gi = n % nglass, t = n / nglass;
   int ti = (int)(t / ((int64_t)tile * tile)), tj = (int)((t / tile) % tile), tk = (int)(t % tile);
   int tt[3] = {ti, tj, tk};
+  const double* toff = gs + 3 * nglass;
   float lp[3];
-  for (int d = 0; d < 3; ++d) {
-    double x = __dadd_rn(__dmul_rn(__ddiv_rn((double)glass[3 * gi + d], glass_box), box_over_tile),
-                         __dmul_rn((double)tt[d], box_over_tile));
-    lp[d] = (float)x;
-  }
+  for (int d = 0; d < 3; ++d) lp[d] = (float)__dadd_rn(gs[3 * gi + d], toff[tt[d]]);
   float op[3], ov[3];
   readout_one(a, F, lp[0], lp[1], lp[2], op, ov);
   for (int d = 0; d < 3; ++d) {
@@ -830,15 +839,34 @@ int fused_readout(Plan* p, const float* d_lagr, int64_t npart, float* d_pos, flo
   return AAR_OK;
 }
 
-int fused_readout_glass(Plan* p, const float* d_glass, int64_t nglass, double glass_box, int tile, float* d_pos,
-                        float* d_vel, int* d_ids, cudaStream_t st) {
-  int64_t np = nglass * tile * tile * tile;
-  if (np == 0) return AAR_OK;
-  int bs = 256;
+int glass_prepare(Plan* p, const float* d_glass, int64_t nglass, double glass_box, int tile, cudaStream_t st) {
+  const int64_t need = 3 * nglass + tile;
+  if (need > p->gscale_cap) {
+    AAR_CUDA_TRY(p, cudaDeviceSynchronize());  // an earlier read-out may still read the old buffer
+    if (p->d_gscale) cudaFree(p->d_gscale), p->used_bytes -= sizeof(double) * (size_t)p->gscale_cap;
+    p->d_gscale = nullptr;
+    p->gscale_cap = 0;
+    int rc = plan_alloc(p, (void**)&p->d_gscale, sizeof(double) * (size_t)need);
+    if (rc) return rc;
+    p->gscale_cap = need;
+  }
+  k_glass_scale<<<(unsigned)std::min<int64_t>((need + 255) / 256, (int64_t)p->num_sms * 8), 256, 0, st>>>(
+      d_glass, nglass, glass_box, tile, p->prm.box / tile, p->d_gscale);
+  AAR_CUDA_TRY(p, cudaGetLastError());
+  p->last_launches += 1;
+  return AAR_OK;
+}
+
+int fused_readout_glass(Plan* p, int64_t nglass, int tile, float* d_pos, float* d_vel, int* d_ids, cudaStream_t st,
+                        int64_t n0, int64_t n1) {
+  const int64_t np = nglass * tile * tile * tile;
+  if (n1 < 0 || n1 > np) n1 = np;
+  if (n1 <= n0) return AAR_OK;
+  const int bs = 256;
+  const int64_t cnt = n1 - n0;
   { ProfScope ps_(p, "readout_glass", st);
-  k_readout_glass<<<(unsigned)((np + bs - 1) / bs), bs, 0, st>>>(read_args(p), (const float*)p->d_work, d_glass,
-                                                                  nglass, glass_box, tile, p->prm.box / tile, d_pos,
-                                                                  d_vel, d_ids);
+  k_readout_glass<<<(unsigned)((cnt + bs - 1) / bs), bs, 0, st>>>(read_args(p), (const float*)p->d_work, p->d_gscale,
+                                                                   nglass, tile, d_pos, d_vel, d_ids, n0, n1);
   }
   AAR_CUDA_TRY(p, cudaGetLastError());
   p->last_launches += 1;

@@ -286,7 +286,7 @@ int noalloc_gaussian(Plan* p, void* d_out, cudaStream_t st) {
                                                            (const U576*)p->d_rlxpow, 32, seed);
   AAR_CUDA_TRY(p, cudaGetLastError());
   const int hp = N / 2 + 1;
-  const bool fp64 = p->prm.precision == AAR_PLAIN_FP64;
+  const bool fp64 = is_plain(p->prm);
   AAR_CUDA_TRY(p, cudaMemsetAsync(d_out, 0, (fp64 ? sizeof(double2) : sizeof(float2)) * (size_t)total * hp, st));
   const unsigned nb = (unsigned)((total + 127) / 128);
   if (fp64)

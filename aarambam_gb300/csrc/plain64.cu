@@ -1,9 +1,20 @@
-// Plain FP64 form of the IC path: cuFFT Z2D / D2Z (in place, FFTW's padded
-// layout [N][N][2(N/2+1)]) and separate pointwise kernels, with the loop
-// structure of the reference kept 1:1 (Aarambam/LPT/Basis/main.c:564-1516):
-// one c2r per first index, c2r + product + r2c + accumulate per active pair,
-// the 10 counter-term pair transforms, the four potential round-trip
-// transforms, 6 + 1 + 6 transforms for 2LPT -- M + 2P + 41 in all.
+// Plain FP64 forms of the IC path: cuFFT Z2D / D2Z (in place, FFTW's padded
+// layout [N][N][2(N/2+1)]) and separate pointwise kernels.
+//
+// AAR_PLAIN_FP64 keeps the loop structure of the reference 1:1
+// (Aarambam/LPT/Basis/main.c:564-1516): one c2r per first index, c2r +
+// product + r2c + accumulate per active pair, the 10 counter-term pair
+// transforms, the four potential round-trip transforms, 6 + 1 + 6 transforms
+// for 2LPT -- M + 2P + 41 in all.
+//
+// AAR_PLAIN_FP64_REGROUPED is the same arithmetic in FP64 with the modal sum
+// regrouped exactly by linearity of the DFT, as the fused form does it:
+// M filtered c2r f_p, then per active r the real-space product
+// g_r = sum_{p<=q} a'_{pqr} f_p f_q (a' = alpha plus the counter-terms of
+// main.c:1045-1050), one r2c and acc += rho_r g_r; then phi += Fnl acc / N^3
+// without the potential round trips (main.c:1094-1150 are identities up to
+// rounding when the potential is not saved) -- at most 2M + 13 transforms.
+// It separates the gain of the regrouping from that of FP32 and fusion.
 //
 // cuFFT leaves the result of a Z2D on a half spectrum whose kz = 0 / N/2
 // planes are not Hermitian undefined, while FFTW's rfftwnd drops the parts
@@ -16,6 +27,7 @@
 #include <math.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <vector>
 
 #include "aar_internal.cuh"
@@ -25,7 +37,9 @@ namespace aar {
 struct PlainState {
   int N = 0, H = 0, M = 0;
   size_t nc = 0;                 // complex entries per field
-  double2* f[10] = {};           // fields
+  int nf = 0;                    // fields: 10 (reference structure) or max(10, M + 3) (regrouped)
+  double2* f[kMaxModes + 3] = {};
+  double2* disp[6] = {};         // after a run: ZA x, y, z and 2LPT x, y, z (real, padded rows)
   double* qin = nullptr;         // [M][nsq] field filters
   double* qout = nullptr;        // [M][nsq] radial parts rho_n
   double* twb = nullptr;         // [nsq] T(k) / (Dplus Beta)
@@ -33,6 +47,7 @@ struct PlainState {
   cufftHandle z2d = 0, d2z = 0;
   bool plans = false;
   int64_t nsq = 0;
+  size_t bytes = 0;              // device bytes allocated for this state (plan_alloc)
 };
 
 struct PArgs {
@@ -86,6 +101,45 @@ __global__ void kp_herm(PArgs a, double2* x) {
   double2 r = make_double2(0.5 * (u.x + v.x), 0.5 * (u.y - v.y));
   *p = r;
   *q = make_double2(r.x, -r.y);
+}
+
+// g (=|+=) sum_t c_t f_{p_t} f_{q_t} on the padded real layout: the products
+// of one output slot r of the regrouped modal sum (terms in chunks)
+constexpr int kProdChunk = 48;
+struct PTerms {
+  int n;
+  const double* fp[kProdChunk];
+  const double* fq[kProdChunk];
+  double c[kProdChunk];
+};
+__global__ void kp_products(PArgs a, PTerms t, double* g, int accumulate) {
+  int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t n3 = (int64_t)a.N * a.N * a.N;
+  if (c >= n3) return;
+  int64_t idx = (c / a.N) * 2 * a.H + c % a.N;
+  double v = accumulate ? g[idx] : 0.0;
+  for (int i = 0; i < t.n; ++i) v += t.c[i] * t.fp[i][idx] * t.fq[i][idx];
+  g[idx] = v;
+}
+
+// phi <- phi + fnl acc / n3, DC = 0: the combination of main.c:1104-1126
+// without the potential round trips
+__global__ void kp_combine_regrouped(PArgs a, double2* phi, const double2* __restrict__ acc, double fnl, double n3) {
+  int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= (int64_t)a.N * a.N * a.H) return;
+  double2 p = phi[c], q = acc[c];
+  p.x = p.x + fnl * q.x / n3;
+  p.y = p.y + fnl * q.y / n3;
+  if (c == 0) p = make_double2(0.0, 0.0);
+  phi[c] = p;
+}
+
+// real [N][N][N] <- padded real rows [N][N][2H] (copy of a displacement field)
+__global__ void kp_unpad(PArgs a, const double* __restrict__ in, double* out) {
+  int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t n3 = (int64_t)a.N * a.N * a.N;
+  if (c >= n3) return;
+  out[c] = in[(c / a.N) * 2 * a.H + c % a.N];
 }
 
 // real product fj <- fi * fj on the padded real layout (main.c:768-776)
@@ -251,8 +305,8 @@ static PlainState* st_of(Plan* p) { return (PlainState*)p->plain; }
 void plain_free(Plan* p) {
   PlainState* s = st_of(p);
   if (!s) return;
-  for (auto& f : s->f)
-    if (f) cudaFree(f);
+  for (int i = 0; i < s->nf; ++i)
+    if (s->f[i]) cudaFree(s->f[i]);
   if (s->qin) cudaFree(s->qin);
   if (s->qout) cudaFree(s->qout);
   if (s->twb) cudaFree(s->twb);
@@ -261,6 +315,7 @@ void plain_free(Plan* p) {
     cufftDestroy(s->z2d);
     cufftDestroy(s->d2z);
   }
+  p->used_bytes -= s->bytes;
   delete s;
   p->plain = nullptr;
 }
@@ -278,8 +333,11 @@ static double legendre64(int l, double x) {
   return p1;
 }
 
-static int plain_setup(Plan* p) {
+static bool regrouped(const Plan* p) { return p->prm.precision == AAR_PLAIN_FP64_REGROUPED; }
+
+int plain_setup(Plan* p) {
   if (p->plain) return AAR_OK;
+  if (!p->have_tables || !p->have_transfer) return set_err(p, "tables and transfer function must be set"), AAR_ERR_STATE;
   PlainState* s = new PlainState();
   p->plain = s;
   int N = p->N;
@@ -288,13 +346,19 @@ static int plain_setup(Plan* p) {
   s->M = p->M;
   s->nc = (size_t)N * N * s->H;
   s->nsq = 3LL * (N / 2) * (N / 2) + 1;
+  s->nf = regrouped(p) ? std::max(10, p->M + 3) : 10;
   int rc;
-  for (int i = 0; i < 10; ++i)
-    if ((rc = plan_alloc(p, (void**)&s->f[i], sizeof(double2) * s->nc))) return rc;
-  if ((rc = plan_alloc(p, (void**)&s->qin, sizeof(double) * s->nsq * s->M))) return rc;
-  if ((rc = plan_alloc(p, (void**)&s->qout, sizeof(double) * s->nsq * s->M))) return rc;
-  if ((rc = plan_alloc(p, (void**)&s->twb, sizeof(double) * s->nsq))) return rc;
-  if ((rc = plan_alloc(p, (void**)&s->sinc, sizeof(double) * N))) return rc;
+  auto alloc = [&](void** ptr, size_t bytes) {
+    int r = plan_alloc(p, ptr, bytes);
+    if (r == AAR_OK) s->bytes += bytes;
+    return r;
+  };
+  for (int i = 0; i < s->nf; ++i)
+    if ((rc = alloc((void**)&s->f[i], sizeof(double2) * s->nc))) return rc;
+  if ((rc = alloc((void**)&s->qin, sizeof(double) * s->nsq * s->M))) return rc;
+  if ((rc = alloc((void**)&s->qout, sizeof(double) * s->nsq * s->M))) return rc;
+  if ((rc = alloc((void**)&s->twb, sizeof(double) * s->nsq))) return rc;
+  if ((rc = alloc((void**)&s->sinc, sizeof(double) * N))) return rc;
   // host tables with the reference's formulas (main.c:580-637, :833-860)
   const double ns = p->prm.primordial_index, box = p->prm.box;
   const double kmin = 2 * kPi / box, kmax = 2 * kPi / box * p->prm.nmax;
@@ -352,6 +416,30 @@ static int plain_setup(Plan* p) {
     p->last_launches += 1;                                    \
   } while (0)
 
+// Regrouped modal sum (see the top of the file): per active r the sorted
+// triples p <= q <= r with alpha != 0 give a f_p f_q; the counter-terms of
+// main.c:1045-1050 add -a012 t012 f_0 f_1 to g_2 and +a012 t012 f_0 f_2 to
+// g_1 (FP64 coefficients).
+struct PlainTerm {
+  int p, q;
+  double c;
+};
+static std::vector<std::vector<PlainTerm>> plain_terms(const Plan* p) {
+  const int M = p->M;
+  auto A = [&](int i, int j, int k) { return p->alpha[((size_t)i * M + j) * M + k]; };
+  std::vector<std::vector<PlainTerm>> by_r(M);
+  for (int i = 0; i < M; ++i)
+    for (int j = i; j < M; ++j)
+      for (int k = j; k < M; ++k)
+        if (A(i, j, k) != 0) by_r[k].push_back(PlainTerm{i, j, A(i, j, k)});
+  if (M > 2 && A(0, 1, 2) != 0) {
+    const double c = A(0, 1, 2) * (-A(1, 1, 1) / A(0, 1, 2));
+    by_r[2].push_back(PlainTerm{0, 1, -c});
+    by_r[1].push_back(PlainTerm{0, 2, c});
+  }
+  return by_r;
+}
+
 int plain_run(Plan* p, const float* d_lagr, int64_t npart, float* d_pos, float* d_vel, cudaStream_t st) {
   int rc = plain_setup(p);
   if (rc) return rc;
@@ -383,49 +471,79 @@ int plain_run(Plan* p, const float* d_lagr, int64_t npart, float* d_pos, float* 
   if ((rc = launch_noise_fp64(p, p->d_seed, phi, s->H, st))) return rc;
   AAR_CUDA_TRY(p, cudaMemsetAsync(acc, 0, sizeof(double2) * s->nc, st));
   auto A = [&](int i, int j, int k) { return p->alpha[((size_t)i * M + j) * M + k]; };
-  // pair loop (main.c:564-880)
-  for (int ni = 0; ni < M; ++ni) {
-    PL("plain_filter", gc, kp_filter<<<gc, bs, 0, st>>>(a, s->qin + (size_t)ni * s->nsq, phi, fi));
-    if ((rc = z2d(fi))) return rc;
-    for (int nj = ni; nj < M; ++nj) {
-      Coef w{};
-      bool any = false;
-      for (int nk = nj; nk < M; ++nk) {
-        w.c[nk] = A(ni, nj, nk);
-        any = any || fabs(A(ni, nj, nk)) > 0;
+  const double n3 = (double)((unsigned)N * (unsigned)N * (unsigned)N);
+  if (regrouped(p)) {
+    // M filtered c2r f_p into fields 3 .. M+2 (2 holds g_r)
+    double2* g = s->f[2];
+    double2** fp = s->f + 3;
+    for (int m = 0; m < M; ++m) {
+      PL("plain_filter", gc, kp_filter<<<gc, bs, 0, st>>>(a, s->qin + (size_t)m * s->nsq, phi, fp[m]));
+      if ((rc = z2d(fp[m]))) return rc;
+    }
+    const auto by_r = plain_terms(p);
+    for (int r = 0; r < M; ++r) {
+      if (by_r[r].empty()) continue;
+      const auto& T = by_r[r];
+      for (size_t t0 = 0; t0 < T.size(); t0 += kProdChunk) {
+        PTerms pt{};
+        pt.n = (int)std::min(T.size() - t0, (size_t)kProdChunk);
+        for (int i = 0; i < pt.n; ++i) {
+          pt.fp[i] = (const double*)fp[T[t0 + i].p];
+          pt.fq[i] = (const double*)fp[T[t0 + i].q];
+          pt.c[i] = T[t0 + i].c;
+        }
+        PL("plain_products", gr, kp_products<<<gr, bs, 0, st>>>(a, pt, (double*)g, t0 > 0));
       }
-      if (!any) continue;
-      PL("plain_filter", gc, kp_filter<<<gc, bs, 0, st>>>(a, s->qin + (size_t)nj * s->nsq, phi, fj));
-      if ((rc = z2d(fj))) return rc;
-      PL("plain_mul", gr, kp_mul<<<gr, bs, 0, st>>>(a, (const double*)fi, (double*)fj));
-      if ((rc = d2z(fj))) return rc;
-      PL("plain_acc", gc, kp_acc<<<gc, bs, 0, st>>>(a, w, nj, M, s->qout, fj, acc));
-    }
-  }
-  // counter-terms (main.c:888-1063): all ten pair transforms, weight on (0,1) and (0,2)
-  double a012 = M > 2 ? A(0, 1, 2) : 0, t012 = (M > 2 && a012 != 0) ? -A(1, 1, 1) / a012 : 0;
-  for (int ni = 0; ni <= 3; ++ni) {
-    PL("plain_filter", gc, kp_filter<<<gc, bs, 0, st>>>(a, s->qin + (size_t)ni * s->nsq, phi, fi));
-    if ((rc = z2d(fi))) return rc;
-    for (int nj = ni; nj <= 3; ++nj) {
-      PL("plain_filter", gc, kp_filter<<<gc, bs, 0, st>>>(a, s->qin + (size_t)nj * s->nsq, phi, fj));
-      if ((rc = z2d(fj))) return rc;
-      PL("plain_mul", gr, kp_mul<<<gr, bs, 0, st>>>(a, (const double*)fi, (double*)fj));
-      if ((rc = d2z(fj))) return rc;
+      if ((rc = d2z(g))) return rc;
       Coef w{};
-      if (ni == 0 && nj == 1) w.c[2] = -a012 * t012;
-      if (ni == 0 && nj == 2) w.c[1] = a012 * t012;
-      PL("plain_acc", gc, kp_acc<<<gc, bs, 0, st>>>(a, w, 0, M, s->qout, fj, acc));
+      w.c[r] = 1.0;
+      PL("plain_acc", gc, kp_acc<<<gc, bs, 0, st>>>(a, w, r, r + 1, s->qout, g, acc));
     }
+    PL("plain_combine", gc, kp_combine_regrouped<<<gc, bs, 0, st>>>(a, phi, acc, p->prm.fnl, n3));
+  } else {
+    // pair loop (main.c:564-880)
+    for (int ni = 0; ni < M; ++ni) {
+      PL("plain_filter", gc, kp_filter<<<gc, bs, 0, st>>>(a, s->qin + (size_t)ni * s->nsq, phi, fi));
+      if ((rc = z2d(fi))) return rc;
+      for (int nj = ni; nj < M; ++nj) {
+        Coef w{};
+        bool any = false;
+        for (int nk = nj; nk < M; ++nk) {
+          w.c[nk] = A(ni, nj, nk);
+          any = any || fabs(A(ni, nj, nk)) > 0;
+        }
+        if (!any) continue;
+        PL("plain_filter", gc, kp_filter<<<gc, bs, 0, st>>>(a, s->qin + (size_t)nj * s->nsq, phi, fj));
+        if ((rc = z2d(fj))) return rc;
+        PL("plain_mul", gr, kp_mul<<<gr, bs, 0, st>>>(a, (const double*)fi, (double*)fj));
+        if ((rc = d2z(fj))) return rc;
+        PL("plain_acc", gc, kp_acc<<<gc, bs, 0, st>>>(a, w, nj, M, s->qout, fj, acc));
+      }
+    }
+    // counter-terms (main.c:888-1063): all ten pair transforms, weight on (0,1) and (0,2)
+    double a012 = M > 2 ? A(0, 1, 2) : 0, t012 = (M > 2 && a012 != 0) ? -A(1, 1, 1) / a012 : 0;
+    for (int ni = 0; ni <= 3; ++ni) {
+      PL("plain_filter", gc, kp_filter<<<gc, bs, 0, st>>>(a, s->qin + (size_t)ni * s->nsq, phi, fi));
+      if ((rc = z2d(fi))) return rc;
+      for (int nj = ni; nj <= 3; ++nj) {
+        PL("plain_filter", gc, kp_filter<<<gc, bs, 0, st>>>(a, s->qin + (size_t)nj * s->nsq, phi, fj));
+        if ((rc = z2d(fj))) return rc;
+        PL("plain_mul", gr, kp_mul<<<gr, bs, 0, st>>>(a, (const double*)fi, (double*)fj));
+        if ((rc = d2z(fj))) return rc;
+        Coef w{};
+        if (ni == 0 && nj == 1) w.c[2] = -a012 * t012;
+        if (ni == 0 && nj == 2) w.c[1] = a012 * t012;
+        PL("plain_acc", gc, kp_acc<<<gc, bs, 0, st>>>(a, w, 0, M, s->qout, fj, acc));
+      }
+    }
+    // combine (main.c:1094-1150): two real-space round trips
+    if ((rc = z2d(phi))) return rc;
+    if ((rc = d2z(phi))) return rc;
+    PL("plain_combine", gc, kp_combine<<<gc, bs, 0, st>>>(a, phi, acc, p->prm.fnl, n3));
+    if ((rc = z2d(phi))) return rc;
+    if ((rc = d2z(phi))) return rc;
+    PL("plain_scale", gc, kp_scale<<<gc, bs, 0, st>>>(a, phi, 1.0 / n3));
   }
-  // combine (main.c:1094-1150): two real-space round trips
-  double n3 = (double)((unsigned)N * (unsigned)N * (unsigned)N);
-  if ((rc = z2d(phi))) return rc;
-  if ((rc = d2z(phi))) return rc;
-  PL("plain_combine", gc, kp_combine<<<gc, bs, 0, st>>>(a, phi, acc, p->prm.fnl, n3));
-  if ((rc = z2d(phi))) return rc;
-  if ((rc = d2z(phi))) return rc;
-  PL("plain_scale", gc, kp_scale<<<gc, bs, 0, st>>>(a, phi, 1.0 / n3));
   // 2LPT (main.c:1156-1381)
   double kF = 2 * kPi / p->prm.box;
   double2** d = s->f + 4;  // six Hessian fields: f[4..9]
@@ -443,6 +561,10 @@ int plain_run(Plan* p, const float* d_lagr, int64_t npart, float* d_pos, float* 
     if ((rc = z2d(za[ax]))) return rc;
     if ((rc = z2d(d[ax]))) return rc;
   }
+  for (int ax = 0; ax < 3; ++ax) {
+    s->disp[ax] = za[ax];
+    s->disp[3 + ax] = d[ax];
+  }
   if (npart > 0) {
     PRead r{N, s->H, p->prm.box, p->vel_prefac, p->vel_prefac2,
             (double)(float)((unsigned)N * (unsigned)N * (unsigned)N)};
@@ -451,6 +573,27 @@ int plain_run(Plan* p, const float* d_lagr, int64_t npart, float* d_pos, float* 
                                                         (const double*)d[0], (const double*)d[1], (const double*)d[2],
                                                         d_lagr, npart, d_pos, d_vel));
   }
+  return AAR_OK;
+}
+
+// Displacement field `which` of the last run (0..2 ZA, 3..5 2LPT before its
+// 1/N^3) as float64 [N][N][N].
+int plain_copy_field(Plan* p, int which, double* out, cudaStream_t st) {
+  PlainState* s = st_of(p);
+  if (!s || !s->disp[which]) return set_err(p, "no FP64 displacement fields: run the plan first"), AAR_ERR_STATE;
+  PArgs a{p->grid, s->N, s->H, s->nsq};
+  unsigned gr = (unsigned)(((int64_t)s->N * s->N * s->N + 255) / 256);
+  kp_unpad<<<gr, 256, 0, st>>>(a, (const double*)s->disp[which], out);
+  AAR_CUDA_TRY(p, cudaGetLastError());
+  return AAR_OK;
+}
+
+// The potential spectrum of the last run (the total one once a run is
+// done), complex float64 [N][N][N/2+1].
+int plain_copy_spectrum(Plan* p, void* out, cudaStream_t st) {
+  PlainState* s = st_of(p);
+  if (!s) return set_err(p, "no FP64 spectrum: run the plan first"), AAR_ERR_STATE;
+  AAR_CUDA_TRY(p, cudaMemcpyAsync(out, s->f[0], sizeof(double2) * s->nc, cudaMemcpyDeviceToDevice, st));
   return AAR_OK;
 }
 

@@ -56,7 +56,11 @@ class ICGenerator:
         self.N = int(cfg["Nmesh"])
         self.device = torch.device(device if device is not None else "cuda", torch.cuda.current_device()
                                    if device is None else torch.device(device).index or 0)
-        self.precision = _lib.AAR_FUSED_FP32 if precision == "fp32" else _lib.AAR_PLAIN_FP64
+        forms = {"fp32": _lib.AAR_FUSED_FP32, "fp64": _lib.AAR_PLAIN_FP64,
+                 "fp64_regrouped": _lib.AAR_PLAIN_FP64_REGROUPED}
+        if precision not in forms:
+            raise ValueError(f"precision must be one of {sorted(forms)}")
+        self.precision = forms[precision]
         prm = params_from_config(cfg, self.precision, mem_limit_bytes)
         h = C.c_void_p()
         with torch.cuda.device(self.device):
@@ -73,6 +77,17 @@ class ICGenerator:
         kk = np.ascontiguousarray(k, dtype=np.float64)
         tt = np.ascontiguousarray(T, dtype=np.float64)
         check(self.L, self.h, self.L.aar_set_transfer(self.h, _dptr(kk), _dptr(tt), len(kk)))
+
+    @property
+    def plain(self) -> bool:
+        """True for the plain FP64 cuFFT forms."""
+        return self.precision != _lib.AAR_FUSED_FP32
+
+    def prepare(self) -> None:
+        """Allocate what a run needs now (aar_plan_prepare): the plain forms'
+        fields and cuFFT plans are otherwise made by the first run."""
+        with torch.cuda.device(self.device):
+            check(self.L, self.h, self.L.aar_plan_prepare(self.h))
 
     def close(self):
         if getattr(self, "h", None):
@@ -94,6 +109,11 @@ class ICGenerator:
     @property
     def launches(self) -> int:
         return self.L.aar_last_launch_count(self.h)
+
+    @property
+    def device_bytes(self) -> int:
+        """Device memory the plan holds (aar_plan_device_bytes)."""
+        return int(self.L.aar_plan_device_bytes(self.h))
 
     @property
     def n_modes(self) -> int:
@@ -145,13 +165,19 @@ class ICGenerator:
         check(self.L, self.h, fn(self.h, self._stream()))
 
     def spectrum(self) -> torch.Tensor:
-        """The plan's current potential spectrum, complex64 [N, N, N/2+1]."""
-        out = torch.empty((self.N, self.N, self.N // 2 + 1), dtype=torch.complex64, device=self.device)
+        """The plan's current potential spectrum, complex64 [N, N, N/2+1]
+        (complex128, the total potential of the last run, for the plain
+        forms)."""
+        dt = torch.complex128 if self.plain else torch.complex64
+        out = torch.empty((self.N, self.N, self.N // 2 + 1), dtype=dt, device=self.device)
         check(self.L, self.h, self.L.aar_copy_spectrum(self.h, _ptr(out), self._stream()))
         return out
 
     def field(self, which: int) -> torch.Tensor:
-        out = torch.empty((self.N, self.N, self.N), dtype=torch.float32, device=self.device)
+        """Displacement field `which` (0..2 ZA, 3..5 2LPT before its 1/N^3):
+        float32 for the fused form, float64 for the plain forms (after a run)."""
+        dt = torch.float64 if self.plain else torch.float32
+        out = torch.empty((self.N, self.N, self.N), dtype=dt, device=self.device)
         check(self.L, self.h, self.L.aar_copy_field(self.h, which, _ptr(out), self._stream()))
         return out
 
@@ -204,6 +230,30 @@ class ICGenerator:
         check(self.L, self.h, self.L.aar_stage_readout_glass(self.h, _ptr(glass), glass.shape[0], float(glass_box),
                                                              tile, _ptr(pos), _ptr(vel), _ptr(ids), self._stream()))
         return pos, vel, ids
+
+    def run_glass_host(self, glass: np.ndarray, glass_box: float, tile: int, ids: bool = True, out=None,
+                       wait: bool = True):
+        """Host-buffer glass run (aar_run_glass_host[_async]): the glass goes
+        in, positions, velocities (and IDs) come back in host arrays `out`
+        = (pos, vel, ids or None), allocated when not given.  wait=False
+        returns after enqueueing; call wait_host_copies() before reading."""
+        glass = np.ascontiguousarray(glass, dtype=np.float32)
+        n = glass.shape[0] * tile ** 3
+        if out is None:
+            out = (np.empty((n, 3), np.float32), np.empty((n, 3), np.float32),
+                   np.empty((n,), np.int32) if ids else None)
+        pos, vel, idv = out
+        self._glass_keep = glass  # the host glass must outlive an asynchronous copy
+        fn = self.L.aar_run_glass_host if wait else self.L.aar_run_glass_host_async
+        addr = (lambda a: a.data_ptr()) if isinstance(pos, torch.Tensor) else (lambda a: a.ctypes.data)
+        with torch.cuda.device(self.device):
+            check(self.L, self.h, fn(self.h, glass.ctypes.data, glass.shape[0], float(glass_box), int(tile),
+                                     addr(pos), addr(vel), addr(idv) if idv is not None else None,
+                                     self._stream()))
+        return pos, vel, idv
+
+    def wait_host_copies(self) -> None:
+        check(self.L, self.h, self.L.aar_wait_host_copies(self.h))
 
     def run_host(self, lagr: np.ndarray):
         """The C-ABI host-buffer path: numpy in, numpy out (copies included)."""

@@ -39,7 +39,10 @@ extern "C" {
 
 /* Arithmetic of the run. */
 #define AAR_FUSED_FP32 0  /* own FFTs, fused filters/products/accumulation, FP32 */
-#define AAR_PLAIN_FP64 1  /* cuFFT Z2D/D2Z + separate pointwise kernels, FP64 */
+#define AAR_PLAIN_FP64 1  /* cuFFT Z2D/D2Z + separate pointwise kernels, FP64, the reference's
+                             loop structure (M + 2P + 41 transforms) */
+#define AAR_PLAIN_FP64_REGROUPED 2 /* as AAR_PLAIN_FP64 with the modal sum regrouped by linearity
+                                      (M c2r + R r2c; <= 2M + 13 transforms in all) */
 
 /* Which executable's power spectrum the plan follows. */
 #define AAR_VARIANT_BASIS 0    /* 2LPTBasis: P(k) = Norm k^ns T^2 (LPT/Basis/power.c:240-265) */
@@ -74,9 +77,19 @@ typedef struct aar_plan aar_plan;
    (replaces initialize_ffts main.c:1556-1599 and the parameter broadcast). */
 int aar_plan_create(const aar_params* prm, aar_plan** out);
 
+/* Allocate now what the plan's runs need (the plain forms' FP64 fields,
+   tables and cuFFT plans, the fused form's work fields), so that the first
+   run does no set-up.  Needs tables and transfer function.  Optional: a run
+   without it prepares itself.  (The reference sets up inside
+   displacement_fields, main.c:149-212, 1556-1599.) */
+int aar_plan_prepare(aar_plan* plan);
+
 /* Coefficient tables: alpha as a symmetric [M][M][M] array (as the reference
    stores it after reading AlphaTable.dat, main.c:213-247), X0 as [M] (first
-   value column of AiTable.dat, main.c:249-289). */
+   value column of AiTable.dat, main.c:249-289).  aar_set_tables and
+   aar_set_transfer synchronise the device before they rewrite the plan's
+   device tables, so runs of the plan still in flight finish with the old
+   values. */
 int aar_set_tables(aar_plan* plan, const double* alpha_sym, const double* x0, int32_t n_modes);
 
 /* Tabulated transfer function, raw (k, T) rows in h/Mpc (read_transfer_table
@@ -106,6 +119,35 @@ int aar_run_glass(aar_plan* plan, const float* d_glass_pos, int64_t nglass, doub
    on first use, grown when npart grows, freed with the plan). */
 int aar_run_host(aar_plan* plan, const float* h_lagr_pos, int64_t npart, float* h_pos, float* h_vel, void* stream);
 
+/* aar_run_glass with HOST buffers, on the reference's own dataflow: the
+   glass (nglass float32 [3] positions as read from the GlassFile,
+   read_glass.c:43-84) is copied in, the Lagrangian positions are made on the
+   device from it tiled tile^3 times (read_glass.c:129-214), and the
+   particles are read out in chunks whose positions, velocities and (when
+   h_ids is not NULL) IDs go to the host while later chunks are read out --
+   no N^3 Lagrangian array crosses to the GPU.  npart = nglass * tile^3;
+   h_pos / h_vel float32 [npart][3], h_ids int32 [npart].  Returns when the
+   results are in the host buffers.  The plan owns the device staging
+   (grown on demand, freed with the plan).  Fused form only. */
+int aar_run_glass_host(aar_plan* plan, const float* h_glass, int64_t nglass, double glass_box, int32_t tile,
+                       float* h_pos, float* h_vel, int32_t* h_ids, void* stream);
+
+/* aar_run_glass_host without the wait: the fields and the read-out are
+   enqueued behind earlier work on `stream`, the copies to the host on the
+   plan's own two side streams, and the call returns.  The host buffers hold
+   the results once aar_wait_host_copies(plan) has returned; until then they
+   must stay valid and must not be read.  A following call on the same plan
+   computes the next realisation's fields on `stream` while this one's
+   particles are still on their way out; each staging chunk is handed over by
+   an event, so the next read-out of a chunk waits only for that chunk's
+   copy.  Use pinned host memory (cudaHostAlloc / cudaHostRegister): copies
+   from pageable memory are not asynchronous. */
+int aar_run_glass_host_async(aar_plan* plan, const float* h_glass, int64_t nglass, double glass_box, int32_t tile,
+                             float* h_pos, float* h_vel, int32_t* h_ids, void* stream);
+/* Block until every copy to the host that the plan's aar_run_glass_host*
+   calls have enqueued is done. */
+int aar_wait_host_copies(aar_plan* plan);
+
 /* ---- stage entry points (the same work as aar_run, split; used by tests) ---- */
 
 /* Seed table of main.c:317-349 (uint32 [N][N]) for the plan's seed. */
@@ -125,17 +167,19 @@ int aar_stage_readout_glass(aar_plan* plan, const float* d_glass_pos, int64_t ng
                             float* d_pos, float* d_vel, int32_t* d_ids, void* stream);
 /* Copy the plan's current potential spectrum to d_out as complex
    [N][N][N/2+1] (interleaved re, im; float32 for AAR_FUSED_FP32, float64
-   for AAR_PLAIN_FP64). */
+   for the plain forms, whose spectrum is the total one after a run). */
 int aar_copy_spectrum(aar_plan* plan, void* d_out, void* stream);
 /* Copy displacement field `which` (0..2: ZA x,y,z; 3..5: 2LPT x,y,z as the
-   reference holds them before its 1/N^3) to d_out, float32 [N][N][N]. */
-int aar_copy_field(aar_plan* plan, int32_t which, float* d_out, void* stream);
+   reference holds them before its 1/N^3, main.c:1378-1431) to d_out, real
+   [N][N][N]: float32 for AAR_FUSED_FP32, float64 for the plain forms (after
+   a run). */
+int aar_copy_field(aar_plan* plan, int32_t which, void* d_out, void* stream);
 
 /* No counterpart in the reference.  The Gaussian potential spectrum of the
    plan's seed (what aar_stage_noise + aar_copy_spectrum give for the fused
    form) written straight into the caller's buffer d_out, complex
    [N][N][N/2+1]: float32 pairs for AAR_FUSED_FP32 plans, float64 pairs for
-   AAR_PLAIN_FP64 plans.  Needs the transfer function set (aar_set_transfer);
+   the plain FP64 plans.  Needs the transfer function set (aar_set_transfer);
    the coefficient tables are not used.
    The call allocates nothing: no cudaMalloc / cudaFree and no allocating
    library.  It is for callers that own the device-memory budget themselves,
@@ -150,8 +194,16 @@ int aar_copy_field(aar_plan* plan, int32_t which, float* d_out, void* stream);
    clears it on the stream) and nothing in the scratch has to start at zero.
    The first call on a device resolves the scratch address
    (cudaGetSymbolAddress); make that first call before any stream capture
-   begins.  There is one scratch per device, so calls that overlap on one
-   device (other streams or host threads) race on it: serialise them. */
+   begins.  Under CUDA's lazy module loading, that first call may also be
+   the one that loads the library's noise module on the device, which
+   reserves the 4 MiB array and the module's code: that one-time load is the
+   only device memory the entry point ever causes to be reserved, so make
+   the first call during set-up (or run any other call of the library on the
+   device first).  The cached address belongs to the device's primary
+   context and stays valid for the life of the process; after
+   cudaDeviceReset, or from a non-primary context, it is stale.  There is
+   one scratch per device, so calls that overlap on one device (other
+   streams or host threads) race on it: serialise them. */
 int aar_gaussian_spectrum_noalloc(aar_plan* plan, void* d_out, void* stream);
 
 /* The plan's own 3-D transforms with FFTW's rfftwnd conventions
@@ -279,6 +331,10 @@ int aar_autotune(aar_plan* plan, char* report, int32_t len, void* stream);
    last report into buf (NUL-terminated). */
 int aar_profile_enable(aar_plan* plan, int32_t on);
 int aar_profile_report(aar_plan* plan, char* buf, int32_t len);
+
+/* Device bytes the plan holds now: fields, tables, staging and scratch it
+   allocated (not the caller's buffers). */
+int64_t aar_plan_device_bytes(const aar_plan* plan);
 
 /* Number of kernels the last aar_run* / stage call launched. */
 int aar_last_launch_count(const aar_plan* plan);

@@ -20,7 +20,23 @@ _lib = None
 
 
 def build(ref: bool = False) -> None:
-    subprocess.check_call(["make", "-s", "-C", HERE, "all"] + (["ref"] if ref else []))
+    subprocess.check_call(["make", "-s", "-C", HERE, "all"] + (["ref", "REF=" + reference_checkout()] if ref else []))
+
+
+def reference_checkout() -> str:
+    """Directory the Makefile's `ref` target compiles the reference from:
+    $AARAMBAM_REFERENCE when set, else the Makefile's default."""
+    env = os.environ.get("AARAMBAM_REFERENCE")
+    if env:
+        return env
+    out = subprocess.run(["make", "-s", "-C", HERE, "print-ref"], capture_output=True, text=True)
+    return out.stdout.strip()
+
+
+def reference_present() -> bool:
+    """True when the reference's 2LPT sources can be compiled here."""
+    d = reference_checkout()
+    return bool(d) and os.path.isfile(os.path.join(d, "Aarambam", "LPT", "Basis", "main.c"))
 
 
 class Cosmo(C.Structure):

@@ -40,6 +40,8 @@ CONFIGS = {
     "equil_m9_L500_n256": ("Equilateral", 9, 0.965, 500.0, 256, 1e-4, 150, {}),
     "scalarI_m13_L500_n256_mu0p5": ("ScalarI", 13, 0.965, 500.0, 256, 1e-4, 150, {"mass": 0.5}),
     "scalarI_m16_L500_n256_mu1p5": ("ScalarI", 16, 0.965, 500.0, 256, 1e-4, 150, {"mass": 1.5}),
+    # the batch's 20-mode template (mode counts 6..20 across the batch)
+    "scalarI_m20_L500_n256_mu1p75": ("ScalarI", 20, 0.965, 500.0, 256, 1e-4, 150, {"mass": 1.75}),
     # 1024^3 headline: ScalarI mass=1, 20 modes, Box 1000.
     "scalarI_m20_L1000_n1024": ("ScalarI", 20, 0.965, 1000.0, 1024, 1e-4, 150, {"mass": 1.0}),
     # 1536^3 resonant case: LogResonance w=10, 20 modes, Box 2000.

@@ -77,3 +77,36 @@ def test_batch_rejects_bad_arrays(cuda):
     with pytest.raises(ValueError):
         b.run(lagr, lagr[:1], lagr)
     b.close()
+
+
+def test_batch_recaptured_after_autotune(cuda):
+    """aar_autotune reloads the plan's NVRTC module for its candidates, so a
+    batch graph captured before it must be captured again whatever the
+    tuner's outcome; here the tuner returns an error (its report buffer is
+    too small) after it has tried every candidate."""
+    import ctypes as C
+
+    from aarambam_gb300._lib import AAR_ERR_ARG
+    N, n = 64, 2
+    gens = make_gens(N, n)
+    for g in gens:
+        assert g.set_jit(2) == "on"
+    lagr = [lattice(N, 500.0, cuda) for _ in range(n)]
+    want = [[t.clone() for t in g.run(l)] for g, l in zip(gens, lagr)]
+    b = ICBatch(gens)
+    pos = [torch.empty_like(l) for l in lagr]
+    vel = [torch.empty_like(l) for l in lagr]
+    b.run(lagr, pos, vel)
+    torch.cuda.synchronize()
+    small = C.create_string_buffer(8)
+    rc = gens[0].L.aar_autotune(gens[0].h, small, len(small), gens[0]._stream())
+    assert rc == AAR_ERR_ARG
+    torch.cuda.synchronize()
+    # the tuner may have chosen another row kernel: compare with single runs now
+    want = [[t.clone() for t in g.run(l)] for g, l in zip(gens, lagr)]
+    torch.cuda.synchronize()
+    b.run(lagr, pos, vel)
+    torch.cuda.synchronize()
+    for i in range(n):
+        assert torch.equal(pos[i], want[i][0]) and torch.equal(vel[i], want[i][1]), i
+    b.close()

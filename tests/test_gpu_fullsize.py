@@ -123,3 +123,61 @@ def test_fused_vs_plain_fp64_1024(cuda):
         return (num / den) ** 0.5
     assert rel(pj) < 1e-5
     assert rel(pg) < 1e-5
+
+
+def _delta(psi1, box):
+    """delta = -div psi1 (spectral derivative, FP64), psi1 three [N, N, N] fields."""
+    N = psi1[0].shape[0]
+    dev = psi1[0].device
+    k = 2 * np.pi / box * torch.fft.fftfreq(N, 1.0 / N, dtype=torch.float64, device=dev)
+    kz = 2 * np.pi / box * torch.arange(N // 2 + 1, dtype=torch.float64, device=dev)
+    ks = [k[:, None, None], k[None, :, None], kz[None, None, :]]
+    d = sum(1j * ks[a] * torch.fft.rfftn(psi1[a].double()) for a in range(3))
+    return -torch.fft.irfftn(d, s=(N, N, N))
+
+
+def _rel(a, b):
+    num = sum(float(torch.sum((x.double() - y.double()) ** 2)) for x, y in zip(a, b))
+    den = sum(float(torch.sum(y.double() ** 2)) for y in b)
+    return (num / den) ** 0.5
+
+
+def test_precision_config_512(cuda):
+    """The precision configuration at its stated size: 512^3, Box 1000,
+    ScalarI mass 1, 12 modes.  Relative RMS of delta = -div psi1, psi1 and
+    psi2 of the fused FP32 form against the plain FP64 GPU form's FP64
+    fields (that form is pinned to the FP64 oracle by
+    test_plain_fp64_fields_vs_oracle), and of the particle displacement."""
+    N, box = 512, 1000.0
+    tab, M = "scalarI_m12_L1000_n512", 12
+    cfg = make_cfg(N, box, 1234, 100.0, M, tab, 512)
+    a, x0 = table(tab, M)
+    k, t = bbks()
+    g = torch.arange(N, device=cuda, dtype=torch.float32) * (box / N)
+    gx, gy, gz = torch.meshgrid(g, g, g, indexing="ij")
+    lagr = torch.stack([gx.reshape(-1), gy.reshape(-1), gz.reshape(-1)], 1).contiguous()
+    del gx, gy, gz
+    gf = ICGenerator(cfg, a, x0, k, t)
+    pf, _ = gf.run(lagr)
+    ff = [gf.field(i) for i in range(6)]
+    gf.close()
+    del gf
+    torch.cuda.empty_cache()
+    gp = ICGenerator(cfg, a, x0, k, t, precision="fp64")
+    pp, _ = gp.run(lagr)
+    fp = [gp.field(i) for i in range(6)]
+    gp.close()
+    del gp
+    torch.cuda.empty_cache()
+    e_psi1 = _rel(ff[:3], fp[:3])
+    e_psi2 = _rel(ff[3:], fp[3:])
+    e_delta = _rel([_delta(ff[:3], box)], [_delta(fp[:3], box)])
+
+    def dspl(p):
+        d = p.double() - lagr.double()
+        return d - box * torch.round(d / box)
+    e_disp = _rel([dspl(pf)], [dspl(pp)])
+    print(f"precision 512^3 M=12: delta {e_delta:.3e} psi1 {e_psi1:.3e} psi2 {e_psi2:.3e} displacement {e_disp:.3e}")
+    assert e_psi1 < 1e-5 and e_delta < 1e-5
+    assert e_psi2 < 2e-4
+    assert e_disp < 1e-5

@@ -256,3 +256,68 @@ def test_plain_fp64_form_vs_oracle(cuda, cfg):
     assert rel_rms(d_gpu, d_ref) < 1e-6
     assert rel_rms(vel.cpu().numpy(), r["vel"]) < 1e-6
     assert g.launches > 10
+
+
+@pytest.mark.parametrize("cfg", SMALL, ids=lambda c: f"N{c['Nmesh']}_s{c['Seed']}")
+def test_plain_fp64_regrouped_vs_oracle(cuda, cfg):
+    """Regrouped plain FP64 form (M c2r + R r2c, counter-terms folded into
+    alpha'): particles agree with the FP64 oracle at the float32 storage
+    level, and its FP64 displacement fields and total potential agree with
+    the oracle's to FP64 rounding (different summation order and no
+    potential round trips)."""
+    r = oracle_run(key(cfg))
+    g = gen_for(cfg, precision="fp64_regrouped")
+    pos, vel = g.run(torch.from_numpy(r["lagr"]).cuda())
+    d_gpu = periodic_delta(pos.cpu().numpy(), r["lagr"], cfg["Box"])
+    d_ref = periodic_delta(r["pos"], r["lagr"], cfg["Box"])
+    assert rel_rms(d_gpu, d_ref) < 1e-6
+    assert rel_rms(vel.cpu().numpy(), r["vel"]) < 1e-6
+    f = np.stack([g.field(i).cpu().numpy() for i in range(6)])
+    assert f.dtype == np.float64
+    assert rel_rms(f[:3], r["disp"][:3]) < 1e-9
+    assert rel_rms(f[3:], r["disp"][3:]) < 1e-9
+    tot = r["total"][..., 0] + 1j * r["total"][..., 1]
+    assert rel_rms(g.spectrum().cpu().numpy(), tot) < 1e-9
+
+
+@pytest.mark.parametrize("cfg", SMALL[:2], ids=lambda c: f"N{c['Nmesh']}_s{c['Seed']}")
+def test_plain_fp64_fields_vs_oracle(cuda, cfg):
+    """FP64 field copies of the reference-structure plain form (what the
+    precision comparisons at full size use as the FP64 reference)."""
+    r = oracle_run(key(cfg))
+    g = gen_for(cfg, precision="fp64")
+    g.run(torch.from_numpy(r["lagr"]).cuda())
+    f = np.stack([g.field(i).cpu().numpy() for i in range(6)])
+    assert rel_rms(f[:3], r["disp"][:3]) < 1e-9
+    assert rel_rms(f[3:], r["disp"][3:]) < 1e-9
+
+
+def test_run_glass_host_sync_and_async(cuda):
+    """Host-buffer glass entry points: a random glass tiled 8^3 times (2.1M
+    particles, 16 read-out chunks) gives the device entry point's particles
+    bit for bit; two asynchronous calls with different seeds in a row (the
+    second computing while the first copies out) each deliver their own
+    realisation."""
+    cfg = make_cfg(128, 500.0, 21, 10.0, 8, "local_m8_L500_n128", 128)
+    g = gen_for(cfg)
+    rng = np.random.default_rng(5)
+    glass = rng.uniform(0, 100.0, (4096, 3)).astype(np.float32)
+    dglass = torch.from_numpy(glass).cuda()
+    want = []
+    for seed in (21, 22):
+        g.set_seed(seed)
+        want.append([t.cpu() for t in g.run_glass(dglass, 100.0, 8)])
+    g.set_seed(21)
+    pos, vel, ids = g.run_glass_host(glass, 100.0, 8)
+    assert np.array_equal(pos, want[0][0].numpy()) and np.array_equal(vel, want[0][1].numpy())
+    assert np.array_equal(ids, want[0][2].numpy())
+    n = glass.shape[0] * 8 ** 3
+    bufs = [(torch.empty((n, 3), dtype=torch.float32).pin_memory(), torch.empty((n, 3), dtype=torch.float32).pin_memory(),
+             torch.empty((n,), dtype=torch.int32).pin_memory()) for _ in range(2)]
+    for seed, b in zip((21, 22), bufs):
+        g.set_seed(seed)
+        g.run_glass_host(glass, 100.0, 8, out=b, wait=False)
+    g.wait_host_copies()
+    torch.cuda.synchronize()
+    for b, w in zip(bufs, want):
+        assert all(torch.equal(x, y) for x, y in zip(b, w))

@@ -155,7 +155,7 @@ def test_potential_dump_layout(tmp_path):
 def test_c_abi_library_exports_every_declared_symbol():
     build()
     hdr = open(os.path.join(ROOT, "include", "aarambam.h")).read()
-    declared = set(re.findall(r"^\s*(?:int|void|size_t|const char\*)\s+(aar_[A-Za-z0-9_]+)\s*\(", hdr, re.M))
+    declared = set(re.findall(r"^\s*(?:int|int64_t|void|size_t|const char\*)\s+(aar_[A-Za-z0-9_]+)\s*\(", hdr, re.M))
     assert declared == set(_lib.EXPORTS)
     L = ctypes.CDLL(LIB)
     for name in declared:

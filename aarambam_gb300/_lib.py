@@ -28,13 +28,13 @@ AAR_VARIANT_RESBASIS = 1
 EXPORTS = [
     "aar_plan_create", "aar_set_tables", "aar_set_transfer", "aar_get_scalars", "aar_set_seed", "aar_run",
     "aar_run_glass", "aar_run_host", "aar_run_glass_host", "aar_run_glass_host_async", "aar_wait_host_copies",
-    "aar_plan_prepare", "aar_plan_device_bytes", "aar_seedtable", "aar_stage_noise", "aar_stage_modal", "aar_stage_lpt",
+    "aar_plan_prepare", "aar_plan_device_bytes", "aar_modal_partition", "aar_set_modal_partition", "aar_seedtable", "aar_stage_noise", "aar_stage_modal", "aar_stage_lpt",
     "aar_stage_readout", "aar_stage_readout_glass", "aar_copy_spectrum", "aar_copy_field", "aar_gaussian_spectrum_noalloc", "aar_c2r", "aar_r2c", "aar_last_launch_count", "aar_profile_enable", "aar_profile_report",
     "aar_last_error", "aar_plan_destroy", "aar_version",
     "aar_batch_create", "aar_batch_run", "aar_batch_launch_count", "aar_batch_last_error", "aar_batch_destroy",
     "aar_set_spectrum", "aar_adj_spectral", "aar_adj_source", "aar_adj_products", "aar_set_jit", "aar_jit_status",
     "aar_tetra_covariance_scratch_bytes", "aar_tetra_covariance", "aar_tetra_QS", "aar_tetra_residual",
-    "aar_bordered_cond", "aar_autotune",
+    "aar_bordered_cond", "aar_autotune", "aar_profile_modal_rows",
 ]
 AAR_ADJ_OP_ONE, AAR_ADJ_OP_GAUSS, AAR_ADJ_OP_Q, AAR_ADJ_OP_RHO = 0, 1, 2, 3
 AAR_ADJ_OP_HESS, AAR_ADJ_OP_PSI1, AAR_ADJ_OP_PSI2 = 4, 5, 6
@@ -49,7 +49,8 @@ class Params(C.Structure):
                 ("input_spectrum_unit_length_in_cm", C.c_double), ("fixed_amplitude", C.c_int32),
                 ("phase_flip", C.c_int32), ("sphere_mode", C.c_int32), ("precision", C.c_int32),
                 ("mem_limit_bytes", C.c_int64), ("variant", C.c_int32), ("which_spectrum", C.c_int32),
-                ("a_res", C.c_double), ("w_res", C.c_double), ("phi_res", C.c_double)]
+                ("a_res", C.c_double), ("w_res", C.c_double), ("phi_res", C.c_double),
+                ("noise_fp64", C.c_int32)]
 
 
 class Scalars(C.Structure):
@@ -95,6 +96,9 @@ def load(build_if_missing: bool = False):
     L.aar_run_glass_host_async.argtypes = [vp, vp, i64, C.c_double, i32, vp, vp, vp, vp]
     L.aar_wait_host_copies.argtypes = [vp]
     L.aar_plan_prepare.argtypes = [vp]
+    L.aar_modal_partition.argtypes = [dp, i32, i32, C.POINTER(i32)]
+    L.aar_set_modal_partition.argtypes = [vp, i32, i32]
+    L.aar_profile_modal_rows.argtypes = [vp, vp, i64, vp]
     L.aar_plan_device_bytes.argtypes = [vp]
     L.aar_plan_device_bytes.restype = i64
     L.aar_seedtable.argtypes = [vp, vp, vp]

@@ -80,6 +80,7 @@ struct Plan {
   int64_t xpass_group = 1;       // tiles per item group of the multi-output x passes (passes.cuh)
   std::string jit_status = "off";
   int nterms = 0, nr_active = 0;
+  int modal_part = 0, modal_nparts = 1;  // split of the modal sum over r (this plan's part)
   // plain FP64 form
   void* plain = nullptr;
   int last_launches = 0;      // kernels launched by the last run
@@ -140,6 +141,9 @@ int launch_seedtable(Plan* p, uint32_t seed, uint32_t* d_out, cudaStream_t st);
 int launch_noise_fp32(Plan* p, const uint32_t* d_seed, float2* d_phik, cudaStream_t st);
 int launch_noise_fp64(Plan* p, const uint32_t* d_seed, double2* d_phik, int hp, cudaStream_t st);
 int fused_prepare(Plan* p);
+struct Term;
+std::vector<std::vector<Term>> regrouped_terms(const std::vector<double>& alpha, int M);
+std::vector<int> modal_partition(const std::vector<std::vector<Term>>& by_r, int nparts);
 int fused_modal(Plan* p, cudaStream_t st);
 int fused_lpt(Plan* p, cudaStream_t st);
 int fused_readout(Plan* p, const float* d_lagr, int64_t npart, float* d_pos, float* d_vel, cudaStream_t st);
@@ -165,7 +169,8 @@ int copy_rows(Plan* p, void* dst, int64_t dst_ld, int dst_xb, const void* src, i
               size_t elem, cudaStream_t st);
 int noalloc_gaussian(Plan* p, void* d_out, cudaStream_t st);
 int jit_prepare(Plan* p);
-int jit_modal_rows(Plan* p, float2* work, int64_t fs, cudaStream_t st);
+int jit_modal_rows(Plan* p, float2* work, int64_t fs, cudaStream_t st, int64_t nrows = -1);
+int profile_modal_rows(Plan* p, float2* work, int64_t nrows, cudaStream_t st);
 // the specialised modal accumulation of the same module; false when the
 // plan has none (the generic k_modal_acc runs)
 bool jit_has_acc(const Plan* p);

@@ -17,6 +17,7 @@
 
 #include "aar_internal.cuh"
 #include "ranlux.cuh"
+#include "spectral.cuh"
 
 struct aar_plan {
   aar::Plan p;
@@ -414,8 +415,6 @@ static int create(Plan* p) {
     AAR_CUDA_TRY(p, cudaMemcpy(p->d_rlxpow, pw.data(), sizeof(U576) * 32, cudaMemcpyHostToDevice));
   }
   if (q.precision == AAR_FUSED_FP32) {
-    size_t fbytes = sizeof(float2) * (size_t)N * N * p->HP;
-    if ((rc = plan_alloc(p, (void**)&p->d_phik, fbytes))) return rc;
     std::vector<float2> twN(N), twH(N / 2);
     for (int m = 0; m < N; ++m) {
       long double ang = -2.0L * 3.141592653589793238462643383279502884L * m / N;
@@ -460,10 +459,29 @@ static int create(Plan* p) {
 
 static cudaStream_t S(void* s) { return (cudaStream_t)s; }
 
-static int ready(Plan* p) {
+static int ready_tables(Plan* p) {
   if (!p->have_tables) return set_err(p, "coefficient tables not set"), AAR_ERR_STATE;
   if (!p->have_transfer) return set_err(p, "transfer function not set"), AAR_ERR_STATE;
   return AAR_OK;
+}
+
+// The fused form's fields (the potential spectrum and max(M, 9) work
+// fields) are allocated on first use -- the first run, stage or
+// aar_plan_prepare -- not when the plan is made or its tables are set, so a
+// plan holds no field memory until it computes.
+static int ensure_fields(Plan* p) {
+  if (p->prm.precision != AAR_FUSED_FP32) return AAR_OK;
+  if (!p->d_phik) {
+    int rc = plan_alloc(p, (void**)&p->d_phik, sizeof(float2) * (size_t)p->N * p->N * p->HP);
+    if (rc) return rc;
+  }
+  return alloc_fused(p, p->M);
+}
+
+static int ready(Plan* p) {
+  int rc = ready_tables(p);
+  if (rc) return rc;
+  return ensure_fields(p);
 }
 
 static int run_noise(Plan* p, cudaStream_t st) {
@@ -529,7 +547,6 @@ int aar_set_tables(aar_plan* h, const double* alpha, const double* x0, int32_t M
   plain_free(p);  // plain-form tables are rebuilt on the next run
   int rc;
   if (p->prm.precision == AAR_FUSED_FP32) {
-    if ((rc = alloc_fused(p, M))) return rc;
     if ((rc = mode_tables(p))) return rc;
     if (!p->d_terms && (rc = plan_alloc(p, &p->d_terms, terms_bytes()))) return rc;
     if ((rc = fused_prepare(p))) return rc;
@@ -611,6 +628,7 @@ int aar_stage_readout(aar_plan* h, const float* d_lagr, int64_t npart, float* d_
   Plan* p = &h->p;
   p->last_launches = 0;
   if (p->prm.precision != AAR_FUSED_FP32) return set_err(p, "stage calls are for the fused form"), AAR_ERR_ARG;
+  if (!p->d_work || p->nwork < 6) return set_err(p, "no displacement fields: run the field stages first"), AAR_ERR_STATE;
   return fused_readout(p, d_lagr, npart, d_pos, d_vel, S(stream));
 }
 
@@ -619,6 +637,7 @@ int aar_stage_readout_glass(aar_plan* h, const float* d_glass, int64_t nglass, d
   if (!h || nglass < 0 || tile < 1 || !(glass_box > 0)) return AAR_ERR_ARG;
   Plan* p = &h->p;
   if (p->prm.precision != AAR_FUSED_FP32) return set_err(p, "stage calls are for the fused form"), AAR_ERR_ARG;
+  if (!p->d_work || p->nwork < 6) return set_err(p, "no displacement fields: run the field stages first"), AAR_ERR_STATE;
   p->last_launches = 0;
   int rc = glass_prepare(p, d_glass, nglass, glass_box, tile, S(stream));
   if (rc) return rc;
@@ -930,10 +949,45 @@ int aar_copy_field(aar_plan* h, int32_t which, void* d_out, void* stream) {
   if (!h || !d_out || which < 0 || which > 5) return AAR_ERR_ARG;
   Plan* p = &h->p;
   if (is_plain(p->prm)) return plain_copy_field(p, which, (double*)d_out, S(stream));
-  if (p->prm.precision != AAR_FUSED_FP32 || !p->d_work) return set_err(p, "no FP32 fields in this plan"), AAR_ERR_STATE;
+  if (p->prm.precision != AAR_FUSED_FP32 || !p->d_work || which >= p->nwork)
+    return set_err(p, "no FP32 displacement fields in this plan: run the field stages first"), AAR_ERR_STATE;
   int N = p->N;
   const float* src = (const float*)(p->d_work + (size_t)which * N * N * p->HP);
   return copy_rows(p, d_out, N, 1, src, 2 * p->HP, kXB, N, sizeof(float), S(stream));
+}
+
+int aar_profile_modal_rows(aar_plan* h, void* d_work, int64_t nrows, void* stream) {
+  if (!h || !d_work) return AAR_ERR_ARG;
+  Plan* p = &h->p;
+  int rc = ready_tables(p);  // the caller's fields only: the plan's are not allocated
+  if (rc) return rc;
+  if (p->prm.precision != AAR_FUSED_FP32) return set_err(p, "the row harness is for the fused form"), AAR_ERR_ARG;
+  p->last_launches = 0;
+  return profile_modal_rows(p, (float2*)d_work, nrows, S(stream));
+}
+
+// ------------------------------------------------------------- modal split
+int aar_set_modal_partition(aar_plan* h, int32_t part, int32_t nparts) {
+  if (!h) return AAR_ERR_ARG;
+  Plan* p = &h->p;
+  if (nparts < 1 || nparts > kMaxModes || part < 0 || part >= nparts)
+    return set_err(p, "modal partition: need 0 <= part < nparts <= 32"), AAR_ERR_ARG;
+  if (p->prm.precision != AAR_FUSED_FP32) return set_err(p, "the modal split is for the fused form"), AAR_ERR_ARG;
+  if (part == p->modal_part && nparts == p->modal_nparts) return AAR_OK;
+  ++p->generation;
+  p->modal_part = part;
+  p->modal_nparts = nparts;
+  if (!p->have_tables) return AAR_OK;
+  AAR_CUDA_TRY(p, cudaDeviceSynchronize());  // the term list is rewritten below
+  return fused_prepare(p);
+}
+
+int aar_modal_partition(const double* alpha, int32_t M, int32_t nparts, int32_t* part_of_r) {
+  if (!alpha || !part_of_r || M < 1 || M > kMaxModes || nparts < 1 || nparts > kMaxModes) return AAR_ERR_ARG;
+  std::vector<double> a(alpha, alpha + (size_t)M * M * M);
+  const std::vector<int> part = modal_partition(regrouped_terms(a, M), nparts);
+  for (int r = 0; r < M; ++r) part_of_r[r] = part[r];
+  return AAR_OK;
 }
 
 // ------------------------------------------------------------- JIT rows
@@ -1042,7 +1096,11 @@ int aar_autotune(aar_plan* h, char* report, int32_t len, void* stream) {
 int aar_set_spectrum(aar_plan* h, const void* d_in, void* stream) {
   if (!h || !d_in) return AAR_ERR_ARG;
   Plan* p = &h->p;
-  if (p->prm.precision != AAR_FUSED_FP32 || !p->d_phik) return set_err(p, "aar_set_spectrum is for the fused form"), AAR_ERR_ARG;
+  if (p->prm.precision != AAR_FUSED_FP32) return set_err(p, "aar_set_spectrum is for the fused form"), AAR_ERR_ARG;
+  if (!p->d_phik) {
+    int rc = ensure_fields(p);
+    if (rc) return rc;
+  }
   const int H = p->N / 2 + 1;
   return copy_rows(p, p->d_phik, p->HP, kXB, d_in, H, 1, H, sizeof(float2), S(stream));
 }

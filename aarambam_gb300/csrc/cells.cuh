@@ -68,9 +68,49 @@ __device__ __forceinline__ bool keep_cell(const Grid& g, int kx, int ky, int kz)
 // and P_l by the Bonnet recurrence P_l = A_l kbar P_{l-1} - B_l P_{l-2}.
 struct RhoArgs {
   float s, c1, log2kF, inv_kF2;  // c1 = 2 kmin^s / (kmax^s - kmin^s)
+  float e4, e2;                  // 4 - ns, 2 - ns (exponents of the field filters)
   float x0[kMaxModes];
   float A[kMaxModes], B[kMaxModes];  // (2l-1)/l, (l-1)/l
 };
+
+// Field filter q_n(k) of main.c:580-637 at K cells (n2[i] = |k|^2 in grid
+// units, > 0) in FP32: k^(s (n-3)) k^(4-ns) for n <= 3, (P_{n-1}(kbar) -
+// X0[n-1]) k^(2-ns) above, with kbar and P_l as for rho_n (RhoArgs).  The K
+// recurrences run in lockstep (K independent chains per step).
+template <int K>
+__device__ __forceinline__ void q_mode_cells(const RhoArgs& ra, int n, const int* n2, float* out) {
+  float L[K], kb[K];
+#pragma unroll
+  for (int i = 0; i < K; ++i) {
+    const float lnn2 = logf((float)n2[i]);
+    L[i] = ra.log2kF + lnn2 * 0.72134752044448170368f;  // log2 k
+    kb[i] = -1.f + ra.c1 * expm1f(0.5f * ra.s * lnn2);
+  }
+  if (n <= 3) {
+    const float e = ra.s * (float)(n - 3) + ra.e4;
+#pragma unroll
+    for (int i = 0; i < K; ++i) out[i] = exp2f(e * L[i]);
+    return;
+  }
+  float P0[K], P1[K];
+#pragma unroll
+  for (int i = 0; i < K; ++i) {
+    P0[i] = 1.f;
+    P1[i] = kb[i];
+  }
+  for (int l = 2; l < n; ++l) {
+    const float A = ra.A[l], B = ra.B[l];
+#pragma unroll
+    for (int i = 0; i < K; ++i) {
+      const float Pn = A * kb[i] * P1[i] - B * P0[i];
+      P0[i] = P1[i];
+      P1[i] = Pn;
+    }
+  }
+  const float x0 = ra.x0[n - 1];
+#pragma unroll
+  for (int i = 0; i < K; ++i) out[i] = (P1[i] - x0) * exp2f(ra.e2 * L[i]);
+}
 
 // Neumaier's compensated step: s + c carries the running sum of the t's
 __device__ __forceinline__ void neumaier_add(float& s, float& c, float t) {

@@ -564,6 +564,8 @@ static RhoArgs rho_args(const Plan* p) {
   r.c1 = (float)(2 * kmin_s / (kmax_s - kmin_s));
   r.log2kF = (float)log2(kF);
   r.inv_kF2 = (float)(1 / (kF * kF));
+  r.e4 = (float)(4 - ns);
+  r.e2 = (float)(2 - ns);
   for (int n = 0; n < kMaxModes; ++n) r.x0[n] = n < (int)p->x0.size() ? (float)p->x0[n] : 0.f;
   for (int l = 1; l < kMaxModes; ++l) {
     r.A[l] = (float)((2.0 * l - 1) / l);
@@ -594,7 +596,7 @@ struct Launch {
   }
   static int modal(Plan* p, const ModalArgs& a, cudaStream_t st) {
     int64_t fs = fstride(p);
-    XinvOp<N, W> xo{a, p->d_phik, p->d_work, fs, tiles(p), p->nsq, p->HP, p->d_qtab, p->xpass_group};
+    XinvOp<N, W> xo{a, p->d_phik, p->d_work, fs, tiles(p), p->HP, rho_args(p), p->xpass_group};
     int rc = run_pass<N>(p, xo, tiles(p) * a.M, st, "modal_xinv");
     if (rc) return rc;
     if ((rc = ypass<+1>(p, p->d_work, a.M, nullptr, st, "modal_ypass_inv"))) return rc;
@@ -732,12 +734,14 @@ ModalArgs modal_args(Plan* p) {
   return a;
 }
 
-// Build the regrouped term list: sorted triples p <= q <= r with alpha != 0
-// contribute a f_p f_q to g_r (main.c:833-867); the counter-terms of
-// main.c:1045-1050 add -a012 t012 f_0 f_1 to g_2 and +a012 t012 f_0 f_2 to g_1.
-static int build_terms(Plan* p) {
-  int M = p->M;
-  auto A = [&](int i, int j, int k) { return p->alpha[((size_t)i * M + j) * M + k]; };
+// The regrouped term list by output slot: sorted triples p <= q <= r with
+// alpha != 0 contribute a f_p f_q to g_r (main.c:833-867); the
+// counter-terms of main.c:1045-1050 add -a012 t012 f_0 f_1 to g_2 and
+// +a012 t012 f_0 f_2 to g_1.  The second one sits in the list of r = 2 (its
+// target r stays 1): the row kernels form the slots in descending r and g_2
+// replaces f_2 in place, so f_0 f_2 is taken before that.
+std::vector<std::vector<Term>> regrouped_terms(const std::vector<double>& alpha, int M) {
+  auto A = [&](int i, int j, int k) { return alpha[((size_t)i * M + j) * M + k]; };
   std::vector<std::vector<Term>> by_r(M);
   for (int i = 0; i < M; ++i)
     for (int j = i; j < M; ++j)
@@ -747,9 +751,55 @@ static int build_terms(Plan* p) {
     double t012 = -A(1, 1, 1) / A(0, 1, 2);
     double c = A(0, 1, 2) * t012;
     by_r[2].push_back(Term{0, 1, 2, (float)(-c)});
-    // f_0 f_2 -> g_1 is evaluated in the r = 2 pass (before g_2 replaces f_2)
     by_r[2].push_back(Term{0, 2, 1, (float)(c)});
     if (by_r[1].empty()) by_r[1].push_back(Term{0, 0, 1, 0.f});  // keep a slot for r = 1
+  }
+  return by_r;
+}
+
+// Split of the active r over nparts cooperating plans, balanced by the
+// number of product terms each g_r takes: the r in decreasing term count
+// (ties: lower r first) each go to the part with the fewest terms so far
+// (ties: lower part).  part_of_r[r] = -1 for an r without terms.
+std::vector<int> modal_partition(const std::vector<std::vector<Term>>& by_r, int nparts) {
+  const int M = (int)by_r.size();
+  std::vector<int> cnt(M, 0), part(M, -1);
+  for (const auto& lst : by_r)
+    for (const Term& t : lst) cnt[t.r] += 1;
+  std::vector<int> order;
+  for (int r = 0; r < M; ++r)
+    if (!by_r[r].empty() || cnt[r] > 0) order.push_back(r);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cnt[a] > cnt[b]; });
+  std::vector<long> load(std::max(nparts, 1), 0);
+  for (int r : order) {
+    int best = 0;
+    for (int q = 1; q < nparts; ++q)
+      if (load[q] < load[best]) best = q;
+    part[r] = best;
+    load[best] += cnt[r];
+  }
+  return part;
+}
+
+// The plan's term list (device and host copies): the regrouped terms, or
+// with a modal partition only the slots of the plan's part.  A split keeps
+// the counter-term f_0 f_2 -> g_1 with the part of r = 1: as a term read
+// before g_2 replaces f_2 when r = 2 is in the same part, else as an
+// ordinary term of r = 1 (f_2 is never replaced in that part).
+static int build_terms(Plan* p) {
+  int M = p->M;
+  std::vector<std::vector<Term>> by_r = regrouped_terms(p->alpha, M);
+  if (p->modal_nparts > 1) {
+    const std::vector<int> part = modal_partition(by_r, p->modal_nparts);
+    const int me = p->modal_part;
+    std::vector<std::vector<Term>> mine(M);
+    for (int r = 0; r < M; ++r)
+      for (const Term& t : by_r[r]) {
+        if (part[t.r] != me) continue;
+        if (t.r != r && part[r] != me) mine[t.r].push_back(t);  // counter-term moves to its own slot
+        else mine[r].push_back(t);
+      }
+    by_r.swap(mine);
   }
   TermList tl{};
   std::vector<Term> flat;
@@ -788,6 +838,41 @@ int fused_prepare(Plan* p) {
 }
 
 static_assert(kRowThreads == kRowThreadsHost, "row kernel block size");
+
+// The plan's modal row kernel (NVRTC or generic) on nrows rows of caller
+// fields laid out with field stride nrows * HP: a harness that profiles the
+// row kernel on a few thousand rows without full-size fields.
+int profile_modal_rows(Plan* p, float2* work, int64_t nrows, cudaStream_t st) {
+  if (nrows < 1 || nrows > (int64_t)p->N * p->N) return set_err(p, "profile rows: 1 <= nrows <= N^2"), AAR_ERR_ARG;
+  if (p->nr_active == 0) return set_err(p, "profile rows: no modal terms"), AAR_ERR_STATE;
+  const int64_t fs = nrows * p->HP;
+  if (p->jit) return jit_modal_rows(p, work, fs, st, nrows);
+  return dispatch_n(p->N, [&](auto nc) {
+    constexpr int N = decltype(nc)::value;
+    ModalRowOp op;
+    const TermList& tl = *(const TermList*)p->host_terms.data();
+    const Term* ft = (const Term*)(p->host_terms.data() + sizeof(TermList));
+    constexpr int LS = RowCfg<N>::LS;
+    op.M = p->M;
+    op.nr = tl.nr;
+    for (int i = 0; i < kMaxModes; ++i) op.r_of_slot[i] = tl.r_of_slot[i];
+    for (int i = 0; i <= kMaxModes; ++i) op.begin[i] = tl.begin[i];
+    for (int sl = 0; sl < tl.nr; ++sl)
+      for (int i = tl.begin[sl]; i < tl.begin[sl + 1]; ++i) {
+        const uint32_t early = ft[i].r != tl.r_of_slot[sl] ? 1u : 0u;
+        op.t[i].off = (uint32_t)(ft[i].p * LS) | ((uint32_t)(ft[i].q * LS) << 16) | (early << 31);
+        op.t[i].c = ft[i].c;
+      }
+    const size_t sm_rows = sizeof(float2) * (size_t)(p->M + 1) * LS;
+    {
+      ProfScope ps_(p, "modal_rows", st);
+      k_rows<N, ModalRowOp><<<(unsigned)nrows, kRowThreads, sm_rows, st>>>(op, work, fs, p->HP, p->d_twN, p->d_twH);
+    }
+    AAR_CUDA_TRY(p, cudaGetLastError());
+    p->last_launches += 1;
+    return AAR_OK;
+  });
+}
 
 int fused_modal(Plan* p, cudaStream_t st) {
   ModalArgs a = modal_args(p);

@@ -240,15 +240,15 @@ int jit_prepare(Plan* p) {
   return AAR_OK;
 }
 
-int jit_modal_rows(Plan* p, float2* work, int64_t fs, cudaStream_t st) {
+int jit_modal_rows(Plan* p, float2* work, int64_t fs, cudaStream_t st, int64_t nrows) {
   JitState* j = (JitState*)p->jit;
   long long fsl = fs;
   int hp = p->HP;
   void* args[] = {&work, &fsl, &hp, &p->d_twN, &p->d_twH};
+  if (nrows < 0) nrows = (int64_t)p->N * p->N;
   {
     ProfScope ps_(p, "modal_rows", st);
-    AAR_CUDA_TRY(p, cudaLaunchKernel((const void*)j->kern, dim3((unsigned)((int64_t)p->N * p->N)),
-                                     dim3(j->threads), args, j->smem, st));
+    AAR_CUDA_TRY(p, cudaLaunchKernel((const void*)j->kern, dim3((unsigned)nrows), dim3(j->threads), args, j->smem, st));
   }
   p->last_launches += 1;
   return AAR_OK;

@@ -119,7 +119,10 @@ __device__ __forceinline__ void sincos_u48(uint64_t U, bool flip, float& c, floa
   }
 }
 
-template <bool FP64>
+// FP64: the amplitude and phase by the reference's FP64 formula
+// (main.c:443-459); OUT64: double2 output (the plain forms), else float2
+// (the fused form, FP64 math rounded at the end when FP64).
+template <bool FP64, bool OUT64 = FP64>
 __global__ void k_noise(NoiseArgs a, const uint32_t* __restrict__ seedtable, void* __restrict__ out, int HP) {
   const int N = a.g.N;
   int64_t col = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -158,6 +161,8 @@ __global__ void k_noise(NoiseArgs a, const uint32_t* __restrict__ seedtable, voi
       sincos(phase, &sn, &cs);
       re = phig * cs;
       im = phig * sn;
+      rf = (float)re;
+      imf = (float)im;
     } else {
       int n2 = kx * kx + ky * ky + k * k;
       float amp = __ldg(a.amp + n2);
@@ -182,7 +187,7 @@ __global__ void k_noise(NoiseArgs a, const uint32_t* __restrict__ seedtable, voi
       c1 = row_of(i, j, N, a.xb) * HP;
       c2 = row_of(ii, jj, N, a.xb) * HP;
     }
-    if (FP64) {
+    if (OUT64) {
       double2* o = (double2*)out;
       o[c1] = make_double2(re, im);
       if (c2 >= 0) o[c2] = make_double2(re, -im);
@@ -215,7 +220,10 @@ int launch_noise_fp32(Plan* p, const uint32_t* d_seed, float2* d_phik, cudaStrea
   int64_t cols = (int64_t)p->N * p->N;
   int bs = 128;
   { ProfScope ps_(p, "noise", st);
-  k_noise<false><<<(unsigned)((cols + bs - 1) / bs), bs, 0, st>>>(noise_args(p, kXB), d_seed, d_phik, p->HP);
+  if (p->prm.noise_fp64)
+    k_noise<true, false><<<(unsigned)((cols + bs - 1) / bs), bs, 0, st>>>(noise_args(p, kXB), d_seed, d_phik, p->HP);
+  else
+    k_noise<false><<<(unsigned)((cols + bs - 1) / bs), bs, 0, st>>>(noise_args(p, kXB), d_seed, d_phik, p->HP);
   }
   AAR_CUDA_TRY(p, cudaGetLastError());
   p->last_launches += 1;
@@ -291,6 +299,8 @@ int noalloc_gaussian(Plan* p, void* d_out, cudaStream_t st) {
   const unsigned nb = (unsigned)((total + 127) / 128);
   if (fp64)
     k_noise<true><<<nb, 128, 0, st>>>(noise_args(p, 1), seed, d_out, hp);
+  else if (p->prm.noise_fp64)
+    k_noise<true, false><<<nb, 128, 0, st>>>(noise_args(p, 1), seed, d_out, hp);
   else
     k_noise<false><<<nb, 128, 0, st>>>(noise_args(p, 1), seed, d_out, hp);
   AAR_CUDA_TRY(p, cudaGetLastError());

@@ -109,16 +109,21 @@ __device__ __forceinline__ void group_order(int64_t item, int64_t tiles, int nc,
   t = g * grp + (r - (int64_t)c * gs);
 }
 
-// First modal pass: item = (tile group, p, tile) (group_order); phi tile times q_p(n^2) (zero on
-// the cut, DC and padding columns), inverse x FFT, into field p.
+// First modal pass: item = (tile group, p, tile) (group_order); phi tile
+// times q_p(k) (zero on the cut, DC and padding columns), inverse x FFT,
+// into field p.  q_p is evaluated per cell in FP32 (q_mode_cells: the
+// Legendre recurrence and expm1 form of kbar the accumulation uses for
+// rho_r), before the tile wait, so its arithmetic overlaps the tile load; it
+// replaced a gather from a per-|k|^2 table (3 MB per mode), whose latency the
+// pass could not hide.
 template <int N, int W>
 struct XinvOp {
   ModalArgs a;
   const float2* phi;
   float2* work;
-  int64_t fs, tiles, nsq;
+  int64_t fs, tiles;
   int HP;
-  const float* qtab;
+  RhoArgs ra;
   int64_t grp;
   __device__ void coords(int64_t item, int& o, int& c0, int& p) const {
     int64_t t;
@@ -140,47 +145,64 @@ struct XinvOp {
     int o, c0, p;
     coords(item, o, c0, p);
     const int ky = sidx(o, N);
-    const float* q = qtab + (int64_t)p * nsq;
     if constexpr (C::E == 32 && stage_radix(N, C::E, 0) == 32 && C::THREADS == W * C::T && 32 % C::T == 0) {
       // value i of lane t is line element n = t + T i.  For n >= N/2 the
       // filter depends on |kx| = N - n, which is element 31 - i of lane
-      // (T - t) % T of the same line (same ky, kz): each lane gathers its
+      // (T - t) % T of the same line (same ky, kz): each lane evaluates its
       // 16 values below N/2 and takes the other 16 from its partner by
-      // shuffle (lane t = 0 pairs with itself one place off: it gathers all).
+      // shuffle.  Lane t = 0 pairs with itself one place off: |kx| = T (16 -
+      // j) is its own value 16 - j for j >= 1, and N/2 (j = 0) is one more
+      // evaluation.
       const int t = threadIdx.x % C::T, w = threadIdx.x / C::T;
       const int kz = c0 + w;
       const bool col = kz <= N / 2;
-      float g[16];
+      const int c2 = ky * ky + kz * kz;
+      int n2[16];
+      bool on[16];
 #pragma unroll
       for (int i = 0; i < 16; ++i) {
         const int kx = t + C::T * i;  // < N/2
-        const int n2 = kx * kx + ky * ky + kz * kz;
-        g[i] = col && n2 != 0 && keep_cell(a.g, kx, ky, kz) ? __ldg(q + n2) : 0.f;
+        n2[i] = kx * kx + c2;
+        on[i] = col && n2[i] != 0 && keep_cell(a.g, kx, ky, kz);
+        if (!on[i]) n2[i] = 1;  // a harmless argument; the value is dropped
+      }
+      float g[16];
+      q_mode_cells<16>(ra, p, n2, g);
+#pragma unroll
+      for (int i = 0; i < 16; ++i) {
+        g[i] = on[i] ? g[i] : 0.f;
         r.f[i] = g[i];
+      }
+      float gn = 0.f;  // lane 0: the value at n = N/2 (kx = -N/2)
+      if (t == 0) {
+        const int kx = -N / 2;
+        int m2[1] = {kx * kx + c2};
+        float v[1];
+        q_mode_cells<1>(ra, p, m2, v);
+        gn = col && keep_cell(a.g, kx, ky, kz) ? v[0] : 0.f;
       }
       const int lane = threadIdx.x & 31;
       const int src = (lane - t) + (C::T - t) % C::T;
 #pragma unroll
-      for (int j = 0; j < 16; ++j) r.f[16 + j] = __shfl_sync(0xffffffffu, g[15 - j], src);
-      if (t == 0) {
-#pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          const int kx = sidx(C::T * (16 + j), N);
-          const int n2 = kx * kx + ky * ky + kz * kz;
-          r.f[16 + j] = col && keep_cell(a.g, kx, ky, kz) ? __ldg(q + n2) : 0.f;
-        }
+      for (int j = 0; j < 16; ++j) {
+        const float v = __shfl_sync(0xffffffffu, g[15 - j], src);
+        r.f[16 + j] = t != 0 ? v : (j == 0 ? gn : g[j == 0 ? 0 : 16 - j]);
       }
     } else {
+      int n2[C::E];
+      bool on[C::E];
 #pragma unroll
       for (int i = 0; i < C::E; ++i) {
         int n, w;
         const bool own = fft_owned<N, W>(i, n, w);
-        int kz = c0 + w, kx = sidx(n, N);
-        int n2 = kx * kx + ky * ky + kz * kz;
-        float f = 0.f;
-        if (own && kz <= N / 2 && n2 != 0 && keep_cell(a.g, kx, ky, kz)) f = __ldg(q + n2);
-        r.f[i] = f;
+        const int kz = c0 + w, kx = sidx(n, N);
+        n2[i] = kx * kx + ky * ky + kz * kz;
+        on[i] = own && kz <= N / 2 && n2[i] != 0 && keep_cell(a.g, kx, ky, kz);
+        if (!on[i]) n2[i] = 1;
       }
+      q_mode_cells<C::E>(ra, p, n2, r.f);
+#pragma unroll
+      for (int i = 0; i < C::E; ++i) r.f[i] = on[i] ? r.f[i] : 0.f;
     }
   }
   __device__ bool pre(float2*, int64_t, const Early&) const { return false; }

@@ -18,9 +18,11 @@ from . import _lib
 from ._lib import AarError, check
 
 
-def params_from_config(cfg: dict, precision: int = _lib.AAR_FUSED_FP32, mem_limit_bytes: int = 0) -> _lib.Params:
+def params_from_config(cfg: dict, precision: int = _lib.AAR_FUSED_FP32, mem_limit_bytes: int = 0,
+                       noise_fp64: bool = False) -> _lib.Params:
     """C-ABI parameters of a parameter-file dict; a dict with the A_res /
-    w_res / phi_res tags is a 2LPTResBasis set."""
+    w_res / phi_res tags is a 2LPTResBasis set.  noise_fp64: the fused form's
+    RNG-to-amplitude step in FP64."""
     res = "A_res" in cfg
     return _lib.Params(
         nmesh=cfg["Nmesh"], nsample=cfg["Nsample"], nmax=cfg["Nmax"], seed=cfg["Seed"], box=cfg["Box"],
@@ -33,7 +35,7 @@ def params_from_config(cfg: dict, precision: int = _lib.AAR_FUSED_FP32, mem_limi
         precision=precision, mem_limit_bytes=mem_limit_bytes,
         variant=_lib.AAR_VARIANT_RESBASIS if res else _lib.AAR_VARIANT_BASIS,
         which_spectrum=cfg.get("WhichSpectrum", 0), a_res=cfg.get("A_res", 0.0), w_res=cfg.get("w_res", 0.0),
-        phi_res=cfg.get("phi_res", 0.0))
+        phi_res=cfg.get("phi_res", 0.0), noise_fp64=int(bool(noise_fp64)))
 
 
 def _ptr(t: torch.Tensor) -> int:
@@ -50,7 +52,7 @@ class ICGenerator:
     """One plan: grid, cosmology, coefficient tables and transfer function."""
 
     def __init__(self, cfg: dict, alpha: np.ndarray, x0: np.ndarray, k: np.ndarray, T: np.ndarray,
-                 precision: str = "fp32", device=None, mem_limit_bytes: int = 0):
+                 precision: str = "fp32", device=None, mem_limit_bytes: int = 0, noise_fp64: bool = False):
         self.L = _lib.load()
         self.cfg = dict(cfg)
         self.N = int(cfg["Nmesh"])
@@ -61,7 +63,7 @@ class ICGenerator:
         if precision not in forms:
             raise ValueError(f"precision must be one of {sorted(forms)}")
         self.precision = forms[precision]
-        prm = params_from_config(cfg, self.precision, mem_limit_bytes)
+        prm = params_from_config(cfg, self.precision, mem_limit_bytes, noise_fp64)
         h = C.c_void_p()
         with torch.cuda.device(self.device):
             rc = self.L.aar_plan_create(C.byref(prm), C.byref(h))
@@ -193,10 +195,20 @@ class ICGenerator:
         check(self.L, self.h, self.L.aar_r2c(self.h, _ptr(real), _ptr(out), self._stream()))
         return out
 
-    def readout(self, lagr: torch.Tensor):
+    def set_modal_partition(self, part: int, nparts: int) -> None:
+        """This plan's share of a modal sum split over radial modes
+        (aar_set_modal_partition; (0, 1) is the unsplit sum)."""
+        check(self.L, self.h, self.L.aar_set_modal_partition(self.h, int(part), int(nparts)))
+
+    def set_spectrum(self, spec: torch.Tensor) -> None:
+        """Replace the plan's potential spectrum (complex [N, N, N/2+1])."""
+        spec = spec.to(torch.complex64).contiguous()
+        check(self.L, self.h, self.L.aar_set_spectrum(self.h, _ptr(spec), self._stream()))
+
+    def readout(self, lagr: torch.Tensor, pos: torch.Tensor = None, vel: torch.Tensor = None):
         lagr = lagr.contiguous()
-        pos = torch.empty_like(lagr)
-        vel = torch.empty_like(lagr)
+        pos = torch.empty_like(lagr) if pos is None else pos
+        vel = torch.empty_like(lagr) if vel is None else vel
         check(self.L, self.h, self.L.aar_stage_readout(self.h, _ptr(lagr), lagr.shape[0], _ptr(pos), _ptr(vel),
                                                        self._stream()))
         return pos, vel

@@ -46,11 +46,11 @@ WORKLOADS = {
     "local_m8_n128": (128, 500.0, "local_m8_L500_n128", 8, 128, 10.0),
 }
 # Batching: 32 realisations at 256^3, Box 500, each with its own seed and a
-# template cycling over Local / Equilateral / ScalarI (mass 0.5, 1, 1.5) with
-# 6..16 modes, run as one CUDA graph (aar_batch_*).
+# template cycling over Local / Equilateral / ScalarI (mass 0.5, 1, 1.5, 1.75)
+# with 6..20 modes, run as one CUDA graph (aar_batch_*).
 BATCH_TEMPLATES = [("local_m6_L500_n256", 6, 10.0), ("equil_m9_L500_n256", 9, 100.0),
                    ("scalarI_m10_L500_n256", 10, 100.0), ("scalarI_m13_L500_n256_mu0p5", 13, 100.0),
-                   ("scalarI_m16_L500_n256_mu1p5", 16, 100.0)]
+                   ("scalarI_m16_L500_n256_mu1p5", 16, 100.0), ("scalarI_m20_L500_n256_mu1p75", 20, 100.0)]
 BATCH_WORKLOADS = {"batch32_n256": (32, 256, 500.0)}
 # modal decompositions (Decomposer.go): model, N_modes, Lbox, Nmax, model keywords, reference table
 DECOMP_WORKLOADS = {
@@ -71,6 +71,10 @@ def parse():
     ap.add_argument("--no-autotune", action="store_true", help="keep the default schedule (no aar_autotune)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-n", type=int, default=128)
+    ap.add_argument("--stages-only", action="store_true",
+                    help="profiling case: the field stages (noise, modal, 2LPT) only, no particle arrays")
+    ap.add_argument("--rows-harness", type=int, default=0, metavar="NROWS",
+                    help="profiling case: the modal row kernel alone on NROWS rows (aar_profile_modal_rows)")
     ap.add_argument("--no-plain", action="store_true",
                     help="skip the plain FP64 cuFFT forms (reference loop structure and regrouped, 1 step each)")
     return ap.parse_args()
@@ -511,6 +515,73 @@ def gpu_arm(args):
         dist.destroy_process_group()
 
 
+def stage_arm(args):
+    """Profiling case: the plan's field stages only (no particle arrays, so
+    the device holds just the plan's fields: ~7 GB at 512^3 with 12 modes)."""
+    import torch
+    from aarambam_gb300 import _lib
+    from aarambam_gb300.ic import ICGenerator
+    _lib.load(build_if_missing=True)
+    torch.cuda.set_device(0)
+    cfg = make_cfg(args.workload, 1234)
+    alpha, x0, k, t = load_tables(cfg["table"], cfg["N_modes"])
+    gen = ICGenerator(cfg, alpha, x0, k, t)
+    if not args.no_autotune:
+        gen.autotune()
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        for st in ("noise", "modal", "lpt"):
+            gen.stage(st)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        for st in ("noise", "modal", "lpt"):
+            gen.stage(st)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    print(json.dumps({"case": f"{args.workload} field stages", "ms_per_step": e0.elapsed_time(e1) / args.steps,
+                      "steps": args.steps, "device_bytes": gen.device_bytes}))
+
+
+def rows_arm(args):
+    """Profiling case: the modal row kernel of the workload's plan (NVRTC
+    kernel, 20 modes at 1024^3) on args.rows_harness rows of random fields
+    with a compact field stride (aar_profile_modal_rows)."""
+    import ctypes
+    import torch
+    from aarambam_gb300 import _lib
+    from aarambam_gb300.ic import ICGenerator
+    _lib.load(build_if_missing=True)
+    torch.cuda.set_device(0)
+    cfg = make_cfg(args.workload, 1234)
+    N, M = cfg["Nmesh"], cfg["N_modes"]
+    alpha, x0, k, t = load_tables(cfg["table"], M)
+    R = active_r(alpha)
+    gen = ICGenerator(cfg, alpha, x0, k, t)
+    HP = (N // 2 + 1 + 7) // 8 * 8
+    nrows = args.rows_harness
+    g = torch.Generator(device="cuda").manual_seed(3)
+    work = torch.randn((M + 1) * nrows * HP * 2, device="cuda", generator=g)
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+    def once():
+        _lib.check(gen.L, gen.h, gen.L.aar_profile_modal_rows(gen.h, work.data_ptr(), nrows, st))
+    for _ in range(args.warmup):
+        once()
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        once()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    byts = (M + R) * 8.0 * nrows * HP
+    print(json.dumps({"case": f"modal rows of {args.workload}, {nrows} rows", "jit": gen.jit_status,
+                      "ms_per_launch": ms, "alg_bytes": byts, "gbs": byts / ms / 1e6,
+                      "device_bytes": int(work.numel() * 4 + gen.device_bytes)}))
+
+
 def batch_arm(args):
     """Batching workload: all realisations of the batch per step, one graph
     launch (value = particles of all realisations / step time)."""
@@ -652,6 +723,10 @@ if __name__ == "__main__":
     a = parse()
     if a.impl == "reference":
         reference_arm(a)
+    elif a.stages_only:
+        stage_arm(a)
+    elif a.rows_harness:
+        rows_arm(a)
     elif a.workload in BATCH_WORKLOADS:
         batch_arm(a)
     elif a.workload in DECOMP_WORKLOADS:

@@ -62,6 +62,9 @@ typedef struct aar_params {
   int32_t variant;          /* AAR_VARIANT_BASIS or AAR_VARIANT_RESBASIS */
   int32_t which_spectrum;   /* WhichSpectrum: 0 for Basis; 0, 1 or 2 for ResBasis */
   double a_res, w_res, phi_res; /* ResBasis oscillation (ResBasis/read_param.c:88-99) */
+  int32_t noise_fp64;       /* fused form: 1 = RNG-to-amplitude step (phase, -ln u, sqrt, amplitude)
+                               in FP64 with the reference's formula, rounded to float at the end;
+                               0 (default) = FP32 from the exact 48-bit uniforms */
 } aar_params;
 
 /* Host scalars of the set-up: power.c:391-448 (Norm = sigma8 normalisation,
@@ -306,6 +309,24 @@ int aar_batch_launch_count(const aar_batch* batch);
 const char* aar_batch_last_error(const aar_batch* batch);
 void aar_batch_destroy(aar_batch* batch);
 
+/* ---- the modal sum split over radial modes (no counterpart in the
+   reference, which splits the grid into x-slabs over MPI ranks instead,
+   main.c:1556-1599) ----
+   acc = sum_r rho_r r2c(g_r) is a sum of independent terms once the Gaussian
+   potential is known, so nparts cooperating plans (one per GPU) each
+   regenerate the Gaussian potential from the seed and sum their own share
+   of the r; the shares add up to the unsplit sum.
+   aar_modal_partition: which part each r goes to (-1: r without terms),
+   balanced by the number of product terms per r; host only.
+   aar_set_modal_partition: this plan's part; its aar_stage_modal then adds
+   only its share, Fnl / N^3 sum_{r in part} rho_r r2c(g_r), to the Gaussian
+   potential.  The caller sums (spectrum after the modal stage - Gaussian
+   spectrum) over the parts, adds it to the Gaussian spectrum on one plan
+   (aar_set_spectrum) and continues there with aar_stage_lpt (see
+   aarambam_gb300/modal_split.py).  Fused form; (0, 1) is the unsplit sum. */
+int aar_modal_partition(const double* alpha_sym, int32_t n_modes, int32_t nparts, int32_t* part_of_r);
+int aar_set_modal_partition(aar_plan* plan, int32_t part, int32_t nparts);
+
 /* Run-time specialised modal row and accumulation kernels (no counterpart
    in the reference): mode 0 off, 1 (default) for Nmesh >= 256, 2 always.
    Both are compiled with NVRTC for the plan's alpha-term structure when the tables
@@ -324,6 +345,13 @@ const char* aar_jit_status(const aar_plan* plan);
    overwrites the plan's spectrum and fields.  `report` (may be NULL)
    receives one line per candidate, the chosen one marked '*'. */
 int aar_autotune(aar_plan* plan, char* report, int32_t len, void* stream);
+
+/* Profiling harness (no counterpart in the reference): the plan's modal row
+   kernel (the NVRTC one when in use) on nrows rows of caller fields, d_work
+   = M + 1 fields of nrows rows of HP = round_up(N/2+1, 8) complex float
+   each, field stride nrows * HP.  What a full modal stage runs on N^2 rows,
+   on a case small enough for a counter capture. */
+int aar_profile_modal_rows(aar_plan* plan, void* d_work, int64_t nrows, void* stream);
 
 /* Per-kernel timing: when enabled, CUDA events are recorded on the launching
    stream around every kernel; aar_profile_report synchronises the device and

@@ -719,6 +719,71 @@ void orc_modal_acc(const orc_params *p, int M, const double *alpha, const double
   free(g);
 }
 
+/* The same accumulation regrouped by linearity of the DFT, restricted to the
+   radial modes r with r_on[r] != 0 (the share of one part of a modal sum
+   split over r): acc = sum_r rho_r r2c(g_r), g_r = sum_{p<=q<=r}
+   alpha'_{pqr} f_p f_q, where alpha' is alpha on sorted triples plus the
+   two counter-terms of main.c:1045-1050 (-a012 t012 f_0 f_1 into g_2,
+   +a012 t012 f_0 f_2 into g_1).  Summed over all r it equals orc_modal_acc
+   up to rounding; the sum over a partition of the r equals the unsplit
+   one.  Checker of the split only (FP64, this file's own FFT). */
+void orc_modal_acc_regrouped(const orc_params *p, int M, const double *alpha, const double *x0,
+                             const double *phik, const int *r_on, double *acc) {
+  int N = p->N, H = N / 2 + 1;
+  size_t nc = (size_t)N * N * H, nr = (size_t)N * N * N;
+  double s = (4 - p->ns) / 3;
+#define A3(a, b, c) alpha[((size_t)(a) * M + (b)) * M + (c)]
+  orc_kcell *kc = (orc_kcell *)malloc(sizeof(orc_kcell) * nc);
+  orc_kgrid(p, kc);
+  double *spec = (double *)malloc(sizeof(double) * 2 * nc);
+  double *f = (double *)malloc(sizeof(double) * nr * M);
+  double *gr = (double *)malloc(sizeof(double) * nr);
+  double *G = (double *)malloc(sizeof(double) * 2 * nc);
+  for (int n = 0; n < M; ++n) {
+    orc_filter(p, kc, n, x0, phik, spec);
+    orc_c2r_3d(N, spec, f + (size_t)n * nr);
+  }
+  double a012 = M > 2 ? A3(0, 1, 2) : 0, t012 = (M > 2 && a012 != 0) ? -A3(1, 1, 1) / a012 : 0;
+  memset(acc, 0, sizeof(double) * 2 * nc);
+  for (int r = 0; r < M; ++r) {
+    if (!r_on[r]) continue;
+    memset(gr, 0, sizeof(double) * nr);
+    int any = 0;
+    for (int a = 0; a <= r; ++a)
+      for (int b = a; b <= r; ++b) {
+        double c = A3(a, b, r);
+        if (r == 2 && a == 0 && b == 1) c += -a012 * t012;
+        if (c == 0) continue;
+        any = 1;
+        const double *fa = f + (size_t)a * nr, *fb = f + (size_t)b * nr;
+#pragma omp parallel for schedule(static)
+        for (long x = 0; x < (long)nr; ++x) gr[x] += c * fa[x] * fb[x];
+      }
+    if (r == 1 && a012 * t012 != 0) { /* +a012 t012 f_0 f_2 into g_1 */
+      any = 1;
+      const double c = a012 * t012, *fa = f, *fb = f + 2 * nr;
+#pragma omp parallel for schedule(static)
+      for (long x = 0; x < (long)nr; ++x) gr[x] += c * fa[x] * fb[x];
+    }
+    if (!any) continue;
+    orc_r2c_3d(N, gr, G);
+#pragma omp parallel for schedule(static)
+    for (long c = 0; c < (long)nc; ++c) {
+      if (kc[c].skip) continue;
+      double w = orc_mode_out(r, kc[c].k1, kc[c].kbar, s, x0);
+      acc[2 * c] += w * G[2 * c];
+      acc[2 * c + 1] += w * G[2 * c + 1];
+    }
+  }
+  acc[0] = acc[1] = 0;
+#undef A3
+  free(kc);
+  free(spec);
+  free(f);
+  free(gr);
+  free(G);
+}
+
 /* main.c:1094-1150 */
 void orc_combine(const orc_params *p, double *phik, const double *acc, double *pot_gauss,
                  double *pot_ng) {

@@ -78,6 +78,8 @@ void orc_gauss_potential(const orc_params *p, const uint32_t *seedtable, double 
    alpha: symmetric [M][M][M]; x0: [M]. */
 void orc_modal_acc(const orc_params *p, int M, const double *alpha, const double *x0,
                    const double *phik, double *acc);
+void orc_modal_acc_regrouped(const orc_params *p, int M, const double *alpha, const double *x0,
+                             const double *phik, const int *r_on, double *acc);
 /* Total potential in place: phik <- phik + Fnl*acc/N^3 with the reference's
    two real-space round trips; DC zeroed.  If pot_gauss / pot_ng are non-null
    they receive the real-space fields the reference dumps (write_phi). */

@@ -84,6 +84,8 @@ def lib():
         L.orc_seedtable.argtypes = [C.c_int, C.c_int, up]
         L.orc_gauss_potential.argtypes = [C.POINTER(Params), up, dp]
         L.orc_modal_acc.argtypes = [C.POINTER(Params), C.c_int, dp, dp, dp, dp]
+        L.orc_modal_acc_regrouped.argtypes = [C.POINTER(Params), C.c_int, dp, dp, dp,
+                                              np.ctypeslib.ndpointer(np.int32, flags="C"), dp]
         L.orc_combine.argtypes = [C.POINTER(Params), dp, dp, C.c_void_p, C.c_void_p]
         L.orc_lpt_fields.argtypes = [C.POINTER(Params), dp, dp]
         L.orc_readout.argtypes = [C.POINTER(Params), dp, C.c_int64, fp, fp]
@@ -158,6 +160,18 @@ class Oracle:
         lib().orc_modal_acc(C.byref(self.p), M, np.ascontiguousarray(alpha, np.float64).ravel(),
                             np.ascontiguousarray(x0, np.float64), np.ascontiguousarray(phik).reshape(-1),
                             out.reshape(-1))
+        return out
+
+    def modal_acc_regrouped(self, alpha: np.ndarray, x0: np.ndarray, phik: np.ndarray, r_on=None) -> np.ndarray:
+        """The regrouped accumulation over the radial modes r with r_on[r]
+        (all when None): one part's share of a modal sum split over r."""
+        N = self.N
+        M = alpha.shape[0]
+        on = np.ones(M, np.int32) if r_on is None else np.ascontiguousarray(r_on, np.int32)
+        out = np.zeros((N, N, N // 2 + 1, 2), dtype=np.float64)
+        lib().orc_modal_acc_regrouped(C.byref(self.p), M, np.ascontiguousarray(alpha, np.float64).ravel(),
+                                      np.ascontiguousarray(x0, np.float64), np.ascontiguousarray(phik).reshape(-1),
+                                      on, out.reshape(-1))
         return out
 
     def combine(self, phik: np.ndarray, acc: np.ndarray, want_pot: bool = False):

@@ -8,7 +8,8 @@ from tests.common import bbks, make_cfg, table
 
 pytestmark = pytest.mark.gpu
 
-TEMPLATES = [("local_m6_L500_n256", 6), ("equil_m9_L500_n256", 9), ("scalarI_m10_L500_n256", 10)]
+TEMPLATES = [("local_m6_L500_n256", 6), ("equil_m9_L500_n256", 9), ("scalarI_m10_L500_n256", 10),
+             ("scalarI_m20_L500_n256_mu1p75", 20)]
 
 
 def lattice(N, box, dev):

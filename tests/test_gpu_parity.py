@@ -321,3 +321,28 @@ def test_run_glass_host_sync_and_async(cuda):
     torch.cuda.synchronize()
     for b, w in zip(bufs, want):
         assert all(torch.equal(x, y) for x, y in zip(b, w))
+
+
+@pytest.mark.parametrize("cfg", SMALL[:4], ids=lambda c: f"N{c['Nmesh']}_s{c['Seed']}")
+def test_gaussian_spectrum_fp64_amplitude(cuda, cfg):
+    """noise_fp64: the fused form's RNG-to-amplitude step in FP64 with the
+    reference's formula, rounded to float at the end -- bit-identical to the
+    plain FP64 form's Gaussian spectrum rounded to complex64, and within
+    float rounding of the FP64 oracle per cell."""
+    import ctypes as C
+    g = gen_for(cfg, noise_fp64=True)
+    g.stage("noise")
+    got = g.spectrum()
+    gp = gen_for(cfg, precision="fp64")
+    N = cfg["Nmesh"]
+    ref = torch.empty((N, N, N // 2 + 1), dtype=torch.complex128, device=cuda)
+    rc = gp.L.aar_gaussian_spectrum_noalloc(gp.h, ref.data_ptr(), C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert rc == 0
+    assert torch.equal(got, ref.to(torch.complex64))
+    k, t = bbks()
+    o = O.Oracle(cfg, k, t).gauss()
+    o = o[..., 0] + 1j * o[..., 1]
+    got = got.cpu().numpy()
+    nz = o != 0
+    assert np.array_equal(got != 0, nz)
+    assert (np.abs(got[nz] - o[nz]) / np.abs(o[nz])).max() < 2e-7

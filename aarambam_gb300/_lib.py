@@ -27,7 +27,7 @@ AAR_VARIANT_RESBASIS = 1
 # every symbol include/aarambam.h declares
 EXPORTS = [
     "aar_plan_create", "aar_set_tables", "aar_set_transfer", "aar_get_scalars", "aar_set_seed", "aar_run",
-    "aar_run_glass", "aar_run_host", "aar_run_glass_host", "aar_run_glass_host_async", "aar_wait_host_copies",
+    "aar_run_glass", "aar_run_host", "aar_run_glass_host", "aar_run_glass_host_async", "aar_run_lattice", "aar_wait_host_copies",
     "aar_plan_prepare", "aar_plan_device_bytes", "aar_modal_partition", "aar_set_modal_partition", "aar_seedtable", "aar_stage_noise", "aar_stage_modal", "aar_stage_lpt",
     "aar_stage_readout", "aar_stage_readout_glass", "aar_copy_spectrum", "aar_copy_field", "aar_gaussian_spectrum_noalloc", "aar_c2r", "aar_r2c", "aar_last_launch_count", "aar_profile_enable", "aar_profile_report",
     "aar_last_error", "aar_plan_destroy", "aar_version",
@@ -93,6 +93,7 @@ def load(build_if_missing: bool = False):
     L.aar_run_glass.argtypes = [vp, vp, i64, C.c_double, i32, vp, vp, vp, vp]
     L.aar_run_host.argtypes = [vp, vp, i64, vp, vp, vp]
     L.aar_run_glass_host.argtypes = [vp, vp, i64, C.c_double, i32, vp, vp, vp, vp]
+    L.aar_run_lattice.argtypes = [vp, i32, C.c_double, i32, vp, vp, vp, vp]
     L.aar_run_glass_host_async.argtypes = [vp, vp, i64, C.c_double, i32, vp, vp, vp, vp]
     L.aar_wait_host_copies.argtypes = [vp]
     L.aar_plan_prepare.argtypes = [vp]

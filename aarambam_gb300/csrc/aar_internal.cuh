@@ -114,6 +114,13 @@ struct Plan {
   int64_t glass_cap = 0;
   double* d_gscale = nullptr;  // glass_prepare: 3 nglass + tile products (read_glass.c:129-214)
   int64_t gscale_cap = 0;
+  // lattice read-out (lattice_prepare): per-axis Lagrangian coordinates (+ a
+  // flag word) and the parameter set they were made for
+  float* d_lpa = nullptr;
+  int lat_g = 0, lat_tile = 0;
+  double lat_box = 0;
+  bool lat_fused = false;
+  bool disp_real = false;  // the work slots 0..5 hold the real displacement fields
   float* d_gout = nullptr;  // [npart][3] pos, then [npart][3] vel, then npart int32 ids
   int64_t gout_cap = 0;
   int64_t gout_last = -1;   // particle count of the last host-buffer glass call
@@ -145,7 +152,12 @@ struct Term;
 std::vector<std::vector<Term>> regrouped_terms(const std::vector<double>& alpha, int M);
 std::vector<int> modal_partition(const std::vector<std::vector<Term>>& by_r, int nparts);
 int fused_modal(Plan* p, cudaStream_t st);
-int fused_lpt(Plan* p, cudaStream_t st);
+// rows = false stops before the displacement rows (fused_rows_lattice does them)
+int fused_lpt(Plan* p, cudaStream_t st, bool rows = true);
+int lattice_prepare(Plan* p, int g, double glass_box, int tile, cudaStream_t st, bool& fused);
+int lattice_glass(Plan* p, int g, double glass_box, float* d_glass, cudaStream_t st);
+int fused_rows_lattice(Plan* p, int g, int tile, float* d_pos, float* d_vel, int* d_ids, int64_t row0, int64_t nrows,
+                       cudaStream_t st);
 int fused_readout(Plan* p, const float* d_lagr, int64_t npart, float* d_pos, float* d_vel, cudaStream_t st);
 // glass_prepare makes the per-glass-particle and per-tile products of the
 // Lagrangian positions (plan-owned scratch); fused_readout_glass then reads

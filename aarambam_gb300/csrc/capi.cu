@@ -628,7 +628,8 @@ int aar_stage_readout(aar_plan* h, const float* d_lagr, int64_t npart, float* d_
   Plan* p = &h->p;
   p->last_launches = 0;
   if (p->prm.precision != AAR_FUSED_FP32) return set_err(p, "stage calls are for the fused form"), AAR_ERR_ARG;
-  if (!p->d_work || p->nwork < 6) return set_err(p, "no displacement fields: run the field stages first"), AAR_ERR_STATE;
+  if (!p->d_work || p->nwork < 6 || !p->disp_real)
+    return set_err(p, "no displacement fields: run the field stages first"), AAR_ERR_STATE;
   return fused_readout(p, d_lagr, npart, d_pos, d_vel, S(stream));
 }
 
@@ -637,7 +638,8 @@ int aar_stage_readout_glass(aar_plan* h, const float* d_glass, int64_t nglass, d
   if (!h || nglass < 0 || tile < 1 || !(glass_box > 0)) return AAR_ERR_ARG;
   Plan* p = &h->p;
   if (p->prm.precision != AAR_FUSED_FP32) return set_err(p, "stage calls are for the fused form"), AAR_ERR_ARG;
-  if (!p->d_work || p->nwork < 6) return set_err(p, "no displacement fields: run the field stages first"), AAR_ERR_STATE;
+  if (!p->d_work || p->nwork < 6 || !p->disp_real)
+    return set_err(p, "no displacement fields: run the field stages first"), AAR_ERR_STATE;
   p->last_launches = 0;
   int rc = glass_prepare(p, d_glass, nglass, glass_box, tile, S(stream));
   if (rc) return rc;
@@ -676,6 +678,36 @@ int aar_run_glass(aar_plan* h, const float* d_glass, int64_t nglass, double glas
 
 static int run_glass_host(Plan* p, const float* h_glass, int64_t nglass, double glass_box, int tile, float* h_pos,
                           float* h_vel, int32_t* h_ids, cudaStream_t st, bool sync);
+
+int aar_run_lattice(aar_plan* h, int32_t glass_n, double glass_box, int32_t tile, float* d_pos, float* d_vel,
+                    int32_t* d_ids, void* stream) {
+  if (!h || glass_n < 1 || tile < 1 || !(glass_box > 0) || !d_pos || !d_vel) return AAR_ERR_ARG;
+  Plan* p = &h->p;
+  int rc = ready(p);
+  if (rc) return rc;
+  if (p->prm.precision != AAR_FUSED_FP32) return set_err(p, "aar_run_lattice is for the fused form"), AAR_ERR_ARG;
+  cudaStream_t st = S(stream);
+  bool fused = false;
+  if ((rc = lattice_prepare(p, glass_n, glass_box, tile, st, fused))) return rc;
+  p->last_launches = 0;
+  if ((rc = run_noise(p, st))) return rc;
+  if ((rc = fused_modal(p, st))) return rc;
+  if ((rc = fused_lpt(p, st, !fused))) return rc;
+  if (fused) return fused_rows_lattice(p, glass_n, tile, d_pos, d_vel, d_ids, 0, (int64_t)p->N * p->N, st);
+  // general read-out from the lattice glass made on the device
+  const int64_t nglass = (int64_t)glass_n * glass_n * glass_n;
+  if (nglass > p->glass_cap) {
+    AAR_CUDA_TRY(p, cudaStreamSynchronize(st));
+    if (p->d_glass) cudaFree(p->d_glass), p->used_bytes -= sizeof(float) * 3 * (size_t)p->glass_cap;
+    p->d_glass = nullptr;
+    p->glass_cap = 0;
+    if ((rc = plan_alloc(p, (void**)&p->d_glass, sizeof(float) * 3 * (size_t)nglass))) return rc;
+    p->glass_cap = nglass;
+  }
+  if ((rc = lattice_glass(p, glass_n, glass_box, p->d_glass, st))) return rc;
+  if ((rc = glass_prepare(p, p->d_glass, nglass, glass_box, tile, st))) return rc;
+  return fused_readout_glass(p, nglass, tile, d_pos, d_vel, d_ids, st);
+}
 
 int aar_run_glass_host(aar_plan* h, const float* h_glass, int64_t nglass, double glass_box, int32_t tile,
                        float* h_pos, float* h_vel, int32_t* h_ids, void* stream) {
@@ -775,6 +807,22 @@ int aar_run_host(aar_plan* h, const float* h_lagr, int64_t npart, float* h_pos, 
   return AAR_OK;
 }
 
+// Is the host glass the regular g^3 lattice with coordinates
+// (float)(i * (glass_box / g)) in read_glass.c's particle order?
+static bool host_lattice(const float* gl, int64_t n, double glass_box, int& g) {
+  const int64_t c = llround(cbrt((double)n));
+  if (c < 1 || c * c * c != n) return false;
+  const double sp = glass_box / (double)c;
+  for (int64_t i = 0; i < n; ++i) {
+    const int64_t ix = i / (c * c), iy = (i / c) % c, iz = i % c;
+    if (gl[3 * i] != (float)((double)ix * sp) || gl[3 * i + 1] != (float)((double)iy * sp) ||
+        gl[3 * i + 2] != (float)((double)iz * sp))
+      return false;
+  }
+  g = (int)c;
+  return true;
+}
+
 // Host-buffer glass run (aar_run_glass_host / _async).  Read-out in chunks
 // of particles; chunk c goes to the host on side stream c % 2 as soon as it
 // is read out.  Chunk c's staging is reused by the next call only after the
@@ -829,18 +877,43 @@ static int run_glass_host(Plan* p, const float* h_glass, int64_t nglass, double 
   if (npart != p->gout_last && p->out_done[0])
     for (int i = 0; i < 2; ++i) AAR_CUDA_TRY(p, cudaStreamWaitEvent(st, p->out_done[i], 0));
   p->gout_last = npart;
-  if (nglass > 0)
+  // the reference's default glass is a regular lattice: when the host glass
+  // is one and its tiling lands every particle on a grid point, the
+  // read-out is fused into the displacement rows, chunk by chunk of tile
+  // rows (the rows of tile index ti are contiguous for g a multiple of the
+  // row block, and so are their particles)
+  int g = 0;
+  bool lat = false;
+  if (host_lattice(h_glass, nglass, glass_box, g) && g % kXB == 0 &&
+      (rc = lattice_prepare(p, g, glass_box, tile, st, lat)))
+    return rc;
+  if (nglass > 0 && !lat)
     AAR_CUDA_TRY(p, cudaMemcpyAsync(p->d_glass, h_glass, sizeof(float) * 3 * (size_t)nglass, cudaMemcpyHostToDevice, st));
   if ((rc = run_noise(p, st))) return rc;
   if ((rc = fused_modal(p, st))) return rc;
-  if ((rc = fused_lpt(p, st))) return rc;
-  if ((rc = glass_prepare(p, p->d_glass, nglass, glass_box, tile, st))) return rc;
-  const int nchunk = npart >= (int64_t)Plan::kGlassChunks * 65536 ? Plan::kGlassChunks : 1;
+  if ((rc = fused_lpt(p, st, !lat))) return rc;
+  if (!lat && (rc = glass_prepare(p, p->d_glass, nglass, glass_box, tile, st))) return rc;
+  const int nchunk = lat ? std::min(tile, (int)Plan::kGlassChunks)
+                         : (npart >= (int64_t)Plan::kGlassChunks * 65536 ? Plan::kGlassChunks : 1);
   for (int c = 0; c < nchunk; ++c) {
-    const int64_t a = npart * c / nchunk, b = npart * (c + 1) / nchunk, cnt = b - a;
+    int64_t a, b;
+    if (lat) {
+      const int64_t t0 = (int64_t)tile * c / nchunk, t1 = (int64_t)tile * (c + 1) / nchunk;
+      a = t0 * (int64_t)tile * tile * nglass;
+      b = t1 * (int64_t)tile * tile * nglass;
+    } else {
+      a = npart * c / nchunk;
+      b = npart * (c + 1) / nchunk;
+    }
+    const int64_t cnt = b - a;
     if (cnt == 0) continue;
     AAR_CUDA_TRY(p, cudaStreamWaitEvent(st, p->gchunk_free[c], 0));
-    if ((rc = fused_readout_glass(p, nglass, tile, d_pos, d_vel, d_ids, st, a, b))) return rc;
+    if (lat) {
+      const int64_t t0 = (int64_t)tile * c / nchunk, t1 = (int64_t)tile * (c + 1) / nchunk;
+      if ((rc = fused_rows_lattice(p, g, tile, d_pos, d_vel, d_ids, t0 * g * p->N, (t1 - t0) * g * p->N, st))) return rc;
+    } else if ((rc = fused_readout_glass(p, nglass, tile, d_pos, d_vel, d_ids, st, a, b))) {
+      return rc;
+    }
     cudaStream_t os = p->out_stream[c & 1];
     AAR_CUDA_TRY(p, cudaEventRecord(p->gchunk_read[c], st));
     AAR_CUDA_TRY(p, cudaStreamWaitEvent(os, p->gchunk_read[c], 0));
@@ -949,7 +1022,7 @@ int aar_copy_field(aar_plan* h, int32_t which, void* d_out, void* stream) {
   if (!h || !d_out || which < 0 || which > 5) return AAR_ERR_ARG;
   Plan* p = &h->p;
   if (is_plain(p->prm)) return plain_copy_field(p, which, (double*)d_out, S(stream));
-  if (p->prm.precision != AAR_FUSED_FP32 || !p->d_work || which >= p->nwork)
+  if (p->prm.precision != AAR_FUSED_FP32 || !p->d_work || which >= p->nwork || !p->disp_real)
     return set_err(p, "no FP32 displacement fields in this plan: run the field stages first"), AAR_ERR_STATE;
   int N = p->N;
   const float* src = (const float*)(p->d_work + (size_t)which * N * N * p->HP);

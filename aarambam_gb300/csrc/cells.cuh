@@ -75,26 +75,28 @@ struct RhoArgs {
 
 // Field filter q_n(k) of main.c:580-637 at K cells (n2[i] = |k|^2 in grid
 // units, > 0) in FP32: k^(s (n-3)) k^(4-ns) for n <= 3, (P_{n-1}(kbar) -
-// X0[n-1]) k^(2-ns) above, with kbar and P_l as for rho_n (RhoArgs).  The K
-// recurrences run in lockstep (K independent chains per step).
+// X0[n-1]) k^(2-ns) above, with P_l as for rho_n (RhoArgs).  With k = kF
+// sqrt(n2) and kmin = kF, kbar = -1 + c1 (n2^(s/2) - 1): for integer n2 >= 1
+// the bracket is 0 or at least 2^(s/2) - 1 ~ 0.42, so it has no cancellation
+// and the hardware base-2 logarithm and exponential (absolute error ~2^-22
+// in the exponent; ~4e-7 relative in q) replace logf / expm1f: three
+// special-function operations per cell.  The K recurrences run in lockstep
+// (K independent chains per step).
 template <int K>
 __device__ __forceinline__ void q_mode_cells(const RhoArgs& ra, int n, const int* n2, float* out) {
-  float L[K], kb[K];
+  float lg[K];
 #pragma unroll
-  for (int i = 0; i < K; ++i) {
-    const float lnn2 = logf((float)n2[i]);
-    L[i] = ra.log2kF + lnn2 * 0.72134752044448170368f;  // log2 k
-    kb[i] = -1.f + ra.c1 * expm1f(0.5f * ra.s * lnn2);
-  }
+  for (int i = 0; i < K; ++i) lg[i] = __log2f((float)n2[i]);  // log2 n2
   if (n <= 3) {
     const float e = ra.s * (float)(n - 3) + ra.e4;
 #pragma unroll
-    for (int i = 0; i < K; ++i) out[i] = exp2f(e * L[i]);
+    for (int i = 0; i < K; ++i) out[i] = exp2f(e * fmaf(0.5f, lg[i], ra.log2kF));
     return;
   }
-  float P0[K], P1[K];
+  float kb[K], P0[K], P1[K];
 #pragma unroll
   for (int i = 0; i < K; ++i) {
+    kb[i] = fmaf(ra.c1, exp2f(0.5f * ra.s * lg[i]), -1.f - ra.c1);
     P0[i] = 1.f;
     P1[i] = kb[i];
   }
@@ -109,7 +111,7 @@ __device__ __forceinline__ void q_mode_cells(const RhoArgs& ra, int n, const int
   }
   const float x0 = ra.x0[n - 1];
 #pragma unroll
-  for (int i = 0; i < K; ++i) out[i] = (P1[i] - x0) * exp2f(ra.e2 * L[i]);
+  for (int i = 0; i < K; ++i) out[i] = (P1[i] - x0) * exp2f(ra.e2 * fmaf(0.5f, lg[i], ra.log2kF));
 }
 
 // Neumaier's compensated step: s + c carries the running sum of the t's

@@ -350,6 +350,14 @@ struct ZTypes {
   int t[6];
   float kF;
   const float* isinc2;
+  // t[i] by selects (a dynamic index into the parameter block would copy it
+  // to local memory)
+  __device__ __forceinline__ int at(int i) const {
+    int r = t[0];
+#pragma unroll
+    for (int j = 1; j < 6; ++j) r = i == j ? t[j] : r;
+    return i < 6 ? r : 0;
+  }
 };
 template <int N>
 __global__ void __launch_bounds__(256) k_rows_c2r(float2* work, int64_t fs, int HP, int first, int64_t nrows,
@@ -365,7 +373,7 @@ __global__ void __launch_bounds__(256) k_rows_c2r(float2* work, int64_t fs, int 
   bool act = row < nrows && sub < C::LPW;
   float2* line = sm + (warp * C::LPW + sub) * C::LS;
   float2* f = work + (int64_t)(first + blockIdx.y) * fs + (act ? row : 0) * HP;
-  const ZFac zf{blockIdx.y < 6 ? zt.t[blockIdx.y] : 0, zt.kF, zt.isinc2};
+  const ZFac zf{zt.at(blockIdx.y), zt.kF, zt.isinc2};
   if constexpr (RowFold<N>::value) {
     // folded radix-2 (rows.cuh): the halves hold z_{2m} and z_{2m+1}; lane
     // t writes the pair (z_{2m}, z_{2m+1}) as one 16-byte store
@@ -403,6 +411,50 @@ struct ReadArgs {
   float nb_hi, nb_lo;  // N / Box as a two-float sum
 };
 
+// Cell index and fraction of one coordinate: u = Pos N / Box
+// (main.c:1444-1446) to ~1e-7 of a cell in FP32 -- the product with a
+// two-float split of N/Box -- then the cell index and the fraction with the
+// reference's clamps (main.c:1452-1463).
+__device__ __forceinline__ void cell_coord(const ReadArgs& a, float p, int& i, float& f) {
+  const int N = a.N;
+  float hi = p * a.nb_hi;
+  float lo = fmaf(p, a.nb_hi, -hi) + p * a.nb_lo;
+  if (!(hi >= 0.f)) {  // also catches NaN: the cell index stays inside the grid
+    hi = 0.f;
+    lo = 0.f;
+  }
+  if (hi > (float)N) {
+    hi = (float)N;
+    lo = 0.f;
+  }
+  const float fl = floorf(hi);
+  i = (int)fl;
+  f = (hi - fl) + lo;  // hi - fl is exact
+  if (f < 0.f) {
+    i -= 1;
+    f += 1.f;
+  } else if (f >= 1.f) {
+    i += 1;
+    f -= 1.f;
+  }
+  if (i < 0) {  // (int) truncates: u in (-1, 0) reads cell 0 with a negative fraction
+    f = (float)i + f;
+    i = 0;
+  }
+  if (i >= N) {
+    f += (float)(i - (N - 1));
+    i = N - 1;
+  }
+}
+
+// Position and velocity of a particle at Lagrangian coordinate p from its
+// ZA and 2LPT displacements d1, d2 (main.c:1486-1509): Pos += dis - 3/7
+// dis2 / N^3 with the periodic wrap, Vel = dis vp1 - 3/7 dis2 / N^3 vp2.
+__device__ __forceinline__ void move_particle(const ReadArgs& a, const float* p, const float* dis, const float* dis2,
+                                              float* op, float* ov) {
+  move_particle(a, p, dis, dis2, op, ov);
+}
+
 __device__ __forceinline__ void readout_one(const ReadArgs& a, const float* __restrict__ F, float px, float py,
                                             float pz, float* op, float* ov) {
   const int N = a.N;
@@ -410,40 +462,8 @@ __device__ __forceinline__ void readout_one(const ReadArgs& a, const float* __re
   int ii[3], jj[3];
   float fr[3];
   for (int d = 0; d < 3; ++d) {
-    // u = Pos N / Box (main.c:1444-1446) to ~1e-7 of a cell in FP32: the
-    // product with a two-float split of N/Box, then the cell index and the
-    // fraction with the reference's clamps (main.c:1452-1463)
-    float hi = p[d] * a.nb_hi;
-    float lo = fmaf(p[d], a.nb_hi, -hi) + p[d] * a.nb_lo;
-    if (!(hi >= 0.f)) {  // also catches NaN: the cell index stays inside the grid
-      hi = 0.f;
-      lo = 0.f;
-    }
-    if (hi > (float)N) {
-      hi = (float)N;
-      lo = 0.f;
-    }
-    const float fl = floorf(hi);
-    int i = (int)fl;
-    float f = (hi - fl) + lo;  // hi - fl is exact
-    if (f < 0.f) {
-      i -= 1;
-      f += 1.f;
-    } else if (f >= 1.f) {
-      i += 1;
-      f -= 1.f;
-    }
-    if (i < 0) {  // (int) truncates: u in (-1, 0) reads cell 0 with a negative fraction
-      f = (float)i + f;
-      i = 0;
-    }
-    if (i >= N) {
-      f += (float)(i - (N - 1));
-      i = N - 1;
-    }
-    fr[d] = f;
-    ii[d] = i;
-    jj[d] = (i + 1 == N) ? 0 : i + 1;
+    cell_coord(a, p[d], ii[d], fr[d]);
+    jj[d] = (ii[d] + 1 == N) ? 0 : ii[d] + 1;
   }
   const int64_t rs = 2 * (int64_t)a.HP;
   float u = fr[0], v = fr[1], w = fr[2];
@@ -533,6 +553,118 @@ __global__ void k_readout_glass(ReadArgs a, const float* __restrict__ F, const d
     vel[3 * n + d] = ov[d];
   }
   if (ids) ids[n] = (int)(n + 1);
+}
+
+// ----------------------------------------------------------- lattice read-out
+// Particles of the regular g^3 lattice glass (per-axis glass coordinate
+// (float)(i * glass_box / g), the particle order of read_glass.c:181-214)
+// tiled tile^3 times.  k_lattice_axis makes the Lagrangian coordinate of
+// every lattice index of one axis with the operations of the general glass
+// path (k_glass_scale + k_readout_glass) and flags any that is not exactly
+// on its own grid point by the reference's own FP64 cell coordinate u = Pos
+// / Box * Nmesh (main.c:1444-1446): u must equal the index.  When none is
+// flagged and g tile = Nmesh, every particle sits on a grid point and reads
+// just the grid value under it (the weights of the other seven corners are
+// zero), so the read-out can be fused into the displacement rows:
+// k_rows_lattice.  (The FP32 read-out's two-float coordinate can leave a
+// fraction of ~1e-12 at such a point, which weights the neighbour by as
+// much; the fused read-out takes the grid value, as the FP64 reference
+// does.)
+__global__ void k_lattice_axis(int N, double box, int g, double gsp, double glass_box, double bot, float* lpa,
+                               int* off_grid) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const int gi = i % g, ti = i / g;
+  const float gc = (float)__dmul_rn((double)gi, gsp);
+  const float lp = (float)__dadd_rn(__dmul_rn(__ddiv_rn((double)gc, glass_box), bot), __dmul_rn((double)ti, bot));
+  lpa[i] = lp;
+  const double u = __dmul_rn(__ddiv_rn((double)lp, box), (double)N);
+  if (u != (double)i) atomicOr(off_grid, 1);
+}
+
+// The lattice glass itself (3 g^3 floats), for the general read-out.
+__global__ void k_lattice_glass(int g, double gsp, float* glass) {
+  const int64_t n = (int64_t)g * g * g;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t ix = i / ((int64_t)g * g), iy = (i / g) % g, iz = i % g;
+    glass[3 * i] = (float)__dmul_rn((double)ix, gsp);
+    glass[3 * i + 1] = (float)__dmul_rn((double)iy, gsp);
+    glass[3 * i + 2] = (float)__dmul_rn((double)iz, gsp);
+  }
+}
+
+// The six displacement rows of RPB memory rows (c2r with the z factors, as
+// k_rows_c2r; warp c takes field c), then the particles on the rows' grid
+// points: Pos / Vel from the grid values (readout_one's on-grid branch,
+// main.c:1486-1509) and IDs, written at their tiled-glass particle index.
+// Rows [row0, row0 + nrows) of the x-blocked order.
+template <int N>
+struct LatticeCfg {
+  static constexpr int RPB = RowFold<N>::value ? 1 : RowCfg<N>::LPW;  // rows per block
+  static constexpr size_t SMEM = sizeof(float2) * (size_t)RPB * 6 * RowCfg<N>::LS;
+};
+template <int N>
+__global__ void __launch_bounds__(192, 4) k_rows_lattice(const float2* __restrict__ work, int64_t fs, int HP,
+                                                         const float2* __restrict__ twN, const float2* __restrict__ twH,
+                                                         ZTypes zt, ReadArgs ra, int g, int tile,
+                                                         const float* __restrict__ lpa, float* pos, float* vel,
+                                                         int* ids, int64_t row0, int64_t nrows) {
+  using C = RowCfg<N>;
+  constexpr int H = C::H, RPB = LatticeCfg<N>::RPB;
+  extern __shared__ float2 sm[];  // [RPB][6][LS]
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t rbase = row0 + (int64_t)blockIdx.x * RPB, rend = row0 + nrows;
+  const ZFac zf{zt.at(warp), zt.kF, zt.isinc2};
+  if constexpr (RowFold<N>::value) {
+    constexpr int h = H / 2, HO = h + h / 16;
+    const bool act = rbase < rend;
+    float2* line = sm + warp * C::LS;
+    if (act) row_c2r_pre_fold<N, true>(line, lane, twN, twH, zf, work + (int64_t)warp * fs + rbase * HP);
+    __syncwarp();
+    line_fft_smem<h, 16, +1, 0, 0, 2>(line + (lane >> 4) * HO, lane & 15, twH, act);
+  } else {
+    const int sub = lane / C::T, t = lane % C::T;
+    const int64_t row = rbase + sub;
+    const bool act = sub < RPB && row < rend;
+    float2* line = sm + ((act ? sub : 0) * 6 + warp) * C::LS;
+    if (act) row_c2r_pre<N>(work + (int64_t)warp * fs + row * HP, line, t, C::T, twN, zf);
+    __syncwarp();
+    line_fft_smem<H, C::T, +1>(line, t, twH, act);
+  }
+  __syncthreads();
+  const int64_t g3 = (int64_t)g * g * g;
+  for (int q = threadIdx.x; q < RPB * N; q += blockDim.x) {
+    const int sub = q / N, z = q - sub * N;
+    const int64_t row = rbase + sub;
+    if (row >= rend) break;
+    int x, y;
+    row_xy(row, N, kXB, x, y);
+    float d[6];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+      float2 v;
+      if constexpr (RowFold<N>::value) {
+        // the folded transform leaves z_{2m} at m and z_{2m+1} at h + m
+        // (z_j = (x_{2j}, x_{2j+1})): x_z sits in the pair of z / 4
+        constexpr int h = H / 2, HO = h + h / 16;
+        v = sm[c * C::LS + spad(z >> 2) + (((z >> 1) & 1) ? HO : 0)];
+      } else {
+        v = sm[(sub * 6 + c) * C::LS + spad(z >> 1)];
+      }
+      d[c] = (z & 1) ? v.y : v.x;
+    }
+    const float p[3] = {lpa[x], lpa[y], lpa[z]};
+    float op[3], ov[3];
+    move_particle(ra, p, d, d + 3, op, ov);
+    const int ti = x / g, gi = x - ti * g, tj = y / g, gj = y - tj * g, tk = z / g, gk = z - tk * g;
+    const int64_t n = (((int64_t)ti * tile + tj) * tile + tk) * g3 + ((int64_t)gi * g + gj) * g + gk;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      pos[3 * n + c] = op[c];
+      vel[3 * n + c] = ov[c];
+    }
+    if (ids) ids[n] = (int)(n + 1);
+  }
 }
 
 // ----------------------------------------------------------- host side
@@ -658,7 +790,7 @@ struct Launch {
   // ky; yy: ky^2); the source rows apply the z factors (xz, yz: kz; zz:
   // kz^2) and write S to 6; psi1 (0..2) and psi2 (3..5) likewise from x
   // outputs in 0, 8 (psi1) and 3, 7 (psi2).
-  static int lpt(Plan* p, const LptArgs& a, cudaStream_t st) {
+  static int lpt(Plan* p, const LptArgs& a, cudaStream_t st, bool rows = true) {
     int64_t fs = fstride(p);
     float2* phit = p->d_work + 7 * fs;  // T/(D Beta) phi, read by the Hessian and psi1 passes
     {
@@ -697,6 +829,10 @@ struct Launch {
       YFanOp<N, W> yf{a, p->d_work, fs, tiles(p), p->HP, {0, 8, 8, 3, 7, 7}, {0, 1, 2, 3, 4, 5}, {3, 4, 3, 3, 4, 3}, 1};
       if ((rc = run_pass<N>(p, yf, tiles(p) * 6, st, "lpt_ypass_inv_disp"))) return rc;
     }
+    // the displacement rows: here, or fused with the lattice read-out
+    // (fused_rows_lattice), which leaves no real fields behind
+    p->disp_real = rows;
+    if (!rows) return AAR_OK;
     using R = RowCfg<N>;
     int lines_per_block = 8 * R::LPW;
     int64_t nrows = (int64_t)N * N;
@@ -891,9 +1027,9 @@ LptArgs lpt_args(Plan* p) {
   return a;
 }
 
-int fused_lpt(Plan* p, cudaStream_t st) {
+int fused_lpt(Plan* p, cudaStream_t st, bool rows) {
   LptArgs a = lpt_args(p);
-  return dispatch_n(p->N, [&](auto nc) { return Launch<decltype(nc)::value>::lpt(p, a, st); });
+  return dispatch_n(p->N, [&](auto nc) { return Launch<decltype(nc)::value>::lpt(p, a, st, rows); });
 }
 
 static ReadArgs read_args(Plan* p) {
@@ -922,6 +1058,66 @@ int fused_readout(Plan* p, const float* d_lagr, int64_t npart, float* d_pos, flo
   AAR_CUDA_TRY(p, cudaGetLastError());
   p->last_launches += 1;
   return AAR_OK;
+}
+
+// Lattice read-out set-up for (g, glass_box, tile): the per-axis Lagrangian
+// coordinates and whether the rows can read out (see k_lattice_axis); made
+// once per parameter set (one synchronisation), then cached.
+int lattice_prepare(Plan* p, int g, double glass_box, int tile, cudaStream_t st, bool& fused) {
+  fused = false;
+  if ((int64_t)g * tile != p->N) return AAR_OK;
+  if (p->lat_g == g && p->lat_box == glass_box && p->lat_tile == tile) {
+    fused = p->lat_fused;
+    return AAR_OK;
+  }
+  int rc;
+  if (!p->d_lpa && (rc = plan_alloc(p, (void**)&p->d_lpa, sizeof(float) * (p->N + 1)))) return rc;
+  int* d_flag = (int*)(p->d_lpa + p->N);
+  AAR_CUDA_TRY(p, cudaMemsetAsync(d_flag, 0, sizeof(int), st));
+  k_lattice_axis<<<(p->N + 255) / 256, 256, 0, st>>>(p->N, p->prm.box, g, glass_box / g, glass_box, p->prm.box / tile,
+                                                      p->d_lpa, d_flag);
+  AAR_CUDA_TRY(p, cudaGetLastError());
+  int flag = 1;
+  AAR_CUDA_TRY(p, cudaMemcpyAsync(&flag, d_flag, sizeof(int), cudaMemcpyDeviceToHost, st));
+  AAR_CUDA_TRY(p, cudaStreamSynchronize(st));
+  p->lat_g = g;
+  p->lat_box = glass_box;
+  p->lat_tile = tile;
+  p->lat_fused = flag == 0;
+  fused = p->lat_fused;
+  return AAR_OK;
+}
+
+int lattice_glass(Plan* p, int g, double glass_box, float* d_glass, cudaStream_t st) {
+  const int64_t n = (int64_t)g * g * g;
+  k_lattice_glass<<<(unsigned)std::min<int64_t>((n + 255) / 256, (int64_t)p->num_sms * 8), 256, 0, st>>>(
+      g, glass_box / g, d_glass);
+  AAR_CUDA_TRY(p, cudaGetLastError());
+  p->last_launches += 1;
+  return AAR_OK;
+}
+
+// The displacement rows with the lattice read-out fused (rows [row0, row0 +
+// nrows) of the x-blocked order; lattice_prepare said fused).
+int fused_rows_lattice(Plan* p, int g, int tile, float* d_pos, float* d_vel, int* d_ids, int64_t row0, int64_t nrows,
+                       cudaStream_t st) {
+  if (nrows <= 0) return AAR_OK;
+  const LptArgs la = lpt_args(p);
+  const ZTypes zt{{3, 3, 4, 3, 3, 4}, la.m.g.kF, la.isinc2};
+  return dispatch_n(p->N, [&](auto nc) {
+    constexpr int N = decltype(nc)::value;
+    using L = LatticeCfg<N>;
+    AAR_CUDA_TRY(p, cudaFuncSetAttribute(k_rows_lattice<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::SMEM));
+    {
+      ProfScope ps_(p, "lpt_rows_readout", st);
+      k_rows_lattice<N><<<(unsigned)((nrows + L::RPB - 1) / L::RPB), 192, L::SMEM, st>>>(
+          p->d_work, (int64_t)N * N * p->HP, p->HP, p->d_twN, p->d_twH, zt, read_args(p), g, tile, p->d_lpa, d_pos,
+          d_vel, d_ids, row0, nrows);
+    }
+    AAR_CUDA_TRY(p, cudaGetLastError());
+    p->last_launches += 1;
+    return AAR_OK;
+  });
 }
 
 int glass_prepare(Plan* p, const float* d_glass, int64_t nglass, double glass_box, int tile, cudaStream_t st) {

@@ -179,20 +179,53 @@ __device__ __forceinline__ float2 post1(float2 z, float2 zr, float2 w) {
 
 // X from the line buffer (in place, GLOBAL false) or from the row in global
 // memory (GLOBAL true, `src`)
+// One quad of the folded pre-step: a = X_k, b = X_{H-k}, c = X_{h-k},
+// d = X_{h+k} (see row_c2r_pre_fold).
+template <int N>
+__device__ __forceinline__ void pre_fold_quad(float2* line, int k, float2 a, float2 b, float2 c, float2 d,
+                                              const float2* __restrict__ twN, const float2* __restrict__ twH,
+                                              ZFac zf);
+
 template <int N, bool GLOBAL = false>
 __device__ __forceinline__ void row_c2r_pre_fold(float2* line, int lane, const float2* __restrict__ twN,
                                                  const float2* __restrict__ twH, ZFac zf,
                                                  const float2* __restrict__ src = nullptr) {
   constexpr int H = N / 2, h = H / 2, Q = H / 4;
-  for (int k = lane; k <= Q; k += 32) {
+  if constexpr (GLOBAL) {
+    // all of the lane's loads first (independent, in flight together), then
+    // the quads: the loads of one quad no longer wait for the previous
+    // quad's arithmetic and stores
+    constexpr int NIT = (Q + 32) / 32;  // quads k = lane + 32 it <= Q
+    float2 qa[NIT], qb[NIT], qc[NIT], qd[NIT];
+#pragma unroll
+    for (int it = 0; it < NIT; ++it) {
+      const int k = lane + 32 * it;
+      if (k <= Q) {
+        qa[it] = src[k];
+        qb[it] = src[H - k];
+        qc[it] = src[h - k];
+        qd[it] = src[h + k];
+      }
+    }
+#pragma unroll
+    for (int it = 0; it < NIT; ++it) {
+      const int k = lane + 32 * it;
+      if (k <= Q) pre_fold_quad<N>(line, k, qa[it], qb[it], qc[it], qd[it], twN, twH, zf);
+    }
+    return;
+  }
+  for (int k = lane; k <= Q; k += 32)
+    pre_fold_quad<N>(line, k, line[spad(k)], line[spad(H - k)], line[spad(h - k)], line[spad(h + k)], twN, twH, zf);
+}
+
+template <int N>
+__device__ __forceinline__ void pre_fold_quad(float2* line, int k, float2 a, float2 b, float2 c, float2 d,
+                                              const float2* __restrict__ twN, const float2* __restrict__ twH,
+                                              ZFac zf) {
+  constexpr int H = N / 2, h = H / 2, Q = H / 4;
+  {
     const float2 wk = __ldg(twN + k);  // e^{-2 pi i k/N}
     const float2 vk = __ldg(twH + k);  // e^{-2 pi i k/H}
-    float2 a, b, c, d;
-    if constexpr (GLOBAL) {
-      a = src[k], b = src[H - k], c = src[h - k], d = src[h + k];
-    } else {
-      a = line[spad(k)], b = line[spad(H - k)], c = line[spad(h - k)], d = line[spad(h + k)];
-    }
     if (zf.type) {
       a = cscale(a, zf.at(k));
       b = cscale(b, zf.at(H - k));

@@ -232,6 +232,19 @@ class ICGenerator:
                                                    _ptr(pos), _ptr(vel), _ptr(ids), self._stream()))
         return pos, vel, ids
 
+    def run_lattice(self, glass_n: int, glass_box: float, tile: int, pos: torch.Tensor = None,
+                    vel: torch.Tensor = None, ids: torch.Tensor = None):
+        """Whole path for the regular glass_n^3 lattice glass tiled tile^3
+        times (aar_run_lattice): no glass array; pos / vel float32 [n, 3]
+        and ids int32 [n] (optional) on the device."""
+        n = glass_n ** 3 * tile ** 3
+        pos = torch.empty((n, 3), dtype=torch.float32, device=self.device) if pos is None else pos
+        vel = torch.empty((n, 3), dtype=torch.float32, device=self.device) if vel is None else vel
+        check(self.L, self.h, self.L.aar_run_lattice(self.h, int(glass_n), float(glass_box), int(tile), _ptr(pos),
+                                                     _ptr(vel), _ptr(ids) if ids is not None else None,
+                                                     self._stream()))
+        return pos, vel, ids
+
     def readout_glass(self, glass: torch.Tensor, glass_box: float, tile: int):
         """Read-out stage alone, Lagrangian positions from the tiled glass."""
         glass = glass.contiguous()

@@ -71,6 +71,9 @@ def parse():
     ap.add_argument("--no-autotune", action="store_true", help="keep the default schedule (no aar_autotune)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-n", type=int, default=128)
+    ap.add_argument("--split-modal", action="store_true",
+                    help="under torchrun: all ranks make one realisation together, the modal sum split over r "
+                         "(aarambam_gb300.modal_split; one reduce to rank 0, which runs 2LPT and the read-out)")
     ap.add_argument("--stages-only", action="store_true",
                     help="profiling case: the field stages (noise, modal, 2LPT) only, no particle arrays")
     ap.add_argument("--rows-harness", type=int, default=0, metavar="NROWS",
@@ -187,6 +190,8 @@ def alg_bytes(name: str, N: int, M: int, R: int, npart: int) -> float:
         "lpt_ypass_fwd_source": 2 * F, "lpt_xfwd_source": 2 * F, "lpt_xpsi2": 3 * F, "lpt_xpsi1": 3 * F,
         "lpt_ypass_inv_disp": 10 * F,
         "lpt_rows_c2r": 12 * F, "readout": 6 * 4.0 * N ** 3 + 36.0 * npart,
+        # displacement rows with the lattice read-out fused: 6 fields in, Pos / Vel out
+        "lpt_rows_readout": 6 * F + 24.0 * npart,
     }
     return table.get(name, float("nan"))
 
@@ -363,10 +368,16 @@ def gpu_arm(args):
     gen = ICGenerator(cfg, alpha, x0, k, t)
     # the plan's schedule, chosen by timing the candidates on this GPU
     tuned = [] if args.no_autotune else [l for l in gen.autotune().splitlines() if l.strip()]
-    lagr = lattice_positions(N, cfg["Box"], dev)
-    npart = lagr.shape[0]
-    pos = torch.empty_like(lagr)
-    vel = torch.empty_like(lagr)
+    # particles: the reference's default glass, a regular 64^3 lattice, tiled
+    # N/64 times (read_glass.c:129-214) -- aar_run_lattice, no glass array
+    gn = min(N, 64)
+    tile = N // gn
+    npart = N ** 3
+    pos = torch.empty((npart, 3), dtype=torch.float32, device=dev)
+    vel = torch.empty_like(pos)
+
+    def step():
+        gen.run_lattice(gn, 100.0, tile, pos, vel)
 
     def barrier():
         torch.cuda.synchronize()
@@ -374,7 +385,7 @@ def gpu_arm(args):
             dist.barrier()
 
     for _ in range(args.warmup):
-        gen.run(lagr, pos, vel)
+        step()
     barrier()
     clk = Clocks(local)
     stream = torch.cuda.current_stream()
@@ -382,7 +393,7 @@ def gpu_arm(args):
     e0.record(stream)
     launches = 0
     for _ in range(args.steps):
-        gen.run(lagr, pos, vel)
+        step()
         launches += gen.launches
     e1.record(stream)
     barrier()
@@ -390,11 +401,25 @@ def gpu_arm(args):
     elapsed = max_over_ranks(e0.elapsed_time(e1) / 1e3, dev)
     value = job_rate(world, args.steps, npart, elapsed)
 
+    # the same realisations from an N^3 array of Lagrangian positions in HBM
+    # (aar_run: the general trilinear read-out), for comparison
+    lagr = lattice_positions(N, cfg["Box"], dev)
+    gen.run(lagr, pos, vel)
+    barrier()
+    a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ka = max(1, min(args.steps, 3))
+    a0.record(stream)
+    for _ in range(ka):
+        gen.run(lagr, pos, vel)
+    a1.record(stream)
+    barrier()
+    value_array = job_rate(world, ka, npart, max_over_ranks(a0.elapsed_time(a1) / 1e3, dev))
+
     # per-kernel times of one profiled step (events on the launching stream)
     buf = __import__("ctypes").create_string_buffer(1 << 16)
     gen.L.aar_profile_enable(gen.h, 1)
     for _ in range(max(1, min(args.steps, 2))):
-        gen.run(lagr, pos, vel)
+        step()
     gen.L.aar_profile_report(gen.h, buf, len(buf))
     gen.L.aar_profile_enable(gen.h, 0)
     kernels = {}
@@ -447,7 +472,9 @@ def gpu_arm(args):
             gen.run_glass_host(glass, 100.0, tile, out=out)
         barrier()
         ts = max_over_ranks(time.perf_counter() - t1, dev) / 2
-        # same particles as the device-resident run (lattice = tiled lattice glass)
+        # same particles as the device-resident run (the same tiled lattice glass)
+        step()
+        barrier()
         same = bool(torch.equal(h_pos, pos.cpu()) and torch.equal(h_vel, vel.cpu()))
         # copy bandwidth from the device to the pinned host buffers
         c0, c1 = (torch.cuda.Event(enable_timing=True) for _ in range(2))
@@ -499,12 +526,15 @@ def gpu_arm(args):
         precision["fused_vs_plain_fp64_at_512"] = precision_vs_plain()
 
     if rank == 0:
-        out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        out = {"metric": METRIC, "value": value, "value_lagrangian_array": value_array, "unit": UNIT,
+               "n_gpus": world, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                "config": {"workload": f"{args.workload}: Nmesh={N}^3 particles, Box={cfg['Box']} Mpc/h, "
                                       f"{cfg['table']} ({M} modes, {R} active r), Fnl={cfg['Fnl']}, BBKS T(k), "
-                                      f"z=49", "nmesh": N, "n_modes": M, "l2": "working set >> L2 (no flush)",
+                                      f"z=49, particles from a {gn}^3 lattice glass tiled {tile}^3 times "
+                                      f"(aar_run_lattice)", "nmesh": N, "n_modes": M,
+                          "l2": "working set >> L2 (no flush)",
                           "parallelism": "replicas" if world > 1 else "single GPU"},
                "roofline": roofline, "path_roofline": path_roof, "cpu_baseline": cpu, "e2e": e2e,
                "plain_fp64": plain.get("plain_fp64"), "plain_fp64_regrouped": plain.get("plain_fp64_regrouped"),
@@ -512,6 +542,68 @@ def gpu_arm(args):
                "schedule": tuned}
         print(json.dumps(out))
     if world > 1:
+        dist.destroy_process_group()
+
+
+def split_arm(args):
+    """One realisation per step made by all ranks together: each rank
+    regenerates the Gaussian potential, sums its share of the radial modes
+    (balanced by product terms) and one reduce gives rank 0 the potential,
+    which then runs 2LPT and the read-out (strong scaling: the work per step
+    is fixed).  Time = max over ranks, CUDA events, barrier on both sides."""
+    import torch
+    import torch.distributed as dist
+    from aarambam_gb300 import _lib, modal_split
+    from aarambam_gb300.ic import ICGenerator
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1 or "MASTER_ADDR" in os.environ:
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    _lib.load(build_if_missing=True)
+    cfg = make_cfg(args.workload, 1234)
+    N, M = cfg["Nmesh"], cfg["N_modes"]
+    alpha, x0, k, t = load_tables(cfg["table"], M)
+    gen = ICGenerator(cfg, alpha, x0, k, t)
+    lagr = lattice_positions(N, cfg["Box"], dev) if rank == 0 else None
+    pos = torch.empty_like(lagr) if rank == 0 else None
+    vel = torch.empty_like(lagr) if rank == 0 else None
+    distributed = dist.is_available() and dist.is_initialized()
+
+    def step():
+        if distributed:
+            modal_split.split_run(gen, lagr, rank, world, pos=pos, vel=vel)
+        else:
+            gen.run(lagr, pos, vel)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if distributed:
+            dist.barrier()
+    for _ in range(args.warmup):
+        step()
+    barrier()
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    barrier()
+    el = max_over_ranks(e0.elapsed_time(e1) / 1e3, dev)
+    part = modal_split.partition(alpha, world)
+    if rank == 0:
+        print(json.dumps({"metric": METRIC, "value": args.steps * N ** 3 / el, "unit": UNIT, "n_gpus": world,
+                          "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+                          "higher_is_better": True, "scaling": "strong", "vs_baseline": None, "dtype": "f32",
+                          "data": "synthetic",
+                          "config": {"workload": f"{args.workload}: one realisation per step, modal sum split over "
+                                                 f"{world} ranks by radial mode", "nmesh": N, "n_modes": M,
+                                     "parallelism": f"modal split x{world}",
+                                     "part_of_r": part.tolist()}}))
+    if distributed:
         dist.destroy_process_group()
 
 
@@ -723,6 +815,8 @@ if __name__ == "__main__":
     a = parse()
     if a.impl == "reference":
         reference_arm(a)
+    elif a.split_modal:
+        split_arm(a)
     elif a.stages_only:
         stage_arm(a)
     elif a.rows_harness:

@@ -117,6 +117,24 @@ int aar_run(aar_plan* plan, const float* d_lagr_pos, int64_t npart, float* d_pos
 int aar_run_glass(aar_plan* plan, const float* d_glass_pos, int64_t nglass, double glass_box, int32_t tile,
                   float* d_pos, float* d_vel, int32_t* d_ids, void* stream);
 
+/* As aar_run_glass for the regular glass_n^3 lattice glass -- per-axis
+   coordinates (float)(i * glass_box / glass_n), the particle order of
+   read_glass.c:181-214, the layout of the reference's default glass
+   (defaults/dummy_glass_dmonly_64.dat, 64^3) -- tiled tile^3 times, with no
+   glass array.  When glass_n * tile == Nmesh and every tiled coordinate
+   falls exactly on a grid point by the reference's FP64 cell coordinate
+   u = Pos / Box * Nmesh (main.c:1444-1446; checked on the device once per
+   parameter set, one synchronisation), each particle reads only the grid
+   value under it, as the reference does, and the read-out is fused into the
+   displacement rows: the real displacement fields are then not kept
+   (aar_copy_field / aar_stage_readout need aar_stage_lpt).  The general
+   read-out's FP32 two-float coordinate can leave fractions of ~1e-12 at
+   such points; its results agree with the fused ones to float rounding.
+   Otherwise the general read-out runs.  Positions, velocities and IDs as
+   aar_run_glass (d_ids may be NULL). */
+int aar_run_lattice(aar_plan* plan, int32_t glass_n, double glass_box, int32_t tile, float* d_pos, float* d_vel,
+                    int32_t* d_ids, void* stream);
+
 /* aar_run with HOST buffers: copies in, runs on `stream`, copies out and
    synchronises.  The device staging buffers are owned by the plan (allocated
    on first use, grown when npart grows, freed with the plan). */
@@ -128,7 +146,9 @@ int aar_run_host(aar_plan* plan, const float* h_lagr_pos, int64_t npart, float* 
    device from it tiled tile^3 times (read_glass.c:129-214), and the
    particles are read out in chunks whose positions, velocities and (when
    h_ids is not NULL) IDs go to the host while later chunks are read out --
-   no N^3 Lagrangian array crosses to the GPU.  npart = nglass * tile^3;
+   no N^3 Lagrangian array crosses to the GPU.  A glass that is the regular
+   lattice (as aar_run_lattice describes) gets aar_run_lattice's fused
+   read-out, in chunks of tile rows.  npart = nglass * tile^3;
    h_pos / h_vel float32 [npart][3], h_ids int32 [npart].  Returns when the
    results are in the host buffers.  The plan owns the device staging
    (grown on demand, freed with the plan).  Fused form only. */

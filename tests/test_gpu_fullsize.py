@@ -219,3 +219,24 @@ def test_modal_potential_vs_plain_fp64_512(cuda):
     print(f"modal 512^3 M=12 vs plain FP64: non-Gaussian part {e_ng:.3e}, total {e_tot:.3e}")
     assert e_ng < 2e-4
     assert e_tot < 1e-6
+
+
+def test_run_lattice_1024(cuda):
+    """The 1024^3 bench workload through aar_run_lattice (64^3 lattice glass
+    tiled 16 times, read-out fused into the folded displacement rows): the
+    general glass read-out's particles to float rounding (the grid value
+    under each particle against the FP32 two-float coordinate's ~1e-12
+    neighbour weights)."""
+    from aarambam_gb300 import gadget
+    N = 1024
+    tab, M = "scalarI_m20_L1000_n1024", 20
+    cfg = make_cfg(N, 1000.0, 12, 100.0, M, tab, 1024)
+    gen = ICGenerator(cfg, *table(tab, M), *bbks())
+    glass = torch.from_numpy(gadget.lattice_glass(64, 100.0)).cuda()
+    pos_g, vel_g, _ = gen.run_glass(glass, 100.0, 16)
+    pos, vel, _ = gen.run_lattice(64, 100.0, 16)
+    same = float((pos == pos_g).all(1).float().mean())
+    print(f"lattice read-out at 1024^3: {100 * same:.4f} % of particles bit-identical to the general read-out")
+    assert same > 0.999
+    torch.testing.assert_close(pos, pos_g, rtol=1e-6, atol=1e-4)
+    torch.testing.assert_close(vel, vel_g, rtol=1e-6, atol=1e-6 * float(vel_g.abs().max()))

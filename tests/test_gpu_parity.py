@@ -346,3 +346,36 @@ def test_gaussian_spectrum_fp64_amplitude(cuda, cfg):
     nz = o != 0
     assert np.array_equal(got != 0, nz)
     assert (np.abs(got[nz] - o[nz]) / np.abs(o[nz])).max() < 2e-7
+
+
+@pytest.mark.parametrize("N,g,box", [(16, 8, 500.0), (32, 16, 500.0), (64, 16, 1000.0), (128, 64, 500.0),
+                                     (256, 64, 500.0), (512, 64, 1000.0), (64, 16, 777.7)])
+def test_run_lattice_matches_glass(cuda, N, g, box):
+    """aar_run_lattice (the regular g^3 lattice glass tiled N/g times, no
+    glass array) gives the general glass read-out's particles: with the
+    read-out fused into the displacement rows where the lattice lands on
+    grid points (the grid value under each particle, as the FP64 reference
+    reads it; the general FP32 read-out may weight a neighbour by ~1e-12
+    there, so agreement to float rounding), and bit for bit through the
+    general read-out where it does not (Box 777.7)."""
+    from aarambam_gb300 import gadget
+    cfg = make_cfg(N, box, 31, 100.0, 10, "scalarI_m10_L500_n256", max(N, 256))
+    gen = gen_for(cfg)
+    tile = N // g
+    glass = torch.from_numpy(gadget.lattice_glass(g, 100.0)).cuda()
+    pos_g, vel_g, ids_g = gen.run_glass(glass, 100.0, tile)
+    n = N ** 3
+    ids = torch.zeros(n, dtype=torch.int32, device=cuda)
+    pos, vel, _ = gen.run_lattice(g, 100.0, tile, ids=ids)
+    assert torch.equal(ids, ids_g)
+    if box == 777.7:  # not on grid points: the general read-out, bit for bit
+        assert torch.equal(pos, pos_g) and torch.equal(vel, vel_g)
+    same = float((pos == pos_g).all(1).float().mean())
+    assert same > 0.999
+    torch.testing.assert_close(pos, pos_g, rtol=1e-6, atol=1e-4)
+    torch.testing.assert_close(vel, vel_g, rtol=1e-6, atol=1e-6 * float(vel_g.abs().max()))
+    # and again through the host-glass entry point (lattice detected on the host): the same
+    # fused read-out, so bit for bit with aar_run_lattice
+    hp, hv, hi = gen.run_glass_host(gadget.lattice_glass(g, 100.0), 100.0, tile)
+    assert np.array_equal(hp, pos.cpu().numpy()) and np.array_equal(hv, vel.cpu().numpy())
+    assert np.array_equal(hi, ids_g.cpu().numpy())

@@ -108,7 +108,10 @@ def test_partition_balanced_and_complete():
 def test_split_shares_add_up_gpu(cuda, N, nparts):
     """On one GPU, the shares of all parts (each through the plan's own
     modal stage, NVRTC kernels re-specialised per part at 256^3) add up to
-    the unsplit non-Gaussian potential to FP32 rounding."""
+    the unsplit non-Gaussian potential to FP32 rounding.  Each share is read
+    as (total - Gaussian) of an FP32 spectrum, so it carries the rounding of
+    the total potential: bounded like the other parity tests (non-Gaussian
+    part 1e-4, total 1e-6)."""
     from aarambam_gb300.ic import ICGenerator
     tab, M = "scalarI_m20_L1000_n1024", 20
     cfg = make_cfg(N, 1000.0, 5, 100.0, M, tab, 1024)
@@ -125,4 +128,6 @@ def test_split_shares_add_up_gpu(cuda, N, nparts):
         tot += (g.spectrum() - gauss).to(torch.complex128)
     g.set_modal_partition(0, 1)
     err = float(torch.linalg.vector_norm(tot - ng) / torch.linalg.vector_norm(ng))
-    assert err < 1e-5
+    err_tot = float(torch.linalg.vector_norm(tot - ng) / torch.linalg.vector_norm(gauss.to(torch.complex128) + ng))
+    assert err < 1e-4
+    assert err_tot < 1e-6

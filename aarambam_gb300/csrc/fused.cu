@@ -452,7 +452,15 @@ __device__ __forceinline__ void cell_coord(const ReadArgs& a, float p, int& i, f
 // dis2 / N^3 with the periodic wrap, Vel = dis vp1 - 3/7 dis2 / N^3 vp2.
 __device__ __forceinline__ void move_particle(const ReadArgs& a, const float* p, const float* dis, const float* dis2,
                                               float* op, float* ov) {
-  move_particle(a, p, dis, dis2, op, ov);
+  for (int ax = 0; ax < 3; ++ax) {
+    const float d1 = dis[ax], d2 = dis2[ax] * a.inv_n3;
+    float d = d1 - (3.f / 7.f) * d2;
+    float x = p[ax] + d;
+    if (x < 0.f) x += a.box;
+    if (x >= a.box) x -= a.box;
+    op[ax] = x;
+    ov[ax] = d1 * a.vp1 - (3.f / 7.f) * d2 * a.vp2;
+  }
 }
 
 __device__ __forceinline__ void readout_one(const ReadArgs& a, const float* __restrict__ F, float px, float py,
@@ -494,15 +502,7 @@ __device__ __forceinline__ void readout_one(const ReadArgs& a, const float* __re
                  d2[o100 + k0] * f5 + d2[o100 + k1] * f6 + d2[o110 + k0] * f7 + d2[o110 + k1] * f8;
     }
   }
-  for (int ax = 0; ax < 3; ++ax) {
-    const float d1 = dis[ax], d2 = dis2[ax] * a.inv_n3;
-    float d = d1 - (3.f / 7.f) * d2;
-    float x = p[ax] + d;
-    if (x < 0.f) x += a.box;
-    if (x >= a.box) x -= a.box;
-    op[ax] = x;
-    ov[ax] = d1 * a.vp1 - (3.f / 7.f) * d2 * a.vp2;
-  }
+  move_particle(a, p, dis, dis2, op, ov);
 }
 
 // One particle per thread.  (Measured at 1024^3 on a lattice: four

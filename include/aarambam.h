@@ -128,7 +128,7 @@ int aar_run_glass(aar_plan* plan, const float* d_glass_pos, int64_t nglass, doub
    value under it, as the reference does, and the read-out is fused into the
    displacement rows: the real displacement fields are then not kept
    (aar_copy_field / aar_stage_readout need aar_stage_lpt).  The general
-   read-out's FP32 two-float coordinate can leave fractions of ~1e-12 at
+   read-out's FP32 two-float coordinate can leave fractions of ~1e-7 at
    such points; its results agree with the fused ones to float rounding.
    Otherwise the general read-out runs.  Positions, velocities and IDs as
    aar_run_glass (d_ids may be NULL). */

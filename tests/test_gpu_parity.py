@@ -348,34 +348,82 @@ def test_gaussian_spectrum_fp64_amplitude(cuda, cfg):
     assert (np.abs(got[nz] - o[nz]) / np.abs(o[nz])).max() < 2e-7
 
 
-@pytest.mark.parametrize("N,g,box", [(16, 8, 500.0), (32, 16, 500.0), (64, 16, 1000.0), (128, 64, 500.0),
+def lattice_expected(gen, cfg, g, glass_box, tile):
+    """Positions and velocities of the lattice particles read straight off
+    the grid (FP64 from the plan's FP32 displacement fields after
+    aar_stage_lpt): each particle (x, y, z) moves by its grid point's
+    psi1 - 3/7 psi2 / N^3 (main.c:1486-1509), particles in read_glass.c's
+    tiled order."""
+    N, box = cfg["Nmesh"], cfg["Box"]
+    gen.stage("noise")
+    gen.stage("modal")
+    gen.stage("lpt")
+    f = [gen.field(i).double() for i in range(6)]
+    s = gen.scalars
+    i = torch.arange(N, dtype=torch.float64, device=f[0].device)
+    gi, ti = torch.remainder(i, g), torch.div(i, g, rounding_mode="floor")
+    gc = (gi * (glass_box / g)).float().double()
+    bot = box / tile
+    lp = (gc / glass_box * bot + ti * bot).float().double()
+    n3 = float(np.float32(float(N) ** 3))
+    d2 = [x / n3 for x in f[3:]]
+    pos = [lp.view(-1, 1, 1) if a == 0 else lp.view(1, -1, 1) if a == 1 else lp.view(1, 1, -1) for a in range(3)]
+    P = torch.stack([torch.remainder(pos[a] + f[a] - 3.0 / 7.0 * d2[a], box) for a in range(3)], -1)
+    V = torch.stack([f[a] * s["vel_prefac"] - 3.0 / 7.0 * d2[a] * s["vel_prefac2"] for a in range(3)], -1)
+    # grid point (x, y, z) -> particle ((ti tile + tj) tile + tk) g^3 + (gi g + gj) g + gk
+    X = torch.arange(N, device=f[0].device)
+    t, q = torch.div(X, g, rounding_mode="floor"), torch.remainder(X, g)
+    tx, ty, tz = t.view(-1, 1, 1), t.view(1, -1, 1), t.view(1, 1, -1)
+    qx, qy, qz = q.view(-1, 1, 1), q.view(1, -1, 1), q.view(1, 1, -1)
+    idx = (((tx * tile + ty) * tile + tz) * g ** 3 + (qx * g + qy) * g + qz).reshape(-1)
+    Pn = torch.empty((N ** 3, 3), dtype=torch.float64, device=f[0].device)
+    Vn = torch.empty_like(Pn)
+    Pn[idx] = P.reshape(-1, 3)
+    Vn[idx] = V.reshape(-1, 3)
+    return Pn, Vn
+
+
+def close_periodic(a, b, box, atol):
+    """Positions equal to atol, modulo the box (a particle at the edge may
+    wrap on one side and not the other)."""
+    d = (a.double() - b.double()).abs()
+    return bool(torch.all(torch.minimum(d, box - d) <= atol))
+
+
+# (N, g, Box): N / Box a power of two puts every lattice point exactly on the
+# grid in the general read-out's FP32 coordinate too (bit-identical paths);
+# Box 500 / 1000 leave it fractions of ~1e-7 there; Box 777.7 puts the
+# lattice off the grid (the general read-out runs inside aar_run_lattice)
+@pytest.mark.parametrize("N,g,box", [(16, 8, 256.0), (32, 16, 512.0), (64, 16, 1000.0), (128, 64, 1024.0),
                                      (256, 64, 500.0), (512, 64, 1000.0), (64, 16, 777.7)])
 def test_run_lattice_matches_glass(cuda, N, g, box):
     """aar_run_lattice (the regular g^3 lattice glass tiled N/g times, no
-    glass array) gives the general glass read-out's particles: with the
-    read-out fused into the displacement rows where the lattice lands on
-    grid points (the grid value under each particle, as the FP64 reference
-    reads it; the general FP32 read-out may weight a neighbour by ~1e-12
-    there, so agreement to float rounding), and bit for bit through the
-    general read-out where it does not (Box 777.7)."""
+    glass array) against the general glass read-out and against the grid
+    values under the particles."""
     from aarambam_gb300 import gadget
     cfg = make_cfg(N, box, 31, 100.0, 10, "scalarI_m10_L500_n256", max(N, 256))
     gen = gen_for(cfg)
     tile = N // g
     glass = torch.from_numpy(gadget.lattice_glass(g, 100.0)).cuda()
     pos_g, vel_g, ids_g = gen.run_glass(glass, 100.0, tile)
-    n = N ** 3
-    ids = torch.zeros(n, dtype=torch.int32, device=cuda)
-    pos, vel, _ = gen.run_lattice(g, 100.0, tile, ids=ids)
+    pos = torch.full_like(pos_g, float("nan"))
+    vel = torch.full_like(vel_g, float("nan"))
+    ids = torch.zeros(N ** 3, dtype=torch.int32, device=cuda)
+    gen.run_lattice(g, 100.0, tile, pos, vel, ids)
     assert torch.equal(ids, ids_g)
-    if box == 777.7:  # not on grid points: the general read-out, bit for bit
+    vtol = 1e-6 * float(vel_g.abs().max())
+    exact = box == 777.7 or (N / box) in [2.0 ** -k for k in range(12)]
+    if exact:
         assert torch.equal(pos, pos_g) and torch.equal(vel, vel_g)
-    same = float((pos == pos_g).all(1).float().mean())
-    assert same > 0.999
-    torch.testing.assert_close(pos, pos_g, rtol=1e-6, atol=1e-4)
-    torch.testing.assert_close(vel, vel_g, rtol=1e-6, atol=1e-6 * float(vel_g.abs().max()))
-    # and again through the host-glass entry point (lattice detected on the host): the same
-    # fused read-out, so bit for bit with aar_run_lattice
+    else:
+        assert close_periodic(pos, pos_g, box, 1e-4)
+        torch.testing.assert_close(vel, vel_g, rtol=1e-6, atol=vtol)
+    if box != 777.7:  # the fused read-out: the grid value under each particle
+        P, V = lattice_expected(gen, cfg, g, 100.0, tile)
+        assert close_periodic(pos, P, box, 1e-4)
+        torch.testing.assert_close(vel.double(), V, rtol=1e-6, atol=vtol)
+    # and through the host-glass entry point (lattice detected on the host):
+    # the same read-out, bit for bit with aar_run_lattice
     hp, hv, hi = gen.run_glass_host(gadget.lattice_glass(g, 100.0), 100.0, tile)
     assert np.array_equal(hp, pos.cpu().numpy()) and np.array_equal(hv, vel.cpu().numpy())
     assert np.array_equal(hi, ids_g.cpu().numpy())

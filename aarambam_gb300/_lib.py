@@ -21,6 +21,7 @@ AAR_ERR_TRANSFER_DUP = 777
 AAR_FUSED_FP32 = 0
 AAR_PLAIN_FP64 = 1
 AAR_PLAIN_FP64_REGROUPED = 2
+AAR_SLAB_FP32 = 3
 AAR_VARIANT_BASIS = 0
 AAR_VARIANT_RESBASIS = 1
 
@@ -50,7 +51,7 @@ class Params(C.Structure):
                 ("phase_flip", C.c_int32), ("sphere_mode", C.c_int32), ("precision", C.c_int32),
                 ("mem_limit_bytes", C.c_int64), ("variant", C.c_int32), ("which_spectrum", C.c_int32),
                 ("a_res", C.c_double), ("w_res", C.c_double), ("phi_res", C.c_double),
-                ("noise_fp64", C.c_int32)]
+                ("noise_fp64", C.c_int32), ("nslab", C.c_int32)]
 
 
 class Scalars(C.Structure):

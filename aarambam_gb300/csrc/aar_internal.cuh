@@ -83,6 +83,8 @@ struct Plan {
   int modal_part = 0, modal_nparts = 1;  // split of the modal sum over r (this plan's part)
   // plain FP64 form
   void* plain = nullptr;
+  // slab form (slab.cu)
+  void* slab = nullptr;
   int last_launches = 0;      // kernels launched by the last run
   uint64_t generation = 0;    // bumped by every set_* call (captured graphs of the plan go stale)
   size_t used_bytes = 0;      // device bytes this plan holds
@@ -173,6 +175,14 @@ void plain_free(Plan* p);
 inline bool is_plain(const aar_params& q) {
   return q.precision == AAR_PLAIN_FP64 || q.precision == AAR_PLAIN_FP64_REGROUPED;
 }
+// the FP32 forms share the plan's field layout (x-blocked rows of HP complex)
+inline bool is_fp32(const aar_params& q) { return q.precision == AAR_FUSED_FP32 || q.precision == AAR_SLAB_FP32; }
+int build_term_list(Plan* p);  // the regrouped term list (fused.cu)
+RhoArgs rho_args(const Plan* p);
+int slab_check(const aar_params& q, std::string& why);
+int slab_setup(Plan* p);
+int slab_run(Plan* p, cudaStream_t st);
+void slab_free(Plan* p);
 int fused_c2r(Plan* p, const float2* in, float* out, cudaStream_t st);
 int fused_r2c(Plan* p, const float* in, float2* out, cudaStream_t st);
 int fused_configure_xform(Plan* p);

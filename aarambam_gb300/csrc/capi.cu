@@ -197,7 +197,7 @@ static int set_transfer(Plan* p, const double* k, const double* t, int n) {
   // per-n^2 tables for the FP32 form: noise amplitude and T / (D Beta),
   // rewritten with synchronous copies (ordered only against the legacy
   // stream): runs in flight on other streams finish first
-  if (p->prm.precision == AAR_FUSED_FP32) {
+  if (is_fp32(p->prm)) {
     AAR_CUDA_TRY(p, cudaDeviceSynchronize());
     int N = p->N;
     int64_t nsq = 3LL * (N / 2) * (N / 2) + 1;
@@ -282,6 +282,7 @@ static void plan_release(Plan* p) {
   p->d_gout = nullptr;
   p->glass_cap = p->gout_cap = 0;
   plain_free(p);
+  slab_free(p);
 }
 
 static bool pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
@@ -368,11 +369,15 @@ static int create(Plan* p) {
   const aar_params& q = p->prm;
   int N = q.nmesh;
   if (q.nsample > q.nmax) return set_err(p, "Nmax must be >= Nsample (main.c:200)"), AAR_ERR_NMAX;
-  if (q.precision != AAR_FUSED_FP32 && !is_plain(q)) return set_err(p, "unknown precision"), AAR_ERR_ARG;
+  if (!is_fp32(q) && !is_plain(q)) return set_err(p, "unknown precision"), AAR_ERR_ARG;
   if (q.precision == AAR_FUSED_FP32 && !(pow2(N) && N >= 16 && N <= 1024))
     return set_err(p, "fused FP32 form supports Nmesh = 16..1024, powers of two"), AAR_ERR_ARG;
   if (is_plain(q) && !(N >= 4 && N % 2 == 0 && N <= 2048))
     return set_err(p, "plain FP64 form supports even Nmesh up to 2048"), AAR_ERR_ARG;
+  if (q.precision == AAR_SLAB_FP32) {
+    std::string why;
+    if (slab_check(q, why)) return set_err(p, why), AAR_ERR_ARG;
+  }
   if (!(q.box > 0) || q.nsample <= 0) return set_err(p, "Box and Nsample must be positive"), AAR_ERR_ARG;
   if (q.seed < 0) return set_err(p, "Seed must be >= 0"), AAR_ERR_ARG;
   if (q.variant == AAR_VARIANT_BASIS) {
@@ -414,7 +419,7 @@ static int create(Plan* p) {
     if ((rc = plan_alloc(p, &p->d_rlxpow, sizeof(U576) * 32))) return rc;
     AAR_CUDA_TRY(p, cudaMemcpy(p->d_rlxpow, pw.data(), sizeof(U576) * 32, cudaMemcpyHostToDevice));
   }
-  if (q.precision == AAR_FUSED_FP32) {
+  if (is_fp32(q)) {
     std::vector<float2> twN(N), twH(N / 2);
     for (int m = 0; m < N; ++m) {
       long double ang = -2.0L * 3.141592653589793238462643383279502884L * m / N;
@@ -470,6 +475,7 @@ static int ready_tables(Plan* p) {
 // aar_plan_prepare -- not when the plan is made or its tables are set, so a
 // plan holds no field memory until it computes.
 static int ensure_fields(Plan* p) {
+  if (p->prm.precision == AAR_SLAB_FP32) return slab_setup(p);
   if (p->prm.precision != AAR_FUSED_FP32) return AAR_OK;
   if (!p->d_phik) {
     int rc = plan_alloc(p, (void**)&p->d_phik, sizeof(float2) * (size_t)p->N * p->N * p->HP);
@@ -488,6 +494,18 @@ static int run_noise(Plan* p, cudaStream_t st) {
   int rc = launch_seedtable(p, (uint32_t)p->prm.seed, p->d_seed, st);
   if (rc) return rc;
   return launch_noise_fp32(p, p->d_seed, p->d_phik, st);
+}
+
+// The FP32 forms' field stages: noise, the modal sum and 2LPT, up to the six
+// displacement fields (rows = false: the fused form stops before its
+// displacement rows, which the lattice read-out then fuses).  The slab form
+// always leaves the real fields.
+static int field_stages(Plan* p, cudaStream_t st, bool rows = true) {
+  int rc = run_noise(p, st);
+  if (rc) return rc;
+  if (p->prm.precision == AAR_SLAB_FP32) return slab_run(p, st);
+  if ((rc = fused_modal(p, st))) return rc;
+  return fused_lpt(p, st, rows);
 }
 
 }  // namespace aar
@@ -546,6 +564,10 @@ int aar_set_tables(aar_plan* h, const double* alpha, const double* x0, int32_t M
   p->M = M;
   plain_free(p);  // plain-form tables are rebuilt on the next run
   int rc;
+  if (p->prm.precision == AAR_SLAB_FP32) {
+    if (!p->d_terms && (rc = plan_alloc(p, &p->d_terms, terms_bytes()))) return rc;
+    if ((rc = build_term_list(p))) return rc;
+  }
   if (p->prm.precision == AAR_FUSED_FP32) {
     if ((rc = mode_tables(p))) return rc;
     if (!p->d_terms && (rc = plan_alloc(p, &p->d_terms, terms_bytes()))) return rc;
@@ -654,9 +676,7 @@ int aar_run(aar_plan* h, const float* d_lagr, int64_t npart, float* d_pos, float
   p->last_launches = 0;
   cudaStream_t st = S(stream);
   if (is_plain(p->prm)) return plain_run(p, d_lagr, npart, d_pos, d_vel, st);
-  if ((rc = run_noise(p, st))) return rc;
-  if ((rc = fused_modal(p, st))) return rc;
-  if ((rc = fused_lpt(p, st))) return rc;
+  if ((rc = field_stages(p, st))) return rc;
   return fused_readout(p, d_lagr, npart, d_pos, d_vel, st);
 }
 
@@ -666,12 +686,10 @@ int aar_run_glass(aar_plan* h, const float* d_glass, int64_t nglass, double glas
   Plan* p = &h->p;
   int rc = ready(p);
   if (rc) return rc;
-  if (p->prm.precision != AAR_FUSED_FP32) return set_err(p, "aar_run_glass is for the fused form"), AAR_ERR_ARG;
+  if (!is_fp32(p->prm)) return set_err(p, "aar_run_glass is for the FP32 forms"), AAR_ERR_ARG;
   p->last_launches = 0;
   cudaStream_t st = S(stream);
-  if ((rc = run_noise(p, st))) return rc;
-  if ((rc = fused_modal(p, st))) return rc;
-  if ((rc = fused_lpt(p, st))) return rc;
+  if ((rc = field_stages(p, st))) return rc;
   if ((rc = glass_prepare(p, d_glass, nglass, glass_box, tile, st))) return rc;
   return fused_readout_glass(p, nglass, tile, d_pos, d_vel, d_ids, st);
 }
@@ -685,14 +703,13 @@ int aar_run_lattice(aar_plan* h, int32_t glass_n, double glass_box, int32_t tile
   Plan* p = &h->p;
   int rc = ready(p);
   if (rc) return rc;
-  if (p->prm.precision != AAR_FUSED_FP32) return set_err(p, "aar_run_lattice is for the fused form"), AAR_ERR_ARG;
+  if (!is_fp32(p->prm)) return set_err(p, "aar_run_lattice is for the FP32 forms"), AAR_ERR_ARG;
   cudaStream_t st = S(stream);
   bool fused = false;
-  if ((rc = lattice_prepare(p, glass_n, glass_box, tile, st, fused))) return rc;
+  // the slab form keeps real displacement fields: the general read-out
+  if (p->prm.precision == AAR_FUSED_FP32 && (rc = lattice_prepare(p, glass_n, glass_box, tile, st, fused))) return rc;
   p->last_launches = 0;
-  if ((rc = run_noise(p, st))) return rc;
-  if ((rc = fused_modal(p, st))) return rc;
-  if ((rc = fused_lpt(p, st, !fused))) return rc;
+  if ((rc = field_stages(p, st, !fused))) return rc;
   if (fused) return fused_rows_lattice(p, glass_n, tile, d_pos, d_vel, d_ids, 0, (int64_t)p->N * p->N, st);
   // general read-out from the lattice glass made on the device
   const int64_t nglass = (int64_t)glass_n * glass_n * glass_n;
@@ -766,9 +783,7 @@ int aar_run_host(aar_plan* h, const float* h_lagr, int64_t npart, float* h_pos, 
       AAR_CUDA_TRY(p, cudaMemcpyAsync(d_in, h_lagr, bytes, cudaMemcpyHostToDevice, p->copy_stream));
     AAR_CUDA_TRY(p, cudaEventRecord(p->copy_done, p->copy_stream));
     p->last_launches = 0;
-    if ((rc = run_noise(p, st))) return rc;
-    if ((rc = fused_modal(p, st))) return rc;
-    if ((rc = fused_lpt(p, st))) return rc;
+    if ((rc = field_stages(p, st))) return rc;
     AAR_CUDA_TRY(p, cudaStreamWaitEvent(st, p->copy_done, 0));
     // read-out in chunks; each chunk's Pos/Vel go to the host on one of two
     // side streams while the next chunks are read out
@@ -832,7 +847,7 @@ static int run_glass_host(Plan* p, const float* h_glass, int64_t nglass, double 
                           float* h_vel, int32_t* h_ids, cudaStream_t st, bool sync) {
   int rc = ready(p);
   if (rc) return rc;
-  if (p->prm.precision != AAR_FUSED_FP32) return set_err(p, "aar_run_glass_host is for the fused form"), AAR_ERR_ARG;
+  if (!is_fp32(p->prm)) return set_err(p, "aar_run_glass_host is for the FP32 forms"), AAR_ERR_ARG;
   const int64_t t3 = (int64_t)tile * tile * tile;
   const int64_t npart = nglass * t3;
   if (npart > 0 && (!h_glass || !h_pos || !h_vel)) return set_err(p, "null host buffer"), AAR_ERR_ARG;
@@ -884,14 +899,12 @@ static int run_glass_host(Plan* p, const float* h_glass, int64_t nglass, double 
   // row block, and so are their particles)
   int g = 0;
   bool lat = false;
-  if (host_lattice(h_glass, nglass, glass_box, g) && g % kXB == 0 &&
+  if (p->prm.precision == AAR_FUSED_FP32 && host_lattice(h_glass, nglass, glass_box, g) && g % kXB == 0 &&
       (rc = lattice_prepare(p, g, glass_box, tile, st, lat)))
     return rc;
   if (nglass > 0 && !lat)
     AAR_CUDA_TRY(p, cudaMemcpyAsync(p->d_glass, h_glass, sizeof(float) * 3 * (size_t)nglass, cudaMemcpyHostToDevice, st));
-  if ((rc = run_noise(p, st))) return rc;
-  if ((rc = fused_modal(p, st))) return rc;
-  if ((rc = fused_lpt(p, st, !lat))) return rc;
+  if ((rc = field_stages(p, st, !lat))) return rc;
   if (!lat && (rc = glass_prepare(p, p->d_glass, nglass, glass_box, tile, st))) return rc;
   const int nchunk = lat ? std::min(tile, (int)Plan::kGlassChunks)
                          : (npart >= (int64_t)Plan::kGlassChunks * 65536 ? Plan::kGlassChunks : 1);
@@ -938,7 +951,7 @@ int aar_copy_spectrum(aar_plan* h, void* d_out, void* stream) {
   if (!h || !d_out) return AAR_ERR_ARG;
   Plan* p = &h->p;
   if (is_plain(p->prm)) return plain_copy_spectrum(p, d_out, S(stream));
-  if (p->prm.precision != AAR_FUSED_FP32 || !p->d_phik) return set_err(p, "no FP32 spectrum in this plan"), AAR_ERR_STATE;
+  if (!is_fp32(p->prm) || !p->d_phik) return set_err(p, "no FP32 spectrum in this plan"), AAR_ERR_STATE;
   const int H = p->N / 2 + 1;
   return copy_rows(p, d_out, H, 1, p->d_phik, p->HP, kXB, H, sizeof(float2), S(stream));
 }
@@ -1022,7 +1035,7 @@ int aar_copy_field(aar_plan* h, int32_t which, void* d_out, void* stream) {
   if (!h || !d_out || which < 0 || which > 5) return AAR_ERR_ARG;
   Plan* p = &h->p;
   if (is_plain(p->prm)) return plain_copy_field(p, which, (double*)d_out, S(stream));
-  if (p->prm.precision != AAR_FUSED_FP32 || !p->d_work || which >= p->nwork || !p->disp_real)
+  if (!is_fp32(p->prm) || !p->d_work || which >= p->nwork || !p->disp_real)
     return set_err(p, "no FP32 displacement fields in this plan: run the field stages first"), AAR_ERR_STATE;
   int N = p->N;
   const float* src = (const float*)(p->d_work + (size_t)which * N * N * p->HP);

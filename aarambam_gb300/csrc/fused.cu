@@ -687,7 +687,7 @@ static int run_pass(Plan* p, const Op& op, int64_t nitems, cudaStream_t st, cons
   return AAR_OK;
 }
 
-static RhoArgs rho_args(const Plan* p) {
+RhoArgs rho_args(const Plan* p) {
   RhoArgs r{};
   const double ns = p->prm.primordial_index, box = p->prm.box;
   const double kF = 2 * kPi / box, kmin = kF, kmax = kF * p->prm.nmax;
@@ -959,6 +959,11 @@ static int build_terms(Plan* p) {
   p->nterms = tl.nterms;
   p->nr_active = nr;
   return AAR_OK;
+}
+
+int build_term_list(Plan* p) {
+  if (p->M > kMaxModes) return set_err(p, "N_modes above 32 is not supported"), AAR_ERR_ARG;
+  return build_terms(p);
 }
 
 int fused_prepare(Plan* p) {

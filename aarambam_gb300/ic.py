@@ -19,10 +19,10 @@ from ._lib import AarError, check
 
 
 def params_from_config(cfg: dict, precision: int = _lib.AAR_FUSED_FP32, mem_limit_bytes: int = 0,
-                       noise_fp64: bool = False) -> _lib.Params:
+                       noise_fp64: bool = False, nslab: int = 0) -> _lib.Params:
     """C-ABI parameters of a parameter-file dict; a dict with the A_res /
     w_res / phi_res tags is a 2LPTResBasis set.  noise_fp64: the fused form's
-    RNG-to-amplitude step in FP64."""
+    RNG-to-amplitude step in FP64.  nslab: x-slabs of the slab form."""
     res = "A_res" in cfg
     return _lib.Params(
         nmesh=cfg["Nmesh"], nsample=cfg["Nsample"], nmax=cfg["Nmax"], seed=cfg["Seed"], box=cfg["Box"],
@@ -35,7 +35,7 @@ def params_from_config(cfg: dict, precision: int = _lib.AAR_FUSED_FP32, mem_limi
         precision=precision, mem_limit_bytes=mem_limit_bytes,
         variant=_lib.AAR_VARIANT_RESBASIS if res else _lib.AAR_VARIANT_BASIS,
         which_spectrum=cfg.get("WhichSpectrum", 0), a_res=cfg.get("A_res", 0.0), w_res=cfg.get("w_res", 0.0),
-        phi_res=cfg.get("phi_res", 0.0), noise_fp64=int(bool(noise_fp64)))
+        phi_res=cfg.get("phi_res", 0.0), noise_fp64=int(bool(noise_fp64)), nslab=int(nslab))
 
 
 def _ptr(t: torch.Tensor) -> int:
@@ -52,18 +52,22 @@ class ICGenerator:
     """One plan: grid, cosmology, coefficient tables and transfer function."""
 
     def __init__(self, cfg: dict, alpha: np.ndarray, x0: np.ndarray, k: np.ndarray, T: np.ndarray,
-                 precision: str = "fp32", device=None, mem_limit_bytes: int = 0, noise_fp64: bool = False):
+                 precision: str = "fp32", device=None, mem_limit_bytes: int = 0, noise_fp64: bool = False,
+                 nslab: int = 8):
         self.L = _lib.load()
         self.cfg = dict(cfg)
         self.N = int(cfg["Nmesh"])
         self.device = torch.device(device if device is not None else "cuda", torch.cuda.current_device()
                                    if device is None else torch.device(device).index or 0)
+        # "slab_fp32": the FP32 arithmetic streamed over nslab x-slabs
+        # (AAR_SLAB_FP32), for grids whose fused fields do not fit the GPU
         forms = {"fp32": _lib.AAR_FUSED_FP32, "fp64": _lib.AAR_PLAIN_FP64,
-                 "fp64_regrouped": _lib.AAR_PLAIN_FP64_REGROUPED}
+                 "fp64_regrouped": _lib.AAR_PLAIN_FP64_REGROUPED, "slab_fp32": _lib.AAR_SLAB_FP32}
         if precision not in forms:
             raise ValueError(f"precision must be one of {sorted(forms)}")
         self.precision = forms[precision]
-        prm = params_from_config(cfg, self.precision, mem_limit_bytes, noise_fp64)
+        prm = params_from_config(cfg, self.precision, mem_limit_bytes, noise_fp64,
+                                 nslab if self.precision == _lib.AAR_SLAB_FP32 else 0)
         h = C.c_void_p()
         with torch.cuda.device(self.device):
             rc = self.L.aar_plan_create(C.byref(prm), C.byref(h))
@@ -83,7 +87,7 @@ class ICGenerator:
     @property
     def plain(self) -> bool:
         """True for the plain FP64 cuFFT forms."""
-        return self.precision != _lib.AAR_FUSED_FP32
+        return self.precision in (_lib.AAR_PLAIN_FP64, _lib.AAR_PLAIN_FP64_REGROUPED)
 
     def prepare(self) -> None:
         """Allocate what a run needs now (aar_plan_prepare): the plain forms'

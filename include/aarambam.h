@@ -43,6 +43,12 @@ extern "C" {
                              loop structure (M + 2P + 41 transforms) */
 #define AAR_PLAIN_FP64_REGROUPED 2 /* as AAR_PLAIN_FP64 with the modal sum regrouped by linearity
                                       (M c2r + R r2c; <= 2M + 13 transforms in all) */
+#define AAR_SLAB_FP32 3  /* the fused form's FP32 arithmetic streamed over nslab strided real-space
+                            x-slabs, for grids whose fused fields do not fit one GPU (1536^3): the
+                            filtered fields and products exist per slab, the transform stages are
+                            recomputed per slab ((Nmesh/nslab, Nmesh, Nmesh) cuFFT FP32 transforms
+                            of spectra folded along x), the modal sum is accumulated compensated
+                            across slabs; even Nmesh = 8..2048, a multiple of 4 */
 
 /* Which executable's power spectrum the plan follows. */
 #define AAR_VARIANT_BASIS 0    /* 2LPTBasis: P(k) = Norm k^ns T^2 (LPT/Basis/power.c:240-265) */
@@ -57,7 +63,7 @@ typedef struct aar_params {
   double unit_length_in_cm, unit_mass_in_g, unit_velocity_in_cm_per_s;
   double input_spectrum_unit_length_in_cm;
   int32_t fixed_amplitude, phase_flip, sphere_mode;
-  int32_t precision;        /* AAR_FUSED_FP32 or AAR_PLAIN_FP64 */
+  int32_t precision;        /* AAR_FUSED_FP32, AAR_PLAIN_FP64, AAR_PLAIN_FP64_REGROUPED or AAR_SLAB_FP32 */
   int64_t mem_limit_bytes;  /* refuse plan allocations beyond this (0 = no cap) */
   int32_t variant;          /* AAR_VARIANT_BASIS or AAR_VARIANT_RESBASIS */
   int32_t which_spectrum;   /* WhichSpectrum: 0 for Basis; 0, 1 or 2 for ResBasis */
@@ -65,6 +71,9 @@ typedef struct aar_params {
   int32_t noise_fp64;       /* fused form: 1 = RNG-to-amplitude step (phase, -ln u, sqrt, amplitude)
                                in FP64 with the reference's formula, rounded to float at the end;
                                0 (default) = FP32 from the exact 48-bit uniforms */
+  int32_t nslab;            /* AAR_SLAB_FP32: number of x-slabs S (Nmesh % S == 0, Nmesh / S >= 2);
+                               device memory ~ (8.8 + 39/S) fields of Nmesh^2 (Nmesh/2+1) complex
+                               floats at 20 modes; ignored by the other forms */
 } aar_params;
 
 /* Host scalars of the set-up: power.c:391-448 (Norm = sigma8 normalisation,

@@ -152,6 +152,23 @@ def test_potential_dump_layout(tmp_path):
     assert rec["coord"][5] == (0 * 4 + 1) * 2 * 3 + 1  # (i*N + j) * 2(N/2+1) + k
 
 
+def test_params_struct_mirrors_header():
+    """The ctypes aar_params has the header's fields, in order, with the same
+    C types (the plan reads the caller's struct by layout)."""
+    hdr = open(os.path.join(ROOT, "include", "aarambam.h")).read()
+    body = re.search(r"typedef struct aar_params \{(.*?)\} aar_params;", hdr, re.S).group(1)
+    body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+    fields = []
+    for decl in body.split(";"):
+        decl = decl.strip()
+        if not decl:
+            continue
+        ctype, names = decl.split(None, 1)
+        fields += [(n.strip(), ctype) for n in names.split(",")]
+    ct = {"int32_t": ctypes.c_int32, "int64_t": ctypes.c_int64, "double": ctypes.c_double}
+    assert [(n, ct[t]) for n, t in fields] == list(_lib.Params._fields_)
+
+
 def test_c_abi_library_exports_every_declared_symbol():
     build()
     hdr = open(os.path.join(ROOT, "include", "aarambam.h")).read()

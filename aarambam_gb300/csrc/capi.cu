@@ -697,6 +697,7 @@ int aar_run_glass(aar_plan* h, const float* d_glass, int64_t nglass, double glas
 static int run_glass_host(Plan* p, const float* h_glass, int64_t nglass, double glass_box, int tile, float* h_pos,
                           float* h_vel, int32_t* h_ids, cudaStream_t st, bool sync);
 
+
 int aar_run_lattice(aar_plan* h, int32_t glass_n, double glass_box, int32_t tile, float* d_pos, float* d_vel,
                     int32_t* d_ids, void* stream) {
   if (!h || glass_n < 1 || tile < 1 || !(glass_box > 0) || !d_pos || !d_vel) return AAR_ERR_ARG;

@@ -535,24 +535,51 @@ __global__ void k_glass_scale(const float* __restrict__ glass, int64_t nglass, d
 }
 
 // Particles n0 <= n < n1 (indices of the whole tiled set, particle order of
-// read_glass.c:181-214: tile index outer, glass index inner).
-__global__ void k_readout_glass(ReadArgs a, const float* __restrict__ F, const double* __restrict__ gs,
-                                int64_t nglass, int tile, float* pos, float* vel, int* ids, int64_t n0, int64_t n1) {
-  int64_t n = n0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= n1) return;
-  int64_t gi = n % nglass, t = n / nglass;
-  int ti = (int)(t / ((int64_t)tile * tile)), tj = (int)((t / tile) % tile), tk = (int)(t % tile);
-  int tt[3] = {ti, tj, tk};
-  const double* toff = gs + 3 * nglass;
-  float lp[3];
-  for (int d = 0; d < 3; ++d) lp[d] = (float)__dadd_rn(gs[3 * gi + d], toff[tt[d]]);
-  float op[3], ov[3];
-  readout_one(a, F, lp[0], lp[1], lp[2], op, ov);
-  for (int d = 0; d < 3; ++d) {
-    pos[3 * n + d] = op[d];
-    vel[3 * n + d] = ov[d];
+// read_glass.c:181-214: tile index outer, glass index inner).  A block's
+// positions and velocities go through shared memory and out as 16-byte
+// stores of whole lines: the outputs may be page-locked host memory written
+// over the host link (4-byte stores 12 bytes apart: 37 GB/s at 1536^3; whole
+// lines 41-47 GB/s, the rate the copy engines reach on the same link).
+constexpr int kReadoutThreads = 256;
+__global__ void __launch_bounds__(kReadoutThreads) k_readout_glass(ReadArgs a, const float* __restrict__ F,
+                                                                   const double* __restrict__ gs, int64_t nglass,
+                                                                   int tile, float* pos, float* vel, int* ids,
+                                                                   int64_t n0, int64_t n1) {
+  __shared__ float4 sp4[3 * kReadoutThreads / 4], sv4[3 * kReadoutThreads / 4];
+  float* sp = (float*)sp4;
+  float* sv = (float*)sv4;
+  const int64_t base = n0 + (int64_t)blockIdx.x * kReadoutThreads;
+  const int64_t n = base + threadIdx.x;
+  if (n < n1) {
+    int64_t gi = n % nglass, t = n / nglass;
+    int ti = (int)(t / ((int64_t)tile * tile)), tj = (int)((t / tile) % tile), tk = (int)(t % tile);
+    int tt[3] = {ti, tj, tk};
+    const double* toff = gs + 3 * nglass;
+    float lp[3];
+    for (int d = 0; d < 3; ++d) lp[d] = (float)__dadd_rn(gs[3 * gi + d], toff[tt[d]]);
+    float op[3], ov[3];
+    readout_one(a, F, lp[0], lp[1], lp[2], op, ov);
+    for (int d = 0; d < 3; ++d) {
+      sp[3 * threadIdx.x + d] = op[d];
+      sv[3 * threadIdx.x + d] = ov[d];
+    }
+    if (ids) ids[n] = (int)(n + 1);
   }
-  if (ids) ids[n] = (int)(n + 1);
+  __syncthreads();
+  const int cnt = (int)min((int64_t)kReadoutThreads, n1 - base);
+  float* po = pos + 3 * base;
+  float* vo = vel + 3 * base;
+  if (cnt == kReadoutThreads && ((reinterpret_cast<uintptr_t>(po) | reinterpret_cast<uintptr_t>(vo)) & 15) == 0) {
+    for (int i = threadIdx.x; i < 3 * kReadoutThreads / 4; i += kReadoutThreads) {
+      reinterpret_cast<float4*>(po)[i] = sp4[i];
+      reinterpret_cast<float4*>(vo)[i] = sv4[i];
+    }
+  } else {
+    for (int i = threadIdx.x; i < 3 * cnt; i += kReadoutThreads) {
+      po[i] = sp[i];
+      vo[i] = sv[i];
+    }
+  }
 }
 
 // ----------------------------------------------------------- lattice read-out
@@ -1148,7 +1175,7 @@ int fused_readout_glass(Plan* p, int64_t nglass, int tile, float* d_pos, float* 
   const int64_t np = nglass * tile * tile * tile;
   if (n1 < 0 || n1 > np) n1 = np;
   if (n1 <= n0) return AAR_OK;
-  const int bs = 256;
+  const int bs = kReadoutThreads;
   const int64_t cnt = n1 - n0;
   { ProfScope ps_(p, "readout_glass", st);
   k_readout_glass<<<(unsigned)((cnt + bs - 1) / bs), bs, 0, st>>>(read_args(p), (const float*)p->d_work, p->d_gscale,

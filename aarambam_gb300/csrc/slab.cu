@@ -54,7 +54,7 @@ struct SlabState {
   cufftHandle c2r = 0, r2c = 0;
   bool have_c2r = false, have_r2c = false;
   void* fft_work = nullptr;
-  size_t fft_bytes = 0;
+  size_t fft_need = 0, fft_alloc = 0;  // work area bytes the plans need / allocated
 };
 
 // Geometry of one slab pass.
@@ -72,11 +72,6 @@ struct SlabTerms {
   float c[kMaxTerms];
 };
 
-struct SlotList {
-  int nr;
-  int r[kMaxModes];
-};
-
 __device__ __forceinline__ void slab_cell(int64_t t, const SlabGeo& a, int& k1, int& ky, int& kz) {
   kz = (int)(t % a.H);
   const int64_t r = t / a.H;
@@ -91,6 +86,38 @@ __device__ __forceinline__ float2 slab_tw(const float2* __restrict__ twN, int kx
 
 __device__ __forceinline__ float2 mul_conj(float2 x, float2 w) {  // x conj(w)
   return make_float2(x.x * w.x + x.y * w.y, x.y * w.x - x.x * w.y);
+}
+
+// Hermitian projection of the kz = 0 and kz = N/2 planes of nf slab fields
+// ((L, N) grids): X(k1, ky) <- (X(k1, ky) + conj X(-k1, -ky)) / 2.  FFTW's
+// c2r -- the reference's, and the fused form's rows, which drop Im X_0 and
+// Im X_{N/2} of a row after its x and y passes -- ignores the anti-Hermitian
+// part of these planes, which factors odd in kz on the Nyquist plane (psi_z,
+// d_xz, d_yz) create; cuFFT's C2R leaves the result for such input undefined
+// (it differed with the transform size).  The projection commutes with the
+// fold: conj of the twiddle at -kx is the twiddle at kx.
+__global__ void __launch_bounds__(256) k_slab_herm(float2* F, int nf, int64_t sf, int L, int N, int H) {
+  const int64_t plane = (int64_t)L * N;
+  const int64_t total = (int64_t)nf * 2 * plane;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    const int f = (int)(i / (2 * plane));
+    const int64_t rem = i - (int64_t)f * 2 * plane;
+    const int kz = rem < plane ? 0 : N / 2;
+    const int64_t ij = rem < plane ? rem : rem - plane;
+    const int k1 = (int)(ij / N), ky = (int)(ij - (int64_t)k1 * N);
+    const int64_t me = ij, pa = (int64_t)((L - k1) % L) * N + (N - ky) % N;
+    if (me > pa) continue;
+    float2* a = F + (int64_t)f * sf + me * H + kz;
+    if (me == pa) {
+      a->y = 0.f;
+      continue;
+    }
+    float2* b = F + (int64_t)f * sf + pa * H + kz;
+    const float2 u = *a, v = *b;
+    const float2 r = make_float2(0.5f * (u.x + v.x), 0.5f * (u.y - v.y));
+    *a = r;
+    *b = make_float2(r.x, -r.y);
+  }
 }
 
 // Field filters q_p(k), p < M, at one cell (n2 = |k|^2 in grid units, > 0):
@@ -162,76 +189,112 @@ __global__ void __launch_bounds__(256) k_slab_fold_modal(SlabGeo a, RhoArgs ra, 
 }
 
 // g_r = sum_t c_t f_p f_q on the slab's real points (row length 2H, the
-// first N values of a row): the M values of a point go to the thread's own
-// column of shared memory, the terms read them by index.
-__global__ void __launch_bounds__(256) k_slab_products(SlabTerms tm, const float* __restrict__ f, float* __restrict__ g,
-                                                       int64_t fsr, int N, int H, int64_t rows) {
-  __shared__ float fv[kMaxModes][256];
-  const int64_t total = rows * N;
+// first N values of a row), two neighbouring points per thread (N is even):
+// the M pairs of a thread go to its own column of shared memory, the terms
+// read them by index, one 8-byte load per factor.
+constexpr int kProdThreads = 128;
+__global__ void __launch_bounds__(kProdThreads) k_slab_products(SlabTerms tm, const float* __restrict__ f,
+                                                                float* __restrict__ g, int64_t fsr, int N, int H,
+                                                                int64_t rows) {
+  __shared__ float2 fv[kMaxModes][kProdThreads];
+  const int half = N / 2;
+  const int64_t total = rows * half;
   const int tid = threadIdx.x;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + tid; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t row = i / N;
-    const int64_t o = row * 2 * H + (i - row * N);
-    for (int p = 0; p < tm.M; ++p) fv[p][tid] = f[(int64_t)p * fsr + o];
+    const int64_t row = i / half;
+    const int64_t o = row * 2 * H + 2 * (i - row * half);
+    for (int p = 0; p < tm.M; ++p) fv[p][tid] = *reinterpret_cast<const float2*>(f + (int64_t)p * fsr + o);
     for (int sl = 0; sl < tm.nr; ++sl) {
-      float acc = 0.f;
-      for (int k = tm.begin[sl]; k < tm.begin[sl + 1]; ++k) acc += tm.c[k] * fv[tm.p[k]][tid] * fv[tm.q[k]][tid];
-      g[(int64_t)sl * fsr + o] = acc;
+      float2 acc = make_float2(0.f, 0.f);
+      for (int k = tm.begin[sl]; k < tm.begin[sl + 1]; ++k) {
+        const float c = tm.c[k];
+        const float2 a = fv[tm.p[k]][tid], b = fv[tm.q[k]][tid];
+        acc.x += c * a.x * b.x;
+        acc.y += c * a.y * b.y;
+      }
+      *reinterpret_cast<float2*>(g + (int64_t)sl * fsr + o) = acc;
     }
   }
 }
 
-// acc(k) += sum_r rho_r(k) e^{-2 pi i kx s / N} G_{r,s}(kx mod L, ky, kz),
-// Neumaier-compensated across slots and slabs in (acc_s, acc_c); rho_r per
-// cell with the expressions of k_modal_acc.  Cut cells and k = 0 are not
+// acc(k) += e^{-2 pi i kx s / N} sum_r rho_r(k) G_{r,s}(kx mod L, ky, kz):
+// the slot sum Neumaier-compensated in the slab's frame, then rotated by the
+// twiddle once and added to the running compensated sum (acc_s, acc_c) of
+// the slabs.  rho_r per cell with k_modal_acc's expressions, its logarithm
+// and exponentials in the base-2 hardware forms of q_mode_cells (every slab
+// re-evaluates them; the bracket k^s / kmin^s - 1 of kbar is 0 or at least
+// 0.42 for integer n2, no cancellation to guard).  The modes are walked in
+// one unrolled pass r = 0 .. MAXM-1 with one Legendre recurrence and a
+// bit mask of the active r: straight-line code (a walk over the slot list
+// with a recurrence loop per slot stalled on instruction fetch, 900
+// instructions per cell and slab at 11 slots).  Cut cells and k = 0 are not
 // touched (the combine skips them).
-template <int MAXR>
-__global__ void __launch_bounds__(256) k_slab_acc_modal(SlabGeo a, RhoArgs ra, SlotList sl,
+struct SlotMap {
+  uint32_t active;        // bit r: r has a product field
+  int rmax;               // highest active r
+  int slot[kMaxModes];    // its slab field
+};
+
+template <int MAXM>
+__global__ void __launch_bounds__(256) k_slab_acc_modal(SlabGeo a, RhoArgs ra, SlotMap sm,
                                                         const float2* __restrict__ G, const float2* __restrict__ twN,
                                                         float2* acc_s, float2* acc_c, int first) {
+  const int dm = (int)(((int64_t)a.L * a.s) % a.N);  // twiddle index step from kx to kx + L
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < a.sf; t += (int64_t)gridDim.x * blockDim.x) {
     int k1, ky, kz;
     slab_cell(t, a, k1, ky, kz);
-    float2 v[MAXR];
+    float2 v[MAXM];
 #pragma unroll
-    for (int j = 0; j < MAXR; ++j)
-      if (j < sl.nr) v[j] = __ldg(G + (int64_t)j * a.sf + t);
+    for (int r = 0; r < MAXM; ++r)
+      v[r] = (sm.active >> r) & 1u ? __ldg(G + (int64_t)sm.slot[r] * a.sf + t) : make_float2(0.f, 0.f);
     const int ys = sidx(ky, a.N);
-    for (int k2 = 0; k2 < a.S; ++k2) {
+    int m = (int)(((int64_t)k1 * a.s) % a.N);
+    for (int k2 = 0; k2 < a.S; ++k2, m = (m + dm >= a.N) ? m + dm - a.N : m + dm) {
       const int kx = k1 + a.L * k2, xs = sidx(kx, a.N);
       const int n2 = xs * xs + ys * ys + kz * kz;
       if (n2 == 0 || !keep_cell(a.g, xs, ys, kz)) continue;
       const int64_t e = row_of(kx, ky, a.N, kXB) * a.HP + kz;
-      const float2 w = slab_tw(twN, kx, a.s, a.N);
-      const float lnn2 = logf((float)n2);
-      const float kbar = -1.f + ra.c1 * expm1f(0.5f * ra.s * lnn2);
-      const float Lk = ra.log2kF + lnn2 * 0.72134752044448170368f;  // log2 k
-      const float inv_k2 = ra.inv_kF2 / (float)n2;
-      float P0 = 1.f, P1 = kbar;
-      int deg = 1;
       float2 s = first ? make_float2(0.f, 0.f) : acc_s[e];
       float2 c = first ? make_float2(0.f, 0.f) : acc_c[e];
+      const float2 w = __ldg(twN + m);
+      const float lg = __log2f((float)n2);
+      const float Lk = fmaf(0.5f, lg, ra.log2kF);  // log2 k
+      float2 ps = make_float2(0.f, 0.f), pc = make_float2(0.f, 0.f);
 #pragma unroll
-      for (int j = 0; j < MAXR; ++j) {
-        if (j < sl.nr) {
-          const int r = sl.r[j];
-          float rho;
-          if (r <= 3) {
-            rho = r == 3 ? 1.f : exp2f(ra.s * (float)(r - 3) * Lk);
-          } else {
-            while (deg < r - 1) {
-              ++deg;
-              const float Pn = ra.A[deg] * kbar * P1 - ra.B[deg] * P0;
+      for (int r = 0; r < 4 && r < MAXM; ++r)
+        if ((sm.active >> r) & 1u) {
+          const float rho = r == 3 ? 1.f : exp2f(ra.s * (float)(r - 3) * Lk);
+          neumaier_add(ps.x, pc.x, v[r].x * rho);
+          neumaier_add(ps.y, pc.y, v[r].y * rho);
+        }
+      if constexpr (MAXM > 4) {
+        if (sm.rmax >= 4) {
+          const float kbar = fmaf(ra.c1, exp2f(0.5f * ra.s * lg), -1.f - ra.c1);
+          const float inv_k2 = ra.inv_kF2 / (float)n2;
+          float P0 = 1.f, P1 = kbar;  // P_{l-1}, P_l with l = 1
+#pragma unroll
+          for (int r = 4; r < MAXM; ++r) {
+            if (r > sm.rmax) break;
+            // mode r takes P_{r-1}: one recurrence step (two for r = 4)
+#pragma unroll
+            for (int l = (r == 4 ? 2 : r - 1); l <= r - 1; ++l) {
+              const float Pn = ra.A[l] * kbar * P1 - ra.B[l] * P0;
               P0 = P1;
               P1 = Pn;
             }
-            rho = (P1 - ra.x0[r - 1]) * inv_k2;
+            if ((sm.active >> r) & 1u) {
+              const float rho = (P1 - ra.x0[r - 1]) * inv_k2;
+              neumaier_add(ps.x, pc.x, v[r].x * rho);
+              neumaier_add(ps.y, pc.y, v[r].y * rho);
+            }
           }
-          const float2 u = cmul(v[j], w);
-          neumaier_add(s.x, c.x, u.x * rho);
-          neumaier_add(s.y, c.y, u.y * rho);
         }
       }
+      const float2 u = cmul(ps, w), uc = cmul(pc, w);
+      neumaier_add(s.x, c.x, u.x);
+      neumaier_add(s.y, c.y, u.y);
+      c.x += uc.x;
+      c.y += uc.y;
       acc_s[e] = s;
       acc_c[e] = c;
     }
@@ -372,7 +435,7 @@ void slab_free(Plan* p) {
   if (s->have_r2c) cufftDestroy(s->r2c);
   if (s->fft_work) {
     cudaFree(s->fft_work);
-    p->used_bytes -= s->fft_bytes;
+    p->used_bytes -= s->fft_alloc;
   }
   delete s;
   p->slab = nullptr;
@@ -402,15 +465,8 @@ int slab_setup(Plan* p) {
   const size_t arena = std::max(modal, (size_t)(7 * ff + 6 * sf));
   SlabState* s = st_of(p);
   int rc;
+  cufftResult r;
   if (!p->d_phik && (rc = plan_alloc(p, (void**)&p->d_phik, sizeof(float2) * (size_t)ff))) return rc;
-  if (s && s->arena == arena && p->d_work) return AAR_OK;
-  if (p->d_work) {
-    cudaFree(p->d_work);
-    p->used_bytes -= sizeof(float2) * (s ? s->arena : (size_t)p->nwork * ff);
-    p->d_work = nullptr;
-    p->nwork = 0;
-  }
-  p->disp_real = false;
   if (!s) {
     s = new SlabState();
     p->slab = s;
@@ -419,7 +475,6 @@ int slab_setup(Plan* p) {
     s->H = H;
     s->sf = sf;
     s->ff = ff;
-    cufftResult r;
     size_t w1 = 0, w2 = 0;
     if ((r = cufftCreate(&s->c2r)) != CUFFT_SUCCESS) return cufft_err(p, "cufftCreate", r);
     s->have_c2r = true;
@@ -429,13 +484,32 @@ int slab_setup(Plan* p) {
     cufftSetAutoAllocation(s->r2c, 0);
     if ((r = cufftMakePlan3d(s->c2r, L, N, N, CUFFT_C2R, &w1)) != CUFFT_SUCCESS) return cufft_err(p, "cufftMakePlan3d C2R", r);
     if ((r = cufftMakePlan3d(s->r2c, L, N, N, CUFFT_R2C, &w2)) != CUFFT_SUCCESS) return cufft_err(p, "cufftMakePlan3d R2C", r);
-    s->fft_bytes = std::max<size_t>(std::max(w1, w2), 256);
-    if ((rc = plan_alloc(p, &s->fft_work, s->fft_bytes))) return rc;
+    s->fft_need = std::max<size_t>(std::max(w1, w2), 256);
+  }
+  if (s->fft_work && s->fft_alloc < s->fft_need) {
+    cudaFree(s->fft_work);
+    p->used_bytes -= s->fft_alloc;
+    s->fft_work = nullptr;
+    s->fft_alloc = 0;
+  }
+  if (!s->fft_work) {
+    if ((rc = plan_alloc(p, &s->fft_work, s->fft_need))) return rc;
+    s->fft_alloc = s->fft_need;
     if ((r = cufftSetWorkArea(s->c2r, s->fft_work)) != CUFFT_SUCCESS) return cufft_err(p, "cufftSetWorkArea", r);
     if ((r = cufftSetWorkArea(s->r2c, s->fft_work)) != CUFFT_SUCCESS) return cufft_err(p, "cufftSetWorkArea", r);
   }
-  if ((rc = plan_alloc(p, (void**)&p->d_work, sizeof(float2) * arena))) return rc;
-  s->arena = arena;
+  if (!(s->arena == arena && p->d_work)) {
+    if (p->d_work) {
+      cudaFree(p->d_work);
+      p->used_bytes -= sizeof(float2) * s->arena;
+      p->d_work = nullptr;
+      p->nwork = 0;
+      s->arena = 0;
+    }
+    p->disp_real = false;
+    if ((rc = plan_alloc(p, (void**)&p->d_work, sizeof(float2) * arena))) return rc;
+    s->arena = arena;
+  }
   s->M = M;
   s->R = R;
   p->nwork = 6;
@@ -479,7 +553,28 @@ int slab_run(Plan* p, cudaStream_t st) {
     cufftResult r = cufftExecR2C(s->r2c, (cufftReal*)x, (cufftComplex*)x);
     return r == CUFFT_SUCCESS ? AAR_OK : cufft_err(p, "cufftExecR2C", r);
   };
+  // n consecutive slab fields from x, one (L, N, N) transform each (measured:
+  // cuFFT's batched plans of the same transforms were slower -- 230 vs 159 ms
+  // for the 256 C2R of a 1024^3 step -- and needed a larger work area)
+  auto c2r_n = [&](float2* x, int n) -> int {
+    for (int i = 0; i < n; ++i) {
+      int rc2 = c2r(x + (int64_t)i * s->sf);
+      if (rc2) return rc2;
+    }
+    return AAR_OK;
+  };
+  auto r2c_n = [&](float2* x, int n) -> int {
+    for (int i = 0; i < n; ++i) {
+      int rc2 = r2c(x + (int64_t)i * s->sf);
+      if (rc2) return rc2;
+    }
+    return AAR_OK;
+  };
   SlabGeo geo{p->grid, N, p->HP, H, L, S, 0, sf};
+  auto herm = [&](float2* x, int nf) -> int {
+    SLAB_LAUNCH("slab_herm", k_slab_herm<<<nb, 256, 0, st>>>(x, nf, sf, L, N, H));
+    return AAR_OK;
+  };
   float2* phi = p->d_phik;
   const float2* twN = p->d_twN;
   if (R > 0) {
@@ -491,17 +586,18 @@ int slab_run(Plan* p, cudaStream_t st) {
     // product terms by target r (slot = ascending active r)
     static_assert(sizeof(SlabTerms) < 32000, "kernel parameter space");
     SlabTerms tm;
-    SlotList sl{};
+    SlotMap smap{};
     {
       const TermList& tl = *(const TermList*)p->host_terms.data();
       const Term* ft = (const Term*)(p->host_terms.data() + sizeof(TermList));
       tm.M = M;
       tm.nr = tl.nr;
-      sl.nr = tl.nr;
       int k = 0;
       for (int j = 0; j < tl.nr; ++j) {
         const int r = tl.r_of_slot[j];
-        sl.r[j] = r;
+        smap.active |= 1u << r;
+        smap.rmax = std::max(smap.rmax, r);
+        smap.slot[r] = j;
         tm.begin[j] = k;
         for (int i = 0; i < tl.nterms; ++i)
           if (ft[i].r == r) {
@@ -521,15 +617,14 @@ int slab_run(Plan* p, cudaStream_t st) {
         return AAR_OK;
       });
       if (rc) return rc;
-      for (int m = 0; m < M; ++m)
-        if ((rc = c2r(f + (int64_t)m * sf))) return rc;
-      SLAB_LAUNCH("slab_products", k_slab_products<<<nb, 256, 0, st>>>(tm, (const float*)f, (float*)g, 2 * sf, N, H,
-                                                                        (int64_t)L * N));
-      for (int j = 0; j < R; ++j)
-        if ((rc = r2c(g + (int64_t)j * sf))) return rc;
-      rc = by_modes(R, [&](auto rcn) {
-        constexpr int MR = decltype(rcn)::value;
-        SLAB_LAUNCH("slab_acc", k_slab_acc_modal<MR><<<nb, 256, 0, st>>>(geo, ra, sl, g, twN, acc_s, acc_c, sl_i == 0));
+      if ((rc = herm(f, M))) return rc;
+      if ((rc = c2r_n(f, M))) return rc;
+      SLAB_LAUNCH("slab_products", k_slab_products<<<2 * nb, kProdThreads, 0, st>>>(tm, (const float*)f, (float*)g,
+                                                                                     2 * sf, N, H, (int64_t)L * N));
+      if ((rc = r2c_n(g, R))) return rc;
+      rc = by_modes(smap.rmax + 1, [&](auto mc) {
+        constexpr int MM = decltype(mc)::value;
+        SLAB_LAUNCH("slab_acc", k_slab_acc_modal<MM><<<nb, 256, 0, st>>>(geo, ra, smap, g, twN, acc_s, acc_c, sl_i == 0));
         return AAR_OK;
       });
       if (rc) return rc;
@@ -544,8 +639,8 @@ int slab_run(Plan* p, cudaStream_t st) {
   for (int sl_i = 0; sl_i < S; ++sl_i) {
     geo.s = sl_i;
     SLAB_LAUNCH("slab_lpt_fold_hess", k_slab_fold_lpt<0><<<nb, 256, 0, st>>>(geo, la, phi, nullptr, twN, h));
-    for (int c = 0; c < 6; ++c)
-      if ((rc = c2r(h + (int64_t)c * sf))) return rc;
+    if ((rc = herm(h, 6))) return rc;
+    if ((rc = c2r_n(h, 6))) return rc;
     SLAB_LAUNCH("slab_lpt_source", k_slab_source<<<nb, 256, 0, st>>>((float*)h, 2 * sf, N, H, (int64_t)L * N));
     if ((rc = r2c(h))) return rc;
     SLAB_LAUNCH("slab_lpt_acc", k_slab_acc_plain<<<nb, 256, 0, st>>>(geo, h, twN, Sk, sl_i == 0));
@@ -553,8 +648,8 @@ int slab_run(Plan* p, cudaStream_t st) {
   for (int sl_i = 0; sl_i < S; ++sl_i) {
     geo.s = sl_i;
     SLAB_LAUNCH("slab_lpt_fold_disp", k_slab_fold_lpt<1><<<nb, 256, 0, st>>>(geo, la, phi, Sk, twN, h));
-    for (int c = 0; c < 6; ++c)
-      if ((rc = c2r(h + (int64_t)c * sf))) return rc;
+    if ((rc = herm(h, 6))) return rc;
+    if ((rc = c2r_n(h, 6))) return rc;
     SLAB_LAUNCH("slab_scatter", k_slab_scatter<<<nb, 256, 0, st>>>(geo, (const float*)h, 2 * sf, (float*)p->d_work,
                                                                     2 * ff));
   }

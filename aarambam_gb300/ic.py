@@ -39,8 +39,11 @@ def params_from_config(cfg: dict, precision: int = _lib.AAR_FUSED_FP32, mem_limi
 
 
 def _ptr(t: torch.Tensor) -> int:
-    if not t.is_cuda or not t.is_contiguous():
-        raise ValueError("expected a contiguous CUDA tensor")
+    """Address of a contiguous tensor the device can address: CUDA memory,
+    or page-locked host memory (pin_memory), which kernels read and write
+    directly over the host link."""
+    if not (t.is_cuda or t.is_pinned()) or not t.is_contiguous():
+        raise ValueError("expected a contiguous CUDA or pinned host tensor")
     return t.data_ptr()
 
 
@@ -240,7 +243,7 @@ class ICGenerator:
                     vel: torch.Tensor = None, ids: torch.Tensor = None):
         """Whole path for the regular glass_n^3 lattice glass tiled tile^3
         times (aar_run_lattice): no glass array; pos / vel float32 [n, 3]
-        and ids int32 [n] (optional) on the device."""
+        and ids int32 [n] (optional) on the device or in pinned host memory."""
         n = glass_n ** 3 * tile ** 3
         pos = torch.empty((n, 3), dtype=torch.float32, device=self.device) if pos is None else pos
         vel = torch.empty((n, 3), dtype=torch.float32, device=self.device) if vel is None else vel

@@ -44,7 +44,12 @@ WORKLOADS = {
     "scalarI_m20_n512": (512, 1000.0, "scalarI_m20_L1000_n1024", 20, 1024, 100.0),
     "scalarI_m12_n256": (256, 1000.0, "scalarI_m12_L1000_n512", 12, 512, 100.0),
     "local_m8_n128": (128, 500.0, "local_m8_L500_n128", 8, 128, 10.0),
+    # the large single run: 1536^3, Box 2000, resonant template (LogResonance
+    # w = 10, 20 modes); the slab form (fused fields would need 308 GB)
+    "logres_m20_n1536": (1536, 2000.0, "logres_w10_m20_L2000_n1536", 20, 1536, 100.0),
 }
+# workloads the fused form's fields do not fit: the slab form, this many x-slabs
+SLAB_DEFAULT = {"logres_m20_n1536": 8}
 # Batching: 32 realisations at 256^3, Box 500, each with its own seed and a
 # template cycling over Local / Equilateral / ScalarI (mass 0.5, 1, 1.5, 1.75)
 # with 6..20 modes, run as one CUDA graph (aar_batch_*).
@@ -80,6 +85,11 @@ def parse():
                     help="profiling case: the modal row kernel alone on NROWS rows (aar_profile_modal_rows)")
     ap.add_argument("--no-plain", action="store_true",
                     help="skip the plain FP64 cuFFT forms (reference loop structure and regrouped, 1 step each)")
+    ap.add_argument("--slab", type=int, default=0, metavar="S",
+                    help="run the slab form (AAR_SLAB_FP32) with S x-slabs (default for workloads whose fused "
+                         "fields do not fit one GPU)")
+    ap.add_argument("--slab-device-out", action="store_true",
+                    help="slab form: particles into device buffers instead of pinned host memory")
     return ap.parse_args()
 
 
@@ -545,6 +555,132 @@ def gpu_arm(args):
         dist.destroy_process_group()
 
 
+def slab_alg_bytes(name: str, N: int, S: int, M: int, R: int, npart: int) -> float:
+    """Algorithmic HBM bytes of one launch of each slab-form kernel (F = one
+    half-spectrum field, F_s = F / S one slab field; the accumulations
+    read-modify-write the two compensated accumulator fields)."""
+    F = 8.0 * N * N * (N // 2 + 1)
+    Fs = F / S
+    table = {
+        "seedtable": 4.0 * N * N, "noise": F + 4.0 * N * N,
+        "slab_fold": F + M * Fs, "slab_c2r": 2 * Fs, "slab_r2c": 2 * Fs, "slab_products": (M + R) * Fs,
+        "slab_acc": R * Fs + 4 * F, "slab_combine": 4 * F,
+        "slab_lpt_fold_hess": F + 6 * Fs, "slab_lpt_source": 7 * Fs, "slab_lpt_acc": Fs + 2 * F,
+        "slab_lpt_fold_disp": 2 * F + 6 * Fs, "slab_scatter": 12 * Fs,
+        # glass read-out: the six displacement fields once, Pos / Vel out
+        "readout_glass": 6 * 4.0 * N ** 3 + 24.0 * npart,
+    }
+    return table.get(name, float("nan"))
+
+
+def slab_arm(args):
+    """The slab form (AAR_SLAB_FP32) on one GPU: the 1536^3 large single run
+    (or any workload with --slab S).  Particles: the 64^3 lattice glass tiled
+    N/64 times (aar_run_lattice); by default written straight into pinned host
+    memory by the read-out (page-locked host buffers are device-addressable),
+    so the device holds only the plan (potential, arena, FFT work area)."""
+    import ctypes
+    import torch
+    from aarambam_gb300 import _lib
+    from aarambam_gb300.ic import ICGenerator
+    _lib.load(build_if_missing=True)
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    cfg = make_cfg(args.workload, 1234)
+    N, M = cfg["Nmesh"], cfg["N_modes"]
+    S = args.slab or SLAB_DEFAULT.get(args.workload, 8)
+    alpha, x0, k, t = load_tables(cfg["table"], M)
+    R = active_r(alpha)
+    free0, total = torch.cuda.mem_get_info()
+    gen = ICGenerator(cfg, alpha, x0, k, t, precision="slab_fp32", nslab=S)
+    gen.prepare()
+    gn = min(N, 64)
+    tile = N // gn
+    npart = N ** 3
+    host = not args.slab_device_out
+    t_alloc = time.perf_counter()
+
+    def pinned(shape):
+        # page-locked in place (cudaHostRegister): the caching host
+        # allocator behind pin_memory rounds sizes up to powers of two
+        a = torch.from_numpy(np.empty(shape, np.float32))
+        rc = torch.cuda.cudart().cudaHostRegister(a.data_ptr(), a.numel() * a.element_size(), 0)
+        if int(rc) != 0:
+            raise RuntimeError(f"cudaHostRegister failed ({rc})")
+        return a
+    mk = pinned if host else (lambda shape: torch.empty(shape, dtype=torch.float32, device=dev))
+    pos, vel = mk((npart, 3)), mk((npart, 3))
+    t_alloc = time.perf_counter() - t_alloc
+
+    # positions and velocities (IDs are 1-based int32 in the reference's
+    # 32-bit-ID build and would pass 2^31 at 1536^3)
+    def step():
+        gen.run_lattice(gn, 100.0, tile, pos, vel, None)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    free_min = torch.cuda.mem_get_info()[0]
+    clk = Clocks(0)
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    launches = 0
+    for _ in range(args.steps):
+        step()
+        launches += gen.launches
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    elapsed = e0.elapsed_time(e1) / 1e3
+    free_min = min(free_min, torch.cuda.mem_get_info()[0])
+    value = args.steps * npart / elapsed
+    # per-kernel times of one profiled step
+    buf = ctypes.create_string_buffer(1 << 16)
+    gen.L.aar_profile_enable(gen.h, 1)
+    step()
+    gen.L.aar_profile_report(gen.h, buf, len(buf))
+    gen.L.aar_profile_enable(gen.h, 0)
+    kernels = {}
+    for line in buf.value.decode().strip().splitlines():
+        nm, cnt, ms = line.split(",")
+        kernels[nm] = {"launches": int(cnt), "ms": float(ms)}
+    tot = sum(v["ms"] for v in kernels.values())
+    pk = peaks()
+    for nm, v in kernels.items():
+        per = v["ms"] / v["launches"] / 1e3
+        v["share"] = round(v["ms"] / tot, 4)
+        v["gbs"] = round(slab_alg_bytes(nm, N, S, M, R, npart) / per / 1e9, 1)
+    own = [n for n in kernels if n not in ("slab_c2r", "slab_r2c")]  # cuFFT: library kernels
+    dom = max(own, key=lambda n: kernels[n]["ms"])
+    d_per = kernels[dom]["ms"] / kernels[dom]["launches"] / 1e3
+    achieved = slab_alg_bytes(dom, N, S, M, R, npart) / d_per / 1e9
+    fft_ms = sum(kernels[n]["ms"] for n in ("slab_c2r", "slab_r2c") if n in kernels)
+    out_bytes = 24 * npart
+    print(json.dumps({
+        "metric": f"IC particles/s at {N}^3 (slab FP32 form)", "value": value, "unit": UNIT, "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"{args.workload}: Nmesh={N}^3 particles, Box={cfg['Box']} Mpc/h, {cfg['table']} "
+                               f"({M} modes, {R} active r), Fnl={cfg['Fnl']}, BBKS T(k), z=49, {gn}^3 lattice "
+                               f"glass tiled {tile}^3 times (aar_run_lattice)",
+                   "nmesh": N, "n_modes": M, "nslab": S, "l2": "working set >> L2 (no flush)",
+                   "parallelism": "single GPU",
+                   "particles": "pinned host memory, written by the read-out kernel" if host else "device buffers",
+                   "plan_device_bytes": gen.device_bytes,
+                   "peak_device_gb": round((total - free_min) / 1e9, 2),
+                   "device_gb_before": round((total - free0) / 1e9, 2),
+                   "host_alloc_s": round(t_alloc, 1)},
+        "roofline": {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": pk["hbm_gbs"],
+                     "unit": "GB/s", "frac": round(achieved / pk["hbm_gbs"], 4), "traffic": None,
+                     "peak_source": pk["source"]},
+        "cufft_share": round(fft_ms / tot, 4),
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": out_bytes if host else 0,
+                "api": "aar_run_lattice with page-locked host Pos/Vel buffers" if host else None},
+        "gpu_launches": launches, "clocks": clocks, "kernels": kernels}))
+
+
 def split_arm(args):
     """One realisation per step made by all ranks together: each rank
     regenerates the Gaussian potential, sums its share of the radial modes
@@ -825,5 +961,7 @@ if __name__ == "__main__":
         batch_arm(a)
     elif a.workload in DECOMP_WORKLOADS:
         decomp_arm(a)
+    elif a.slab or a.workload in SLAB_DEFAULT:
+        slab_arm(a)
     else:
         gpu_arm(a)

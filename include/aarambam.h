@@ -14,8 +14,11 @@
  *
  * Conventions: every call returns AAR_OK (0) or an error code (never exits);
  * aar_last_error() gives the message.  Device pointers are caller-owned CUDA
- * allocations on the plan's device; `stream` is a cudaStream_t (NULL = the
- * legacy default stream).  A plan owns its scratch and is not thread-safe;
+ * allocations on the plan's device, or page-locked host memory
+ * (cudaHostAlloc / cudaHostRegister), which the kernels address directly over
+ * the host link -- how the slab form writes 1536^3 particles that do not fit
+ * beside its fields; `stream` is a cudaStream_t (NULL = the legacy default
+ * stream).  A plan owns its scratch and is not thread-safe;
  * distinct plans may run concurrently on distinct streams.
  */
 #ifndef AARAMBAM_H

@@ -120,6 +120,28 @@ def test_slab_read_out_entry_points(cuda):
     assert np.array_equal(hi, ig.cpu().numpy())
 
 
+def test_slab_host_read_out(cuda):
+    """Page-locked host outputs (how the 1536^3 run returns its particles):
+    the read-out kernel writes them over the host link, bit-identical to the
+    read-out into device buffers (a glass tiled to 12^3 x 16^3 particles on
+    a 48^3 grid, off the grid points)."""
+    from aarambam_gb300 import gadget
+    N, g, tile, box = 48, 16, 12, 300.0
+    cfg = make_cfg(N, box, 8, 100.0, 8, "local_m8_L500_n128", 128)
+    gen = gen_for(cfg, precision="slab_fp32", nslab=4)
+    n = g ** 3 * tile ** 3
+    pd = torch.empty((n, 3), dtype=torch.float32, device=cuda)
+    vd = torch.empty_like(pd)
+    idd = torch.zeros(n, dtype=torch.int32, device=cuda)
+    gen.run_lattice(g, 100.0, tile, pd, vd, idd)
+    ph = torch.full((n, 3), float("nan"), dtype=torch.float32).pin_memory()
+    vh = torch.full((n, 3), float("nan"), dtype=torch.float32).pin_memory()
+    ih = torch.zeros(n, dtype=torch.int32).pin_memory()
+    gen.run_lattice(g, 100.0, tile, ph, vh, ih)
+    torch.cuda.synchronize()
+    assert torch.equal(ph, pd.cpu()) and torch.equal(vh, vd.cpu()) and torch.equal(ih, idd.cpu())
+
+
 def test_slab_memory(cuda):
     """Device memory of a slab plan: the potential, max(2F + (M + R) F_s,
     7F + 6 F_s) and the FFT work area (F one plan field, F_s one slab

@@ -67,6 +67,11 @@ struct Plan {
   int rtab_stride = 0;
   int64_t nsq = 0;            // 3 (N/2)^2 + 1
   int qtab_m = 0;             // modes the tables were allocated for
+  // field filters of the first modal pass over (|ky|, kz, |kx|), M (N/2+1)^3
+  // floats (qcube_build); made on first use after each table change
+  float* d_qcube = nullptr;
+  int qcube_m = 0;
+  bool qcube_stale = true;
   void* d_rlxpow = nullptr;   // skip-ahead powers (U576[32])
   int rlx_seg = 0;            // refills per seed-table thread
   // modal term list (device)
@@ -150,6 +155,7 @@ int launch_seedtable(Plan* p, uint32_t seed, uint32_t* d_out, cudaStream_t st);
 int launch_noise_fp32(Plan* p, const uint32_t* d_seed, float2* d_phik, cudaStream_t st);
 int launch_noise_fp64(Plan* p, const uint32_t* d_seed, double2* d_phik, int hp, cudaStream_t st);
 int fused_prepare(Plan* p);
+int qcube_build(Plan* p);
 struct Term;
 std::vector<std::vector<Term>> regrouped_terms(const std::vector<double>& alpha, int M);
 std::vector<int> modal_partition(const std::vector<std::vector<Term>>& by_r, int nparts);

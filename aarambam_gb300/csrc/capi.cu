@@ -238,7 +238,7 @@ static void plan_release(Plan* p) {
   p->prof.clear();
   for (auto e : p->event_pool) cudaEventDestroy(e);
   p->event_pool.clear();
-  void* ptrs[] = {p->d_phik, p->d_work, p->d_seed, p->d_twN, p->d_twH, p->d_amp, p->d_twb, p->d_rlxpow, p->d_terms, p->d_io, p->d_qtab, p->d_rtab, p->d_sinc, p->d_isinc2, p->d_adj_scratch};
+  void* ptrs[] = {p->d_phik, p->d_work, p->d_seed, p->d_twN, p->d_twH, p->d_amp, p->d_twb, p->d_rlxpow, p->d_terms, p->d_io, p->d_qtab, p->d_rtab, p->d_sinc, p->d_isinc2, p->d_adj_scratch, p->d_qcube};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   p->d_phik = p->d_work = nullptr;
@@ -248,6 +248,9 @@ static void plan_release(Plan* p) {
   p->d_rlxpow = p->d_terms = nullptr;
   p->d_qtab = p->d_rtab = nullptr;
   p->d_sinc = p->d_isinc2 = nullptr;
+  p->d_qcube = nullptr;
+  p->qcube_m = 0;
+  p->qcube_stale = true;
   p->d_io = nullptr;
   p->io_cap = 0;
   p->d_adj_scratch = nullptr;
@@ -481,7 +484,9 @@ static int ensure_fields(Plan* p) {
     int rc = plan_alloc(p, (void**)&p->d_phik, sizeof(float2) * (size_t)p->N * p->N * p->HP);
     if (rc) return rc;
   }
-  return alloc_fused(p, p->M);
+  int rc = alloc_fused(p, p->M);
+  if (rc) return rc;
+  return qcube_build(p);
 }
 
 static int ready(Plan* p) {
@@ -569,6 +574,7 @@ int aar_set_tables(aar_plan* h, const double* alpha, const double* x0, int32_t M
     if ((rc = build_term_list(p))) return rc;
   }
   if (p->prm.precision == AAR_FUSED_FP32) {
+    p->qcube_stale = true;  // rebuilt on first use (ensure_fields)
     if ((rc = mode_tables(p))) return rc;
     if (!p->d_terms && (rc = plan_alloc(p, &p->d_terms, terms_bytes()))) return rc;
     if ((rc = fused_prepare(p))) return rc;

@@ -755,7 +755,8 @@ struct Launch {
   }
   static int modal(Plan* p, const ModalArgs& a, cudaStream_t st) {
     int64_t fs = fstride(p);
-    XinvOp<N, W> xo{a, p->d_phik, p->d_work, fs, tiles(p), p->HP, rho_args(p), p->xpass_group};
+    XinvOp<N, W> xo{a, p->d_phik, p->d_work, fs, tiles(p), p->HP, rho_args(p), p->xpass_group,
+                    p->qcube_stale ? nullptr : p->d_qcube};
     int rc = run_pass<N>(p, xo, tiles(p) * a.M, st, "modal_xinv");
     if (rc) return rc;
     if ((rc = ypass<+1>(p, p->d_work, a.M, nullptr, st, "modal_ypass_inv"))) return rc;
@@ -985,6 +986,48 @@ static int build_terms(Plan* p) {
   p->host_terms.insert(p->host_terms.end(), (const char*)flat.data(), (const char*)(flat.data() + flat.size()));
   p->nterms = tl.nterms;
   p->nr_active = nr;
+  return AAR_OK;
+}
+
+// The filter cube of the first modal pass: q_p(|kx|, |ky|, kz) for
+// 0 <= |kx|, |ky|, kz <= N/2 with q_mode_cells' arithmetic, zero on the cut
+// and at k = 0 (keep_cell depends on |k_a| only).  Index ((p K + |ky|) K +
+// kz) K + |kx|, K = N/2 + 1.
+__global__ void __launch_bounds__(256) k_qcube(Grid g, RhoArgs ra, int M, float* __restrict__ q) {
+  const int K = g.N / 2 + 1;
+  const int64_t per = (int64_t)K * K * K;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < per; i += (int64_t)gridDim.x * blockDim.x) {
+    const int ax = (int)(i % K);
+    const int64_t r = i / K;
+    const int kz = (int)(r % K), ay = (int)(r / K);
+    int n2[1] = {ax * ax + ay * ay + kz * kz};
+    const bool on = n2[0] != 0 && keep_cell(g, ax, ay, kz);
+    if (!on) n2[0] = 1;
+    for (int p = 0; p < M; ++p) {
+      float v[1];
+      q_mode_cells<1>(ra, p, n2, v);
+      q[(int64_t)p * per + i] = on ? v[0] : 0.f;
+    }
+  }
+}
+
+int qcube_build(Plan* p) {
+  if (!p->qcube_stale && p->d_qcube) return AAR_OK;
+  const int64_t K = p->N / 2 + 1, per = K * K * K;
+  if (!p->d_qcube || p->qcube_m != p->M) {
+    if (p->d_qcube) cudaFree(p->d_qcube), p->used_bytes -= sizeof(float) * (size_t)per * p->qcube_m;
+    p->d_qcube = nullptr;
+    p->qcube_m = 0;
+    int rc = plan_alloc(p, (void**)&p->d_qcube, sizeof(float) * (size_t)per * p->M);
+    if (rc) return rc;
+    p->qcube_m = p->M;
+  }
+  k_qcube<<<(unsigned)(p->num_sms * 8), 256>>>(p->grid, rho_args(p), p->M, p->d_qcube);
+  AAR_CUDA_TRY(p, cudaGetLastError());
+  // made on the legacy stream once per table set; runs on the caller's
+  // streams read it afterwards
+  AAR_CUDA_TRY(p, cudaDeviceSynchronize());
+  p->qcube_stale = false;
   return AAR_OK;
 }
 

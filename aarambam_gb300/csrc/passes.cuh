@@ -111,11 +111,13 @@ __device__ __forceinline__ void group_order(int64_t item, int64_t tiles, int nc,
 
 // First modal pass: item = (tile group, p, tile) (group_order); phi tile
 // times q_p(k) (zero on the cut, DC and padding columns), inverse x FFT,
-// into field p.  q_p is evaluated per cell in FP32 (q_mode_cells: the
-// Legendre recurrence and expm1 form of kbar the accumulation uses for
-// rho_r), before the tile wait, so its arithmetic overlaps the tile load; it
-// replaced a gather from a per-|k|^2 table (3 MB per mode), whose latency the
-// pass could not hide.
+// into field p.  The factors come from the plan's filter cube (qcube_build:
+// q_p over (|ky|, kz, |kx|), made once per table set with q_mode_cells'
+// arithmetic): a lane's 16 factors of one column are 16 coalesced loads,
+// issued before the tile wait so that both latencies overlap.  Evaluated per
+// cell (qcube null: q_mode_cells, the Legendre recurrence per cell and mode)
+// the pass was issue-bound, 58 ms at 1024^3 with 20 modes; a gather from a
+// per-|k|^2 table (3 MB per mode, scattered indices) was latency-bound.
 template <int N, int W>
 struct XinvOp {
   ModalArgs a;
@@ -125,6 +127,7 @@ struct XinvOp {
   int HP;
   RhoArgs ra;
   int64_t grp;
+  const float* qcube;  // [M][N/2+1 |ky|][N/2+1 kz][N/2+1 |kx|], or null
   __device__ void coords(int64_t item, int& o, int& c0, int& p) const {
     int64_t t;
     group_order(item, tiles, a.M, grp, t, p);
@@ -156,37 +159,54 @@ struct XinvOp {
       const int t = threadIdx.x % C::T, w = threadIdx.x / C::T;
       const int kz = c0 + w;
       const bool col = kz <= N / 2;
-      const int c2 = ky * ky + kz * kz;
-      int n2[16];
-      bool on[16];
-#pragma unroll
-      for (int i = 0; i < 16; ++i) {
-        const int kx = t + C::T * i;  // < N/2
-        n2[i] = kx * kx + c2;
-        on[i] = col && n2[i] != 0 && keep_cell(a.g, kx, ky, kz);
-        if (!on[i]) n2[i] = 1;  // a harmless argument; the value is dropped
-      }
       float g[16];
-      q_mode_cells<16>(ra, p, n2, g);
-#pragma unroll
-      for (int i = 0; i < 16; ++i) {
-        g[i] = on[i] ? g[i] : 0.f;
-        r.f[i] = g[i];
-      }
       float gn = 0.f;  // lane 0: the value at n = N/2 (kx = -N/2)
-      if (t == 0) {
-        const int kx = -N / 2;
-        int m2[1] = {kx * kx + c2};
-        float v[1];
-        q_mode_cells<1>(ra, p, m2, v);
-        gn = col && keep_cell(a.g, kx, ky, kz) ? v[0] : 0.f;
+      if (qcube) {
+        constexpr int K = N / 2 + 1;
+        const float* qr = qcube + (((int64_t)p * K + (ky < 0 ? -ky : ky)) * K + (col ? kz : 0)) * K;
+#pragma unroll
+        for (int i = 0; i < 16; ++i) g[i] = col ? __ldg(qr + t + C::T * i) : 0.f;
+        if (t == 0) gn = col ? __ldg(qr + N / 2) : 0.f;
+      } else {
+        const int c2 = ky * ky + kz * kz;
+        int n2[16];
+        bool on[16];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+          const int kx = t + C::T * i;  // < N/2
+          n2[i] = kx * kx + c2;
+          on[i] = col && n2[i] != 0 && keep_cell(a.g, kx, ky, kz);
+          if (!on[i]) n2[i] = 1;  // a harmless argument; the value is dropped
+        }
+        q_mode_cells<16>(ra, p, n2, g);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) g[i] = on[i] ? g[i] : 0.f;
+        if (t == 0) {
+          const int kx = -N / 2;
+          int m2[1] = {kx * kx + c2};
+          float v[1];
+          q_mode_cells<1>(ra, p, m2, v);
+          gn = col && keep_cell(a.g, kx, ky, kz) ? v[0] : 0.f;
+        }
       }
+#pragma unroll
+      for (int i = 0; i < 16; ++i) r.f[i] = g[i];
       const int lane = threadIdx.x & 31;
       const int src = (lane - t) + (C::T - t) % C::T;
 #pragma unroll
       for (int j = 0; j < 16; ++j) {
         const float v = __shfl_sync(0xffffffffu, g[15 - j], src);
         r.f[16 + j] = t != 0 ? v : (j == 0 ? gn : g[j == 0 ? 0 : 16 - j]);
+      }
+    } else if (qcube) {
+      constexpr int K = N / 2 + 1;
+      const float* qp = qcube + ((int64_t)p * K + (ky < 0 ? -ky : ky)) * K * K;
+#pragma unroll
+      for (int i = 0; i < C::E; ++i) {
+        int n, w;
+        const bool own = fft_owned<N, W>(i, n, w);
+        const int kz = c0 + w, kx = sidx(n, N);
+        r.f[i] = own && kz <= N / 2 ? __ldg(qp + (int64_t)kz * K + (kx < 0 ? -kx : kx)) : 0.f;
       }
     } else {
       int n2[C::E];

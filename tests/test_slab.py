@@ -99,6 +99,29 @@ def test_slab_non_power_of_two_vs_plain_fp64(cuda, N, S, box):
     assert ed < 1e-5
 
 
+@pytest.mark.parametrize("kw", [dict(SphereMode=1, Nsample=40), dict(Fnl=0.0), dict(PhaseFlip=1, FixedAmplitude=1),
+                                dict(A_res=0.3, w_res=12.0, phi_res=0.4, WhichSpectrum=2)],
+                         ids=["sphere_cut", "fnl0", "flip_fixed", "resbasis"])
+def test_slab_options_vs_plain_fp64(cuda, kw):
+    """The slab form under the parameter-file options the other forms take
+    (sphere cut below Nyquist, no non-Gaussian term, phase flip with fixed
+    amplitude, the 2LPTResBasis oscillation) on a 48^3 grid, against the
+    plain FP64 regrouped form: potential to 1e-6, psi1 to 1e-5, particle
+    displacements to 1e-5."""
+    base = dict(Fnl=100.0)
+    base.update(kw)
+    fnl = base.pop("Fnl")
+    cfg = make_cfg(48, 300.0, 13, fnl, 10, "scalarI_m10_L500_n256", 256, **base)
+    lagr = lattice(48, 300.0, cuda)
+    pp, _, sp, fp = run_all(gen_for(cfg, precision="fp64_regrouped"), lagr)
+    ps, _, ss, fs = run_all(gen_for(cfg, precision="slab_fp32", nslab=4), lagr)
+    e_phi, e1 = rel_rms(ss, sp), rel_rms(fs[:3], fp[:3])
+    lg = lagr.cpu().numpy()
+    ed = rel_rms(periodic_delta(ps.cpu().numpy(), lg, 300.0), periodic_delta(pp.cpu().numpy(), lg, 300.0))
+    print(f"{kw}: phi {e_phi:.2e} psi1 {e1:.2e} disp {ed:.2e}")
+    assert e_phi < 1e-6 and e1 < 1e-5 and ed < 1e-5
+
+
 def test_slab_read_out_entry_points(cuda):
     """The slab form leaves the six real displacement fields in the plan's
     layout: aar_run_lattice, aar_run_glass and the host-glass entry point

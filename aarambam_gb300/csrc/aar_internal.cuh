@@ -78,6 +78,7 @@ struct Plan {
   void* d_terms = nullptr;
   std::vector<char> host_terms;  // the same term list on the host (kernel parameter of the row combine)
   int row_ls = 0;                // row-kernel line stride (float2) of this grid size
+  int row_lt = 0;                // float2 slots of the row kernels' lane twiddle table
   void* jit = nullptr;           // run-time specialised modal row kernel (jit.cu), or null
   int jit_mode = 1;              // 0 off, 1 for N >= 256, 2 always
   int jit_minb = 0;              // resident row blocks per SM of the NVRTC kernel (0: by N)

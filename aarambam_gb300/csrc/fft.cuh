@@ -160,6 +160,58 @@ __device__ __forceinline__ float2 tw_load(const float2* __restrict__ tw, int m) 
   return SIGN < 0 ? w : make_float2(w.x, -w.y);
 }
 
+// ------------------------------------------------- lane twiddle tables
+// Stage S >= 1 (span Ns, radix R) multiplies input r of the group of line
+// index j by exp(SIGN 2 pi i r k (N / (Ns R)) / N), k = j mod Ns: per lane a
+// function of k only, the same for every line.  A block keeps them in shared
+// memory as lt[lt_off(S) + (r - 1) Ns + k] = exp(-2 pi i m / N), m = r k
+// (N / (Ns R)), filled once per block (lt_fill), so a lane reads a stage's
+// R - 1 factors as conflict-free shared loads (the lanes of one k
+// broadcast) instead of R - 1 global loads per line at lane-scattered
+// indices of the N-point table -- as many loads per lane and line as it has
+// values, which made the twiddles the largest source of L1 wavefronts of the
+// row kernel after its shared-memory stages.
+__host__ __device__ constexpr int lt_off(int N, int E, int S) {
+  int off = 0;
+  for (int s = 1; s < S; ++s) off += (stage_radix(N, E, s) - 1) * stage_span(N, E, s);
+  return off;
+}
+__host__ __device__ constexpr int lt_size(int N, int E) { return lt_off(N, E, num_stages(N, E)); }
+// entry count rounded up to a whole 16 bytes (what follows stays aligned)
+__host__ __device__ constexpr int lt_slots(int N, int E) { return (lt_size(N, E) + 1) / 2 * 2; }
+
+// the exponent m of table entry i (0 <= i < lt_size(N, E))
+template <int N, int E>
+__device__ __forceinline__ int lt_exponent(int i) {
+  int s = 1, off = 0;
+  for (;;) {
+    const int R = stage_radix(N, E, s), Ns = stage_span(N, E, s), n = (R - 1) * Ns;
+    if (i < off + n) {
+      const int rem = i - off;
+      return (rem / Ns + 1) * (rem % Ns) * (N / (Ns * R));
+    }
+    off += n;
+    ++s;
+  }
+}
+
+// the table of an N-point line with E values per lane from tw (the table of
+// a line TWS times longer), by the block's nthreads threads; ASYNC: as
+// 8-byte cp.async copies (completed by the caller's cp.async wait), so the
+// fill costs no round trip before the thread's other loads issue
+template <int N, int E, int TWS, bool ASYNC = false>
+__device__ __forceinline__ void lt_fill(float2* lt, const float2* __restrict__ tw, int tid, int nthreads) {
+  for (int i = tid; i < lt_size(N, E); i += nthreads) {
+    const float2* src = tw + lt_exponent<N, E>(i) * TWS;
+    if constexpr (ASYNC) {
+      const unsigned d = (unsigned)__cvta_generic_to_shared(lt + i);
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+    } else {
+      lt[i] = __ldg(src);
+    }
+  }
+}
+
 // Shared-memory addresses of the stage loads and stores.  With the padding
 // spad(i) = i + i/16, an index t-part + C (C a multiple of 16) pads to
 // spad(t-part) + C + C/16, so a lane computes one padded base per stage and
@@ -231,14 +283,26 @@ __device__ __forceinline__ void unroll_br(F&& f) {
 // every group b, so the R - 1 twiddles are loaded once per stage.  The table
 // tw holds exp(-2 pi i m / (N TWS)); TWS > 1 reads a longer line's table
 // with stride TWS.
-template <int N, int T, int R, int Ns, int SIGN, int TWS = 1>
+// LT: tw is the block's lane twiddle table (shared memory), LTO this
+// stage's offset in it.
+template <int N, int T, int R, int Ns, int SIGN, int TWS = 1, bool LT = false, int LTO = 0>
+__device__ __forceinline__ float2 stage_twiddle(const float2* __restrict__ tw, int r, int k) {
+  if constexpr (LT) {
+    const float2 w = tw[LTO + (r - 1) * Ns + k];
+    return SIGN < 0 ? w : make_float2(w.x, -w.y);
+  } else {
+    return tw_load<SIGN>(tw, r * k * (N / (Ns * R)) * TWS);
+  }
+}
+
+template <int N, int T, int R, int Ns, int SIGN, int TWS = 1, bool LT = false, int LTO = 0>
 __device__ __forceinline__ void stage_compute(float2* v, int t, const float2* __restrict__ tw) {
   constexpr int E = N / T;
   if constexpr (Ns > 1 && T % Ns == 0 && E / R > 1) {
     const int k = t % Ns;
     float2 w[R];
 #pragma unroll
-    for (int r = 1; r < R; ++r) w[r] = tw_load<SIGN>(tw, r * k * (N / (Ns * R)) * TWS);
+    for (int r = 1; r < R; ++r) w[r] = stage_twiddle<N, T, R, Ns, SIGN, TWS, LT, LTO>(tw, r, k);
 #pragma unroll
     for (int b = 0; b < E / R; ++b) {
 #pragma unroll
@@ -253,7 +317,7 @@ __device__ __forceinline__ void stage_compute(float2* v, int t, const float2* __
         int k = j % Ns;
 #pragma unroll
         for (int r = 1; r < R; ++r)
-          v[b * R + r] = cmul(v[b * R + r], tw_load<SIGN>(tw, r * k * (N / (Ns * R)) * TWS));
+          v[b * R + r] = cmul(v[b * R + r], stage_twiddle<N, T, R, Ns, SIGN, TWS, LT, LTO>(tw, r, k));
       }
       DFT<R, SIGN>::run(v + b * R);
     }
@@ -295,8 +359,9 @@ __device__ __forceinline__ void line_sync(int bar_id) {
 // SCALE multiplies the values of the first stage as they are loaded (line
 // element t + T b + r N/R sits at v[b R + r]) by sc[b R + r] (SCALE 1) or by
 // i sc[b R + r] (SCALE 2): a per-element filter folded into the transform.
-// TWS: twiddle-table stride (tw of a line TWS times longer).
-template <int N, int T, int SIGN, int S = 0, int SCALE = 0, int TWS = 1>
+// TWS: twiddle-table stride (tw of a line TWS times longer).  LT: tw is the
+// block's lane twiddle table in shared memory (lt_fill<N, N/T, TWS>).
+template <int N, int T, int SIGN, int S = 0, int SCALE = 0, int TWS = 1, bool LT = false>
 __device__ __forceinline__ void line_fft_smem(float2* s, int t, const float2* __restrict__ tw, bool act,
                                               int bar_id = 1, const float* sc = nullptr) {
   constexpr int E = N / T;
@@ -313,11 +378,11 @@ __device__ __forceinline__ void line_fft_smem(float2* s, int t, const float2* __
     }
     line_sync<T>(bar_id);
     if (act) {
-      stage_compute<N, T, R, Ns, SIGN, TWS>(v, t, tw);
+      stage_compute<N, T, R, Ns, SIGN, TWS, LT, lt_off(N, E, S)>(v, t, tw);
       stage_store<N, T, R, Ns>(v, s, t);
     }
     line_sync<T>(bar_id);
-    line_fft_smem<N, T, SIGN, S + 1, 0, TWS>(s, t, tw, act, bar_id);
+    line_fft_smem<N, T, SIGN, S + 1, 0, TWS, LT>(s, t, tw, act, bar_id);
   }
 }
 

@@ -119,7 +119,11 @@ __device__ __forceinline__ void tile_store(const float2* sm, float2* __restrict_
 }
 
 // run the W line FFTs of a tile held in shared memory (SCALE: optional
-// per-element factors of the first stage, see line_fft_smem)
+// per-element factors of the first stage, see line_fft_smem).  The second
+// stage reads its twiddles from the global table: a per-block shared-memory
+// lane table (fft.cuh, as the row kernels use) made every tile pass at
+// 1024^3 slower (y pass 42.7 -> 46.7 ms with the table filled by cp.async
+// while the tile loads, 49.6 filled by plain loads).
 template <int N, int W, int SIGN, int SCALE = 0>
 __device__ __forceinline__ void tile_fft(float2* sm, const float2* __restrict__ tw, const float* sc = nullptr) {
   using C = AxisCfg<N, W>;
@@ -645,6 +649,8 @@ __global__ void __launch_bounds__(192, 4) k_rows_lattice(const float2* __restric
   if constexpr (RowFold<N>::value) {
     constexpr int h = H / 2, HO = h + h / 16;
     const bool act = rbase < rend;
+    // (the lane twiddle table of rows_body cost more than it saved here:
+    // one row per block, 13.1 -> 14.5 ms)
     float2* line = sm + warp * C::LS;
     if (act) row_c2r_pre_fold<N, true>(line, lane, twN, twH, zf, work + (int64_t)warp * fs + rbase * HP);
     __syncwarp();
@@ -741,8 +747,11 @@ struct Launch {
   static const int* slot_map(Plan* p) {
     return (const int*)((const char*)p->d_terms + offsetof(DevTerms, tl) + offsetof(TermList, r_of_slot));
   }
+  static constexpr size_t row_smem(int nlines) {
+    return sizeof(float2) * ((size_t)nlines * RowCfg<N>::LS + row_lt_slots<N>());
+  }
   static int configure(Plan* p) {
-    size_t sm_rows = sizeof(float2) * (size_t)(kMaxModes + 1) * RowCfg<N>::LS;
+    size_t sm_rows = row_smem(kMaxModes + 1);
     AAR_CUDA_TRY(p, cudaFuncSetAttribute(k_rows<N, ModalRowOp>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_rows));
     AAR_CUDA_TRY(p, cudaFuncSetAttribute(k_rows<N, SourceRowOp>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_rows));
     return AAR_OK;
@@ -760,7 +769,7 @@ struct Launch {
     int rc = run_pass<N>(p, xo, tiles(p) * a.M, st, "modal_xinv");
     if (rc) return rc;
     if ((rc = ypass<+1>(p, p->d_work, a.M, nullptr, st, "modal_ypass_inv"))) return rc;
-    size_t sm_rows = sizeof(float2) * (size_t)(a.M + 1) * RowCfg<N>::LS;
+    size_t sm_rows = row_smem(a.M + 1);
     if (p->jit) {
       if ((rc = jit_modal_rows(p, p->d_work, fs, st))) return rc;
       if ((rc = ypass<-1>(p, p->d_work, p->nr_active, slot_map(p), st, "modal_ypass_fwd"))) return rc;
@@ -834,7 +843,7 @@ struct Launch {
       YFanOp<N, W> yf{a, p->d_work, fs, tiles(p), p->HP, {0, 8, 8, 6, 6, 6}, {0, 1, 2, 3, 4, 5}, {0, 1, 0, 2, 1, 0}, 1};
       if ((rc = run_pass<N>(p, yf, tiles(p) * 6, st, "lpt_ypass_inv_hess"))) return rc;
     }
-    size_t sm_rows = sizeof(float2) * (size_t)7 * RowCfg<N>::LS;
+    size_t sm_rows = row_smem(7);
     SourceRowOp op{6, a.m.g.kF, a.isinc2};
     {
       ProfScope ps_(p, "lpt_rows_source", st);
@@ -1042,6 +1051,7 @@ int fused_prepare(Plan* p) {
   if (rc) return rc;
   if ((rc = dispatch_n(p->N, [&](auto nc) {
          p->row_ls = RowCfg<decltype(nc)::value>::LS;
+         p->row_lt = row_lt_slots<decltype(nc)::value>();
          return Launch<decltype(nc)::value>::configure(p);
        })))
     return rc;
@@ -1074,7 +1084,7 @@ int profile_modal_rows(Plan* p, float2* work, int64_t nrows, cudaStream_t st) {
         op.t[i].off = (uint32_t)(ft[i].p * LS) | ((uint32_t)(ft[i].q * LS) << 16) | (early << 31);
         op.t[i].c = ft[i].c;
       }
-    const size_t sm_rows = sizeof(float2) * (size_t)(p->M + 1) * LS;
+    const size_t sm_rows = Launch<N>::row_smem(p->M + 1);
     {
       ProfScope ps_(p, "modal_rows", st);
       k_rows<N, ModalRowOp><<<(unsigned)nrows, kRowThreads, sm_rows, st>>>(op, work, fs, p->HP, p->d_twN, p->d_twH);

@@ -227,7 +227,7 @@ int jit_prepare(Plan* p) {
     j->acc_fs = (int64_t)N * N * p->HP;
     p->jit = j;
   }
-  j->smem = sizeof(float2) * (size_t)(M + 1) * p->row_ls;
+  j->smem = sizeof(float2) * ((size_t)(M + 1) * p->row_ls + p->row_lt);
   if (cudaFuncSetAttribute((const void*)j->kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)j->smem) !=
       cudaSuccess) {
     cudaGetLastError();

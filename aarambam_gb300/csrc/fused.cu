@@ -382,7 +382,7 @@ __global__ void __launch_bounds__(256) k_rows_c2r(float2* work, int64_t fs, int 
     // folded radix-2 (rows.cuh): the halves hold z_{2m} and z_{2m+1}; lane
     // t writes the pair (z_{2m}, z_{2m+1}) as one 16-byte store
     constexpr int h = H / 2, HO = h + h / 16;
-    if (act) row_c2r_pre_fold<N, true>(line, lane, twN, twH, zf, f);
+    if (act) row_c2r_pre_fold<N>(line, lane, twN, twH, zf, f);
     __syncwarp();
     line_fft_smem<h, 16, +1, 0, 0, 2>(line + (lane >> 4) * HO, lane & 15, twH, act);
     if (act)
@@ -652,7 +652,7 @@ __global__ void __launch_bounds__(192, 4) k_rows_lattice(const float2* __restric
     // (the lane twiddle table of rows_body cost more than it saved here:
     // one row per block, 13.1 -> 14.5 ms)
     float2* line = sm + warp * C::LS;
-    if (act) row_c2r_pre_fold<N, true>(line, lane, twN, twH, zf, work + (int64_t)warp * fs + rbase * HP);
+    if (act) row_c2r_pre_fold<N>(line, lane, twN, twH, zf, work + (int64_t)warp * fs + rbase * HP);
     __syncwarp();
     line_fft_smem<h, 16, +1, 0, 0, 2>(line + (lane >> 4) * HO, lane & 15, twH, act);
   } else {

@@ -186,104 +186,107 @@ __device__ __forceinline__ float2 post1(float2 z, float2 zr, float2 w) {
   return make_float2(e.x + od.y, e.y - od.x);
 }
 
-// X from the line buffer (in place, GLOBAL false) or from the row in global
-// memory (GLOBAL true, `src`)
-// One quad of the folded pre-step: a = X_k, b = X_{H-k}, c = X_{h-k},
-// d = X_{h+k} (see row_c2r_pre_fold).
-template <int N>
-__device__ __forceinline__ void pre_fold_quad(float2* line, int k, float2 a, float2 b, float2 c, float2 d,
-                                              const float2* __restrict__ twN, const float2* __restrict__ twH,
-                                              ZFac zf);
+// The folded steps walk the quads k = lane + 32 it < Q in Q / 32 rounds; the
+// quad k = Q, which has two outputs only (positions Q and H - Q, where its
+// first and second output pairs coincide), rides with lane 0's first quad
+// k = 0, which has no second pair: lane 0 computes that pair from the quad
+// k = Q instead.  (With k = Q a round of its own, a fifth round ran a whole
+// warp for one quad.)  At j = Q the twiddles of the two pair formulas agree:
+// conj w_Q = i w_Q and -v_Q = conj v_Q (w_Q = e^{-i pi/4}, v_Q = -i).
 
-template <int N, bool GLOBAL = false>
+// Inverse pre-step into the line buffer, from X in global memory (src):
+// first pair (Z_k + Z_{k+h}, (Z_k - Z_{k+h}) e^{2 pi i k/H}) to positions k
+// and h + k from the quad at k; second pair to positions h - k2 and H - k2
+// from the quad at k2 (k2 = k, or Q for lane 0's first quad).
+template <int N>
 __device__ __forceinline__ void row_c2r_pre_fold(float2* line, int lane, const float2* __restrict__ twN,
                                                  const float2* __restrict__ twH, ZFac zf,
-                                                 const float2* __restrict__ src = nullptr) {
+                                                 const float2* __restrict__ src) {
   constexpr int H = N / 2, h = H / 2, Q = H / 4;
-  if constexpr (GLOBAL) {
-    // all of the lane's loads first (independent, in flight together), then
-    // the quads: the loads of one quad no longer wait for the previous
-    // quad's arithmetic and stores
-    constexpr int NIT = (Q + 32) / 32;  // quads k = lane + 32 it <= Q
-    float2 qa[NIT], qb[NIT], qc[NIT], qd[NIT];
+  static_assert(Q % 32 == 0, "folded rows: whole rounds of quads");
+  constexpr int NIT = Q / 32;
+  // all of the lane's loads first (independent, in flight together), then
+  // the quads: the loads of one quad do not wait for the previous quad's
+  // arithmetic and stores
+  float2 qa[NIT], qb[NIT], qc[NIT], qd[NIT];
 #pragma unroll
-    for (int it = 0; it < NIT; ++it) {
-      const int k = lane + 32 * it;
-      if (k <= Q) {
-        qa[it] = src[k];
-        qb[it] = src[H - k];
-        qc[it] = src[h - k];
-        qd[it] = src[h + k];
-      }
-    }
-#pragma unroll
-    for (int it = 0; it < NIT; ++it) {
-      const int k = lane + 32 * it;
-      if (k <= Q) pre_fold_quad<N>(line, k, qa[it], qb[it], qc[it], qd[it], twN, twH, zf);
-    }
-    return;
+  for (int it = 0; it < NIT; ++it) {
+    const int k = lane + 32 * it;
+    qa[it] = src[k];
+    qb[it] = src[H - k];
+    qc[it] = src[h - k];
+    qd[it] = src[h + k];
   }
-  for (int k = lane; k <= Q; k += 32)
-    pre_fold_quad<N>(line, k, line[spad(k)], line[spad(H - k)], line[spad(h - k)], line[spad(h + k)], twN, twH, zf);
-}
-
-template <int N>
-__device__ __forceinline__ void pre_fold_quad(float2* line, int k, float2 a, float2 b, float2 c, float2 d,
-                                              const float2* __restrict__ twN, const float2* __restrict__ twH,
-                                              ZFac zf) {
-  constexpr int H = N / 2, h = H / 2, Q = H / 4;
-  {
-    const float2 wk = __ldg(twN + k);  // e^{-2 pi i k/N}
-    const float2 vk = __ldg(twH + k);  // e^{-2 pi i k/H}
+  const float2 xq = src[Q], x3q = src[H - Q];  // the quad k = Q: X_Q, X_{H-Q} (= X_{h-Q}, X_{h+Q})
+  const float2 wQ = __ldg(twN + Q), vQ = __ldg(twH + Q);
+#pragma unroll
+  for (int it = 0; it < NIT; ++it) {
+    const int k = lane + 32 * it;
+    const bool l0 = it == 0 && lane == 0;
+    float2 a = qa[it], b = qb[it], c = qc[it], d = qd[it];
+    const int k2 = l0 ? Q : k;
+    const float2 wk = __ldg(twN + k), vk = __ldg(twH + k);
+    const float2 w2 = l0 ? wQ : wk, v2 = l0 ? vQ : vk;
+    float2 a2 = l0 ? xq : a, b2 = l0 ? x3q : b, c2 = l0 ? xq : c, d2 = l0 ? x3q : d;
     if (zf.type) {
       a = cscale(a, zf.at(k));
       b = cscale(b, zf.at(H - k));
       c = cscale(c, zf.at(h - k));
       d = cscale(d, zf.at(h + k));
+      a2 = l0 ? cscale(a2, zf.at(Q)) : a;
+      b2 = l0 ? cscale(b2, zf.at(H - Q)) : b;
+      c2 = l0 ? cscale(c2, zf.at(Q)) : c;
+      d2 = l0 ? cscale(d2, zf.at(H - Q)) : d;
     }
     if (k == 0) {  // FFTW c2r: Im X_0, Im X_{N/2} dropped
       a.y = 0.f;
       b.y = 0.f;
     }
-    // e^{+2 pi i j/N} at j = k, H-k, h-k, h+k: conj w, -w, i w, i conj w
+    // e^{+2 pi i j/N} at j = k, h+k: conj w, i conj w; at j = H-k2, h-k2: -w, i w
     const float2 zk = pre1(a, b, make_float2(wk.x, -wk.y));
-    const float2 zHk = pre1(b, a, make_float2(-wk.x, -wk.y));
-    const float2 zhm = pre1(c, d, make_float2(-wk.y, wk.x));
-    const float2 zhp = k == 0 ? zhm : pre1(d, c, make_float2(wk.y, wk.x));
-    // butterflies n = k and n = h - k; e^{2 pi i n/H}: conj v, -v
+    const float2 zhp = pre1(d, c, make_float2(wk.y, wk.x));
+    const float2 zHk = pre1(b2, a2, make_float2(-w2.x, -w2.y));
+    const float2 zhm = pre1(c2, d2, make_float2(-w2.y, w2.x));
+    // butterflies n = k and n = h - k2; e^{2 pi i n/H}: conj v, -v
     line[spad(k)] = cadd(zk, zhp);
     line[spad(h + k)] = cmul(csub(zk, zhp), make_float2(vk.x, -vk.y));
-    if (k != 0 && k != Q) {
-      line[spad(h - k)] = cadd(zhm, zHk);
-      line[spad(H - k)] = cmul(csub(zhm, zHk), make_float2(-vk.x, -vk.y));
-    }
+    line[spad(h - k2)] = cadd(zhm, zHk);
+    line[spad(H - k2)] = cmul(csub(zhm, zHk), make_float2(-v2.x, -v2.y));
   }
 }
 
+// Forward post-step from the line buffer to X (global): per quad k the four
+// outputs X_k, X_{H-k}, X_{h-k}, X_{h+k}; lane 0's first quad gives X_0,
+// X_H, X_h from k = 0 (Z_0 = E_0 + O_0 = Z_H, Z_h = E_0 - O_0) in the same
+// three formulas with its operands selected, and X_Q, X_{H-Q} from the quad
+// k = Q in the fourth and a fifth.
 template <int N>
 __device__ __forceinline__ void row_r2c_post_fold(const float2* line, float2* __restrict__ X, int lane,
                                                   const float2* __restrict__ twN, const float2* __restrict__ twH) {
   constexpr int H = N / 2, h = H / 2, Q = H / 4;
-  for (int k = lane; k <= Q; k += 32) {
-    const float2 wk = __ldg(twN + k);
-    const float2 vk = __ldg(twH + k);
+  static_assert(Q % 32 == 0, "folded rows: whole rounds of quads");
+  constexpr int NIT = Q / 32;
+  const float2 wQ = __ldg(twN + Q), vQ = __ldg(twH + Q);
+#pragma unroll
+  for (int it = 0; it < NIT; ++it) {
+    const int k = lane + 32 * it;
+    const bool l0 = it == 0 && lane == 0;
+    const int k2 = l0 ? Q : k;
+    const float2 wk = __ldg(twN + k), vk = __ldg(twH + k);
+    const float2 v2 = l0 ? vQ : vk;
     const float2 ek = line[spad(k)], ok = cmul(line[spad(h + k)], vk);
     const float2 zk = cadd(ek, ok), zhp = csub(ek, ok);
-    if (k == 0) {
-      // Z_0 = E_0 + O_0 = Z_H, Z_h = E_0 - O_0
-      X[0] = post1(zk, zk, wk);
-      X[H] = post1(zk, zk, make_float2(-1.f, 0.f));
-      X[h] = post1(zhp, zhp, make_float2(0.f, -1.f));
-      continue;
-    }
-    // Z_{h-k} = E_{h-k} - conj(v) O_{h-k}, Z_{H-k} = E_{h-k} + conj(v) O_{h-k}
-    const float2 em = line[spad(h - k)], om = cmul(line[spad(H - k)], make_float2(vk.x, -vk.y));
+    // Z_{h-k2} = E - conj(v) O, Z_{H-k2} = E + conj(v) O from positions h - k2, H - k2
+    const float2 em = line[spad(h - k2)], om = cmul(line[spad(H - k2)], make_float2(v2.x, -v2.y));
     const float2 zhm = csub(em, om), zHk = cadd(em, om);
     // e^{-2 pi i j/N} at j = k, H-k, h-k, h+k: w, -conj w, -i conj w, -i w
-    X[k] = post1(zk, zHk, wk);
-    X[H - k] = post1(zHk, zk, make_float2(-wk.x, wk.y));
-    if (k != Q) {
-      X[h - k] = post1(zhm, zhp, make_float2(-wk.y, -wk.x));
+    X[k] = post1(zk, l0 ? zk : zHk, wk);
+    X[H - k] = post1(l0 ? zk : zHk, zk, make_float2(-wk.x, wk.y));
+    X[h - k] = post1(l0 ? zhp : zhm, zhp, make_float2(-wk.y, -wk.x));
+    if (l0) {
+      X[Q] = post1(zhm, zHk, wQ);
+      X[H - Q] = post1(zHk, zhm, make_float2(-wQ.x, wQ.y));
+    } else {
       X[h + k] = post1(zhp, zhm, make_float2(wk.y, -wk.x));
     }
   }
@@ -335,8 +338,8 @@ __device__ __forceinline__ void rows_body(const Op& op, float2* work, int64_t fs
     for (int l = warp; l < op.nin(); l += nwarps) {
       float2* line = sm + l * C::LS;
       const float2* X = work + (int64_t)op.in_slot(l) * fs + row * HP;
-      if constexpr (Op::kZfac) row_c2r_pre_fold<N, true>(line, lane, twN, twH, op.zfac(l), X);
-      else row_c2r_pre_fold<N, true>(line, lane, twN, twH, ZFac{0, 0.f, nullptr}, X);
+      if constexpr (Op::kZfac) row_c2r_pre_fold<N>(line, lane, twN, twH, op.zfac(l), X);
+      else row_c2r_pre_fold<N>(line, lane, twN, twH, ZFac{0, 0.f, nullptr}, X);
       __syncwarp();
       line_fft_smem<h, 16, +1, 0, 0, 2, true>(line + half * HO, t16, lt, true);
     }

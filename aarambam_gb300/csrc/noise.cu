@@ -119,83 +119,122 @@ __device__ __forceinline__ void sincos_u48(uint64_t U, bool flip, float& c, floa
   }
 }
 
-// FP64: the amplitude and phase by the reference's FP64 formula
-// (main.c:443-459); OUT64: double2 output (the plain forms), else float2
-// (the fused form, FP64 math rounded at the end when FP64).
+// One cell (i, j, k) of a column from its two uniforms U1 (phase), U2
+// (amplitude): the Nyquist / DC skips after the draws, the cut, the
+// Hermitian pair of the k = 0 plane (main.c:396-459).  FP64: the amplitude
+// and phase by the reference's FP64 formula (main.c:443-459); OUT64: double2
+// output (the plain forms), else float2 (the fused form, FP64 math rounded at
+// the end when FP64).
+template <bool FP64, bool OUT64>
+__device__ __forceinline__ void noise_cell(const NoiseArgs& a, int i, int j, int k, uint64_t U1, uint64_t U2, double fx,
+                                           double fy, void* __restrict__ out, int HP) {
+  const int N = a.g.N;
+  if (i == N / 2 || j == N / 2) return;
+  if (i == 0 && j == 0 && k == 0) return;
+  const int kx = sidx(i, N), ky = sidx(j, N);
+  if (!keep_cell(a.g, kx, ky, k)) return;
+  const double box = a.g.box;
+  double re, im;
+  float rf = 0.f, imf = 0.f;
+  if (FP64) {
+    double fz = __ddiv_rn(__dmul_rn((double)(2 * k), kPi), box);
+    double k2 = __dadd_rn(__dadd_rn(__dmul_rn(fx, fx), __dmul_rn(fy, fy)), __dmul_rn(fz, fz));
+    double km = sqrt(k2);
+    double phase = __dmul_rn(__dmul_rn((double)U1 * 3.5527136788005009e-15, 2.0), kPi);
+    if (a.phase_flip) phase = __dadd_rn(phase, kPi);
+    double ampl = (double)U2 * 3.5527136788005009e-15;
+    double phig = noise_osc(a.prm, a.anorm * exp(a.ns * log(km)), km);
+    if (!a.fixed_amp) phig *= -log(ampl);
+    phig = sqrt(phig) * a.fac * a.beta / k2;
+    double sn, cs;
+    sincos(phase, &sn, &cs);
+    re = phig * cs;
+    im = phig * sn;
+    rf = (float)re;
+    imf = (float)im;
+  } else {
+    int n2 = kx * kx + ky * ky + k * k;
+    float amp = __ldg(a.amp + n2);
+    if (!a.fixed_amp) amp *= sqrtf(neg_log_u48(U2));
+    float c, sn;
+    sincos_u48(U1, a.phase_flip != 0, c, sn);
+    rf = amp * c;
+    imf = amp * sn;
+    re = rf;
+    im = imf;
+  }
+  int64_t c1 = -1, c2 = -1;
+  if (k > 0) {
+    c1 = row_of(i, j, N, a.xb) * HP + k;
+  } else if (i == 0) {
+    if (j >= N / 2) return;
+    c1 = row_of(0, j, N, a.xb) * HP;
+    c2 = row_of(0, N - j, N, a.xb) * HP;
+  } else {
+    if (i >= N / 2) return;
+    int ii = N - i, jj = (N - j) % N;
+    c1 = row_of(i, j, N, a.xb) * HP;
+    c2 = row_of(ii, jj, N, a.xb) * HP;
+  }
+  if (OUT64) {
+    double2* o = (double2*)out;
+    o[c1] = make_double2(re, im);
+    if (c2 >= 0) o[c2] = make_double2(re, -im);
+  } else {
+    float2* o = (float2*)out;
+    o[c1] = make_float2(rf, imf);
+    if (c2 >= 0) o[c2] = make_float2(rf, -imf);
+  }
+}
+
+// The rest of a column from cell k on with the generator as it stands:
+// draws one by one (U2 == 0 redrawn, main.c:401-403).  Taken from the
+// start of the first refill block whose pairing a redraw would shift -- a
+// zero U2 has probability 2^-48 -- and never otherwise.  Not inlined: the
+// state indexed by its running position lives in local memory here only.
+template <bool FP64, bool OUT64>
+__device__ __noinline__ void noise_column_rest(NoiseArgs a, Rlx s, int i, int j, int k, double fx, double fy,
+                                                void* __restrict__ out, int HP) {
+  for (; k < a.g.N / 2; ++k) {
+    const uint64_t U1 = rlx_next48(s);
+    uint64_t U2;
+    do U2 = rlx_next48(s);
+    while (U2 == 0);
+    noise_cell<FP64, OUT64>(a, i, j, k, U1, U2, fx, fy, out, HP);
+  }
+}
+
+// One thread per (i, j) column.  A refill of ranlxd1 gives 12 uniforms, the
+// (U1, U2) pairs of six cells while no U2 is zero: the column runs in blocks
+// of six cells reading the refilled state at compile-time indices (it stays
+// in registers), and a block with a zero U2 hands the column from its first
+// draw to noise_column_rest.  Same draws, same cells as one draw at a time.
 template <bool FP64, bool OUT64 = FP64>
 __global__ void k_noise(NoiseArgs a, const uint32_t* __restrict__ seedtable, void* __restrict__ out, int HP) {
   const int N = a.g.N;
   int64_t col = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (col >= (int64_t)N * N) return;
-  int i = (int)(col / N), j = (int)(col % N);
+  const int i = (int)(col / N), j = (int)(col % N);
   Rlx s;
   rlx_seed(s, seedtable[col]);
-  const int kx = sidx(i, N), ky = sidx(j, N);
-  const double box = a.g.box;
   double fx = 0, fy = 0;
   if (FP64) {
-    fx = __ddiv_rn(__dmul_rn((double)(2 * kx), kPi), box);
-    fy = __ddiv_rn(__dmul_rn((double)(2 * ky), kPi), box);
+    fx = __ddiv_rn(__dmul_rn((double)(2 * sidx(i, N)), kPi), a.g.box);
+    fy = __ddiv_rn(__dmul_rn((double)(2 * sidx(j, N)), kPi), a.g.box);
   }
-  for (int k = 0; k < N / 2; ++k) {
-    uint64_t U1 = rlx_next48(s);
-    uint64_t U2;
-    do U2 = rlx_next48(s);
-    while (U2 == 0);
-    if (i == N / 2 || j == N / 2) continue;
-    if (i == 0 && j == 0 && k == 0) continue;
-    if (!keep_cell(a.g, kx, ky, k)) continue;
-    double re, im;
-    float rf = 0.f, imf = 0.f;
-    if (FP64) {
-      double fz = __ddiv_rn(__dmul_rn((double)(2 * k), kPi), box);
-      double k2 = __dadd_rn(__dadd_rn(__dmul_rn(fx, fx), __dmul_rn(fy, fy)), __dmul_rn(fz, fz));
-      double km = sqrt(k2);
-      double phase = __dmul_rn(__dmul_rn((double)U1 * 3.5527136788005009e-15, 2.0), kPi);
-      if (a.phase_flip) phase = __dadd_rn(phase, kPi);
-      double ampl = (double)U2 * 3.5527136788005009e-15;
-      double phig = noise_osc(a.prm, a.anorm * exp(a.ns * log(km)), km);
-      if (!a.fixed_amp) phig *= -log(ampl);
-      phig = sqrt(phig) * a.fac * a.beta / k2;
-      double sn, cs;
-      sincos(phase, &sn, &cs);
-      re = phig * cs;
-      im = phig * sn;
-      rf = (float)re;
-      imf = (float)im;
-    } else {
-      int n2 = kx * kx + ky * ky + k * k;
-      float amp = __ldg(a.amp + n2);
-      if (!a.fixed_amp) amp *= sqrtf(neg_log_u48(U2));
-      float c, sn;
-      sincos_u48(U1, a.phase_flip != 0, c, sn);
-      rf = amp * c;
-      imf = amp * sn;
-      re = rf;
-      im = imf;
+  for (int k = 0; k < N / 2; k += 6) {
+    rlx_refill(s);  // every block consumes whole refills: the position is 12 here
+    const int nk = min(6, N / 2 - k);
+    bool zero = false;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) zero |= c < nk && s.x[2 * c + 1] == 0;
+    if (zero) {
+      noise_column_rest<FP64, OUT64>(a, s, i, j, k, fx, fy, out, HP);
+      return;
     }
-    int64_t c1 = -1, c2 = -1;
-    if (k > 0) {
-      c1 = row_of(i, j, N, a.xb) * HP + k;
-    } else if (i == 0) {
-      if (j >= N / 2) continue;
-      c1 = row_of(0, j, N, a.xb) * HP;
-      c2 = row_of(0, N - j, N, a.xb) * HP;
-    } else {
-      if (i >= N / 2) continue;
-      int ii = N - i, jj = (N - j) % N;
-      c1 = row_of(i, j, N, a.xb) * HP;
-      c2 = row_of(ii, jj, N, a.xb) * HP;
-    }
-    if (OUT64) {
-      double2* o = (double2*)out;
-      o[c1] = make_double2(re, im);
-      if (c2 >= 0) o[c2] = make_double2(re, -im);
-    } else {
-      float2* o = (float2*)out;
-      o[c1] = make_float2(rf, imf);
-      if (c2 >= 0) o[c2] = make_float2(rf, -imf);
-    }
+#pragma unroll
+    for (int c = 0; c < 6; ++c)
+      if (c < nk) noise_cell<FP64, OUT64>(a, i, j, k + c, s.x[2 * c], s.x[2 * c + 1], fx, fy, out, HP);
   }
 }
 

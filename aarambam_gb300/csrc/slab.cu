@@ -39,7 +39,6 @@
 
 #include <algorithm>
 #include <string>
-#include <vector>
 
 #include "aar_internal.cuh"
 #include "spectral.cuh"

@@ -84,6 +84,7 @@ struct Plan {
   int jit_minb = 0;              // resident row blocks per SM of the NVRTC kernel (0: by N)
   int jit_threads = 0;           // threads per block of the NVRTC row kernel (0: 256)
   int64_t xpass_group = 1;       // tiles per item group of the multi-output x passes (passes.cuh)
+  int noise_one_draw = 0;        // noise columns one draw at a time (AAR_NOISE_ONE_DRAW=1, a check)
   std::string jit_status = "off";
   int nterms = 0, nr_active = 0;
   int modal_part = 0, modal_nparts = 1;  // split of the modal sum over r (this plan's part)

@@ -395,6 +395,7 @@ static int create(Plan* p) {
   AAR_CUDA_TRY(p, cudaGetDevice(&p->dev));
   AAR_CUDA_TRY(p, cudaDeviceGetAttribute(&p->num_sms, cudaDevAttrMultiProcessorCount, p->dev));
   if (const char* g = getenv("AAR_XPASS_GROUP")) p->xpass_group = std::max(1LL, atoll(g));
+  if (const char* g = getenv("AAR_NOISE_ONE_DRAW")) p->noise_one_draw = atoi(g) == 1;
   if (const char* g = getenv("AAR_OUT_CHUNKS")) p->out_chunks = std::min(std::max(1, atoi(g)), (int)Plan::kOutChunks);
   p->N = N;
   p->HP = ((N / 2 + 1) + 7) / 8 * 8;

@@ -89,6 +89,7 @@ struct NoiseArgs {
   Grid g;
   int xb;  // row order of the output: row_of(i, j, N, xb)
   int phase_flip, fixed_amp;
+  int one_draw;  // every column one draw at a time (AAR_NOISE_ONE_DRAW=1: checks the six-cell blocks)
   // FP64 form: the reference's own formula
   double anorm, ns, fac, beta;
   aar_params prm;  // variant and ResBasis oscillation (noise_osc)
@@ -222,6 +223,10 @@ __global__ void k_noise(NoiseArgs a, const uint32_t* __restrict__ seedtable, voi
     fx = __ddiv_rn(__dmul_rn((double)(2 * sidx(i, N)), kPi), a.g.box);
     fy = __ddiv_rn(__dmul_rn((double)(2 * sidx(j, N)), kPi), a.g.box);
   }
+  if (a.one_draw) {
+    noise_column_rest<FP64, OUT64>(a, s, i, j, 0, fx, fy, out, HP);
+    return;
+  }
   for (int k = 0; k < N / 2; k += 6) {
     rlx_refill(s);  // every block consumes whole refills: the position is 12 here
     const int nk = min(6, N / 2 - k);
@@ -244,6 +249,7 @@ static NoiseArgs noise_args(Plan* p, int xb) {
   a.xb = xb;
   a.phase_flip = p->prm.phase_flip == 1;
   a.fixed_amp = p->prm.fixed_amplitude != 0;
+  a.one_draw = p->noise_one_draw;
   a.anorm = p->Anorm;
   a.ns = p->prm.primordial_index;
   a.fac = pow(2 * kPi / p->prm.box, 1.5);

@@ -74,6 +74,22 @@ def test_gaussian_spectrum(cuda, cfg):
     assert rel_rms(got, ref) < 3e-7
 
 
+@pytest.mark.parametrize("cfg", SMALL[:4], ids=lambda c: f"N{c['Nmesh']}_s{c['Seed']}")
+def test_noise_blocks_match_one_draw(cuda, cfg, monkeypatch):
+    """The noise kernel's six-cell blocks per generator refill give the
+    same spectrum, bit for bit, as drawing every column one uniform at a
+    time (the path a block with a zero U2 takes), FP32 and FP64 amplitude."""
+    for fp64 in (False, True):
+        g = gen_for(cfg, noise_fp64=fp64)
+        g.stage("noise")
+        fast = g.spectrum().cpu().numpy()
+        monkeypatch.setenv("AAR_NOISE_ONE_DRAW", "1")
+        h = gen_for(cfg, noise_fp64=fp64)
+        monkeypatch.delenv("AAR_NOISE_ONE_DRAW")
+        h.stage("noise")
+        assert np.array_equal(h.spectrum().cpu().numpy(), fast)
+
+
 @pytest.mark.parametrize("N", [16, 32, 64, 128])
 def test_transforms_match_numpy(cuda, N):
     cfg = make_cfg(N, 500.0, 1, 10.0, 8, "local_m8_L500_n128", 128)

@@ -15,6 +15,7 @@
 #include <nvrtc.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <string>
 #include <vector>
 
@@ -59,17 +60,45 @@ static std::string gen_source(int N, int M, int minb, int threads, int pairs, co
   s += "    float2 f[" + std::to_string(M) + "][K];\n";
   s += "#pragma unroll\n    for (int p = 0; p < " + std::to_string(M) + "; ++p)\n";
   s += "#pragma unroll\n      for (int i = 0; i < K; ++i) f[p][i] = sm[p * LS + pos[i]];\n";
-  // one block per output slot; terms accumulate in list order (the
-  // counter-term f0 f2 -> g1 into its own target r)
+  // one block per output slot (the counter-term f0 f2 -> g1 with its own
+  // target r).  The slot's terms are factored: greedily, the field that
+  // occurs in most remaining terms is taken out, g_r += f_F (sum_t c_t f_t),
+  // so a term costs one multiply-add and a group one more (at 20 modes 212
+  // operations for the 134 terms instead of 268).
   for (int sl = 0; sl < tl.nr; ++sl) {
     const int r = tl.r_of_slot[sl];
     s += "    {\n      float2 a[K];\n#pragma unroll\n      for (int i = 0; i < K; ++i) a[i] = make_float2(0.f, 0.f);\n";
-    for (size_t t = 0; t < terms.size(); ++t) {
-      if (terms[t].r != r) continue;
-      const std::string c = "kCoef[" + std::to_string(t) + "]", fp = "f[" + std::to_string(terms[t].p) + "][i]",
-                        fq = "f[" + std::to_string(terms[t].q) + "][i]";
-      s += "#pragma unroll\n      for (int i = 0; i < K; ++i) { a[i].x += " + c + " * " + fp + ".x * " + fq + ".x; a[i].y += " +
-           c + " * " + fp + ".y * " + fq + ".y; }\n";
+    std::vector<size_t> rem;
+    for (size_t t = 0; t < terms.size(); ++t)
+      if (terms[t].r == r) rem.push_back(t);
+    while (!rem.empty()) {
+      std::vector<int> cnt(M, 0);
+      for (size_t t : rem) {
+        cnt[terms[t].p] += 1;
+        if (terms[t].q != terms[t].p) cnt[terms[t].q] += 1;
+      }
+      const int F = (int)(std::max_element(cnt.begin(), cnt.end()) - cnt.begin());
+      std::vector<size_t> keep;
+      bool first = true;
+      for (size_t t : rem) {
+        if (terms[t].p != F && terms[t].q != F) {
+          keep.push_back(t);
+          continue;
+        }
+        const int o = terms[t].p == F ? terms[t].q : terms[t].p;
+        const std::string c = "kCoef[" + std::to_string(t) + "]", fo = "f[" + std::to_string(o) + "][i]";
+        if (first)
+          s += "      {\n      float2 h[K];\n#pragma unroll\n      for (int i = 0; i < K; ++i) h[i] = make_float2(" + c + " * " +
+               fo + ".x, " + c + " * " + fo + ".y);\n";
+        else
+          s += "#pragma unroll\n      for (int i = 0; i < K; ++i) { h[i].x = fmaf(" + c + ", " + fo + ".x, h[i].x); h[i].y = fmaf(" +
+               c + ", " + fo + ".y, h[i].y); }\n";
+        first = false;
+      }
+      const std::string fF = "f[" + std::to_string(F) + "][i]";
+      s += "#pragma unroll\n      for (int i = 0; i < K; ++i) { a[i].x = fmaf(" + fF + ".x, h[i].x, a[i].x); a[i].y = fmaf(" + fF +
+           ".y, h[i].y, a[i].y); }\n      }\n";
+      rem.swap(keep);
     }
     s += "#pragma unroll\n      for (int i = 0; i < K; ++i) sm[" + std::to_string(r) + " * LS + pos[i]] = a[i];\n    }\n";
   }

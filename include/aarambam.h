@@ -75,8 +75,9 @@ typedef struct aar_params {
                                in FP64 with the reference's formula, rounded to float at the end;
                                0 (default) = FP32 from the exact 48-bit uniforms */
   int32_t nslab;            /* AAR_SLAB_FP32: number of x-slabs S (Nmesh % S == 0, Nmesh / S >= 2);
-                               device memory ~ (8.8 + 39/S) fields of Nmesh^2 (Nmesh/2+1) complex
-                               floats at 20 modes; ignored by the other forms */
+                               device memory ~ 1 + max(2 + (M+R)/S, 7 + 6/S) fields of Nmesh^2
+                               (Nmesh/2+1) complex floats (M modes, R active r): 8.75 fields, 128 GB
+                               at 1536^3 with 20 modes and S = 8; ignored by the other forms */
 } aar_params;
 
 /* Host scalars of the set-up: power.c:391-448 (Norm = sigma8 normalisation,

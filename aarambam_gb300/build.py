@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libaarambam_gpu.so")
-SOURCES = ["noise.cu", "fused.cu", "capi.cu", "plain64.cu", "adjoint.cu", "jit.cu", "decomp.cu", "slab.cu"]
+SOURCES = ["noise.cu", "fused.cu", "capi.cu", "plain64.cu", "adjoint.cu", "jit.cu", "decomp.cu", "gram_tc.cu", "slab.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

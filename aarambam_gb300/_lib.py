@@ -35,6 +35,8 @@ EXPORTS = [
     "aar_batch_create", "aar_batch_run", "aar_batch_launch_count", "aar_batch_last_error", "aar_batch_destroy",
     "aar_set_spectrum", "aar_adj_spectral", "aar_adj_source", "aar_adj_products", "aar_set_jit", "aar_jit_status",
     "aar_tetra_covariance_scratch_bytes", "aar_tetra_covariance", "aar_tetra_QS", "aar_tetra_residual",
+    "aar_tetra_modes_ld", "aar_tetra_modes", "aar_modes_covariance_scratch_bytes", "aar_modes_covariance",
+    "aar_modes_project", "aar_modes_residual",
     "aar_bordered_cond", "aar_autotune", "aar_profile_modal_rows",
 ]
 AAR_ADJ_OP_ONE, AAR_ADJ_OP_GAUSS, AAR_ADJ_OP_Q, AAR_ADJ_OP_RHO = 0, 1, 2, 3
@@ -138,6 +140,14 @@ def load(build_if_missing: bool = False):
     L.aar_tetra_covariance.argtypes = [vp] + tetra + [vp, C.c_size_t, vp]
     L.aar_tetra_QS.argtypes = [vp, vp, i32] + tetra + [vp]
     L.aar_tetra_residual.argtypes = [vp, vp, vp, vp, i32] + tetra + [vp]
+    L.aar_tetra_modes_ld.argtypes = [i32]
+    L.aar_tetra_modes_ld.restype = i64
+    L.aar_tetra_modes.argtypes = [vp, i64, vp, vp, vp, i32, vp, vp, vp, i32, vp, i32, i32, vp]
+    L.aar_modes_covariance_scratch_bytes.argtypes = [i32, i32]
+    L.aar_modes_covariance_scratch_bytes.restype = C.c_size_t
+    L.aar_modes_covariance.argtypes = [vp, vp, i64, vp, i32, i32, vp, C.c_size_t, vp]
+    L.aar_modes_project.argtypes = [vp, vp, i32, vp, vp, i64, i32, i32, vp]
+    L.aar_modes_residual.argtypes = [vp, vp, vp, vp, i32, vp, i64, i32, vp]
     L.aar_bordered_cond.argtypes = [vp, vp, i32, vp, vp, i32, vp]
     L.aar_last_error.argtypes = [vp]
     L.aar_last_error.restype = C.c_char_p

@@ -13,9 +13,12 @@ What runs where:
                 functions, the model's shape function, the conjugate-gradient
                 solves (scipy, FP64) and the bookkeeping of the orthogonal
                 matching pursuit;
-  GPU (FP64)    the mode-bispectrum covariance QQ (tetrapyd.c:107-236), the
-                projections QS / QR (tetrapyd.c:238-305, cmbbest.pyx:419-426,
-                :459), the residual R on the tetrapyd (cmbbest.pyx:433) and
+  GPU           the mode bispectra Q_n(t) (FP64, made once per basis and
+                kept on the device), the mode-bispectrum covariance QQ
+                (tetrapyd.c:107-236) on the tensor cores, FP64-accurate (bf16
+                digits, exact level sums), and in FP64 the projections QS / QR
+                (tetrapyd.c:238-305, cmbbest.pyx:419-426, :459), the residual
+                R on the tetrapyd (cmbbest.pyx:433) and
                 one condition number per candidate mode and iteration
                 (cmbbest.pyx:44-47, :443-446) from the bordered-matrix secular
                 equation instead of an SVD per candidate
@@ -161,6 +164,14 @@ class Basis:
         as_d = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).to(dev)
         self._d = dict(w=as_d(self.tetrapyd_grid_weights), i1=as_i(i1), i2=as_i(i2), i3=as_i(i3), p1=as_i(p1),
                        p2=as_i(p2), p3=as_i(p3), f=as_d(self.mode_function_evaluations))
+        # the mode bispectra Q[n][t], made once and read by the covariance and
+        # by every projection and residual of the matching pursuit
+        d = self._d
+        self._ldq = int(_lib.load().aar_tetra_modes_ld(self.tetrapyd_grid_size))
+        self._Q = torch.empty((self.mode_indices.shape[1], self._ldq), dtype=torch.float64, device=dev)
+        self._call("aar_tetra_modes", _ptr(self._Q), self._ldq, _ptr(d["i1"]), _ptr(d["i2"]), _ptr(d["i3"]),
+                   self.tetrapyd_grid_size, _ptr(d["p1"]), _ptr(d["p2"]), _ptr(d["p3"]), self.mode_indices.shape[1],
+                   _ptr(d["f"]), self.mode_p_max, self.k_grid_size, self._stream())
 
     def _tetra_args(self):
         d = self._d
@@ -179,21 +190,23 @@ class Basis:
             raise _lib.AarError(rc, f"{name} failed")
 
     def compute_mode_bispectra_covariance(self):
-        """QQ[n][m] = sum_t w_t Q_n(t) Q_m(t) (tetrapyd.c:107-236), FP64 on the GPU."""
+        """QQ[n][m] = sum_t w_t Q_n(t) Q_m(t) (tetrapyd.c:107-236) on the GPU's
+        tensor cores, FP64-accurate, from the stored mode bispectra."""
         L = _lib.load()
         nm = self.mode_indices.shape[1]
-        nbytes = L.aar_tetra_covariance_scratch_bytes(self.tetrapyd_grid_size, nm)
+        nbytes = L.aar_modes_covariance_scratch_bytes(self.tetrapyd_grid_size, nm)
         scratch = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
         qq = torch.empty((nm, nm), dtype=torch.float64, device=self.device)
-        self._call("aar_tetra_covariance", _ptr(qq), *self._tetra_args(), _ptr(scratch), C.c_size_t(nbytes),
-                   self._stream())
+        self._call("aar_modes_covariance", _ptr(qq), _ptr(self._Q), self._ldq, _ptr(self._d["w"]),
+                   self.tetrapyd_grid_size, nm, _ptr(scratch), C.c_size_t(nbytes), self._stream())
         self._qq_dev = qq
         return qq.cpu().numpy()
 
     def _project_dev(self, X: torch.Tensor) -> torch.Tensor:
         X = X.to(self.device, torch.float64).contiguous()
         out = torch.empty((X.shape[0], self.mode_indices.shape[1]), dtype=torch.float64, device=self.device)
-        self._call("aar_tetra_QS", _ptr(out), _ptr(X), X.shape[0], *self._tetra_args(), self._stream())
+        self._call("aar_modes_project", _ptr(out), _ptr(X), X.shape[0], _ptr(self._d["w"]), _ptr(self._Q), self._ldq,
+                   self.tetrapyd_grid_size, self.mode_indices.shape[1], self._stream())
         return out
 
     def compute_QS_C(self, S):
@@ -206,8 +219,8 @@ class Basis:
         n = len(sel)
         sel_d = torch.from_numpy(np.ascontiguousarray(sel, dtype=np.int32)).to(self.device) if n else None
         coef_d = torch.from_numpy(np.ascontiguousarray(coef, dtype=np.float64)).to(self.device) if n else None
-        self._call("aar_tetra_residual", _ptr(R), _ptr(S_dev), _ptr(sel_d) if n else None,
-                   _ptr(coef_d) if n else None, n, *self._tetra_args(), self._stream())
+        self._call("aar_modes_residual", _ptr(R), _ptr(S_dev), _ptr(sel_d) if n else None,
+                   _ptr(coef_d) if n else None, n, _ptr(self._Q), self._ldq, self.tetrapyd_grid_size, self._stream())
         return R
 
     def _candidate_conds(self, qq_t_dev, msk):
@@ -280,18 +293,24 @@ class Basis:
                 msk = np.ones_like(msk, dtype=bool)
             it = 0
             t0 = time.time()
+            tp = dict.fromkeys(("cg", "residual", "cond", "project"), 0.0)  # seconds per pursuit phase
             while True:
                 if len(norms) <= np.sum(msk):
                     break
                 ix = np.ix_(msk, msk)
+                ta = time.perf_counter()
                 alpha_tmp, _ = conjugate_gradient(QQ_tilde[ix] + np.eye(np.sum(msk)) * regularization, QS_tilde[msk],
                                                   rtol=rtol, atol=0, maxiter=int(Niter))
+                tb = time.perf_counter()
                 # residual of the first shape on the tetrapyd (the reference
                 # subtracts from every row of S and reads element [0, 0])
                 sel = np.where(msk)[0]
                 use = good[sel]
                 R = self._residual_dev(S_dev, sel[use], (alpha_tmp / norms[sel])[use])
                 RR = float(torch.sum(R * R * w_dev))
+                tc = time.perf_counter()
+                tp["cg"] += tb - ta
+                tp["residual"] += tc - tb
                 delta_RR = RR / shape_covariance
                 if np.abs(delta_RR[0, 0]) <= RR_tol:
                     if self.verbose:
@@ -301,13 +320,17 @@ class Basis:
                     if self.verbose:
                         print("\n USED ALL AVAILABLE MODES", flush=True)
                     break
+                ta = time.perf_counter()
                 cond_here, cond = self._candidate_conds(qq_t_dev, msk)
+                tp["cond"] += time.perf_counter() - ta
                 fcond = cond / cond_here - 1
                 if cond_here > cond_tol:
                     if self.verbose:
                         print(f"\n HIT LIMIT OF COND NUM {cond_here:0.4e} > {cond_tol:0.4e}. ENDING SEARCH", flush=True)
                     break
+                ta = time.perf_counter()
                 QR = self._project_dev(R)[0].cpu().numpy() / norms / np.sqrt(RR)
+                tp["project"] += time.perf_counter() - ta
                 QR[badinds] = 0
                 QR = QR[np.invert(msk)]
                 m = np.argsort(np.abs(QR))[-10:]
@@ -316,6 +339,8 @@ class Basis:
                 msk[m] = True
                 it += 1
                 self.omp_log.append((it, float(delta_RR[0, 0]), float(cond_here), int(m)))
+            self.timings.update({f"pursuit_{k}_s": v for k, v in tp.items()})
+            self.timings["pursuit_s"] = time.time() - t0
             if self.verbose:
                 print(f"\n USING MODES {np.where(msk)[0]} ({it} pursuit steps in {time.time() - t0:.2f} s)")
             alpha_tmp, _ = conjugate_gradient(QQ_tilde[np.ix_(msk, msk)] + np.eye(np.sum(msk)) * regularization,

@@ -12,6 +12,10 @@
 //   k_tetra_project out[s][n] = sum_t X_s(t) w_t Q_n(t) (QS for the shape, QR for
 //                  the residual), one warp per (mode, shape);
 //   k_tetra_residual R(t) = S(t) - sum_j c_j Q_{n_j}(t) over the selected modes;
+//   k_modes_project, k_modes_residual  the same from the mode bispectra Q[n][t]
+//                  stored once per basis (aar_tetra_modes, gram_tc.cu): the
+//                  pursuit's per-step projection reads 8 bytes per (mode,
+//                  point) instead of evaluating the 3 x 3 permanent in FP64;
 //   k_bordered_cond  cond of [[A, b_i], [b_i^T, c_i]] for every candidate i
 //                  from the eigen-decomposition A = V diag(lam) V^T of the
 //                  selected block: with z = V^T b_i the extreme eigenvalues
@@ -61,6 +65,47 @@ __global__ void k_tetra_residual(Tetra a, const double* __restrict__ S, const in
       const int n = sel[j];
       sum += coef[j] * q_eval(f, a.nk, a.p1[n], a.p2[n], a.p3[n], x, y, z);
     }
+    R[t] = S[t] - sum;
+  }
+}
+
+// The same two sums from stored mode bispectra Q[n][t] (row stride ldq):
+// the terms, their order and the warp reduction of k_tetra_project and
+// k_tetra_residual, with Q read instead of evaluated.  Each lane issues the
+// loads of eight of its points before their multiply-adds.
+__global__ void k_modes_project(const double* __restrict__ Q, long long ldq, const double* __restrict__ w, int npts,
+                                int nmodes, const double* __restrict__ X, int nshapes, double* __restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  const int64_t wid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (wid >= (int64_t)nmodes * nshapes) return;
+  const int n = (int)(wid % nmodes), s = (int)(wid / nmodes);
+  const double* q = Q + (size_t)n * ldq;
+  const double* x = X + (int64_t)s * npts;
+  double acc = 0.0;
+  int t = lane;
+  for (; t + 7 * 32 < npts; t += 8 * 32) {
+    double xv[8], wv[8], qv[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      xv[j] = x[t + 32 * j];
+      wv[j] = w[t + 32 * j];
+      qv[j] = q[t + 32 * j];
+    }
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc = fma(xv[j] * wv[j], qv[j], acc);
+  }
+  for (; t < npts; t += 32) acc = fma(x[t] * w[t], q[t], acc);
+#pragma unroll
+  for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (lane == 0) out[(int64_t)s * nmodes + n] = acc;
+}
+
+__global__ void k_modes_residual(const double* __restrict__ Q, long long ldq, int npts, const double* __restrict__ S,
+                                 const int* __restrict__ sel, const double* __restrict__ coef, int nsel,
+                                 double* __restrict__ R) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < npts; t += gridDim.x * blockDim.x) {
+    double sum = 0.0;
+    for (int j = 0; j < nsel; ++j) sum += coef[j] * Q[(size_t)sel[j] * ldq + t];
     R[t] = S[t] - sum;
   }
 }
@@ -164,6 +209,26 @@ int aar_tetra_residual(double* d_R, const double* d_S, const int32_t* d_sel, con
   if (e != cudaSuccess) return tetra_status(e);
   k_tetra_residual<<<(unsigned)((tetra_npts + 255) / 256), 256, smem, (cudaStream_t)stream>>>(a, d_S, d_sel, d_coef,
                                                                                                 n_sel, d_R);
+  return tetra_status(cudaGetLastError());
+}
+
+int aar_modes_project(double* d_out, const double* d_X, int32_t n_shapes, const double* d_tetra_weights,
+                      const double* d_Q, int64_t ldq, int32_t tetra_npts, int32_t n_modes, void* stream) {
+  if (!d_out || !d_X || !d_tetra_weights || !d_Q || n_shapes < 1 || tetra_npts < 1 || n_modes < 1 ||
+      ldq < tetra_npts)
+    return AAR_ERR_ARG;
+  const int64_t warps = (int64_t)n_modes * n_shapes;
+  k_modes_project<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
+      d_Q, ldq, d_tetra_weights, tetra_npts, n_modes, d_X, n_shapes, d_out);
+  return tetra_status(cudaGetLastError());
+}
+
+int aar_modes_residual(double* d_R, const double* d_S, const int32_t* d_sel, const double* d_coef, int32_t n_sel,
+                       const double* d_Q, int64_t ldq, int32_t tetra_npts, void* stream) {
+  if (!d_R || !d_S || !d_Q || n_sel < 0 || (n_sel > 0 && (!d_sel || !d_coef)) || tetra_npts < 1 || ldq < tetra_npts)
+    return AAR_ERR_ARG;
+  k_modes_residual<<<(unsigned)((tetra_npts + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
+      d_Q, ldq, tetra_npts, d_S, d_sel, d_coef, n_sel, d_R);
   return tetra_status(cudaGetLastError());
 }
 

@@ -36,7 +36,9 @@
 // 4.4e-15.
 //
 // Kernels:
-//   k_tetra_q       Q[n][t] in FP64 (stored once) and the row maxima of |wQ|, |Q|;
+//   k_tetra_modes   Q[n][t] in FP64 (kept by the caller for the stored-mode
+//                   entry points; the stateless entry point makes it in its
+//                   scratch), k_modes_rowmax the row maxima of |wQ| and |Q|;
 //   k_tetra_digits  the bf16 digits of A (128-row tiles) and B (64-row tiles)
 //                   in the tcgen05 no-swizzle K-major layout, 16 points per
 //                   chunk, the eight digits of a (tile, chunk) contiguous;
@@ -181,24 +183,30 @@ __device__ __forceinline__ void tmem_ld4(uint32_t taddr, uint32_t (&r)[4]) {
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 // ---------------------------------------------------------------- operands
-// Q[n][t] (t < npts_pad; 0 beyond npts) and the row maxima of |w Q| (rowmax[n])
-// and |Q| (rowmax[nm + n]) as the bit patterns of non-negative doubles.
-__global__ void __launch_bounds__(256) k_tetra_q(Tetra a, int npts_pad, double* __restrict__ Q,
-                                                 unsigned long long* __restrict__ rowmax) {
+// Q[n][t] = Q_n(t) for t < npts, 0 for npts <= t < ldq (the mode bispectra
+// kept by the caller for the stored-mode entry points).
+__global__ void __launch_bounds__(256) k_tetra_modes(Tetra a, long long ldq, double* __restrict__ Q) {
   const int n = blockIdx.y;
   const double* r1 = a.f + a.p1[n] * a.nk;
   const double* r2 = a.f + a.p2[n] * a.nk;
   const double* r3 = a.f + a.p3[n] * a.nk;
-  double* qrow = Q + (size_t)n * npts_pad;
+  double* qrow = Q + (size_t)n * ldq;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < ldq; t += (long long)gridDim.x * blockDim.x)
+    qrow[t] = t < a.npts ? q_rows(r1, r2, r3, a.i1[t], a.i2[t], a.i3[t]) : 0.0;
+}
+
+// Row maxima of |w Q| (rowmax[n]) and |Q| (rowmax[nm + n]) over t < npts, as
+// the bit patterns of non-negative doubles.
+__global__ void __launch_bounds__(256) k_modes_rowmax(const double* __restrict__ Q, long long ldq,
+                                                      const double* __restrict__ w, int npts, int nm,
+                                                      unsigned long long* __restrict__ rowmax) {
+  const int n = blockIdx.y;
+  const double* qrow = Q + (size_t)n * ldq;
   double mA = 0.0, mB = 0.0;
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < npts_pad; t += gridDim.x * blockDim.x) {
-    double q = 0.0;
-    if (t < a.npts) {
-      q = q_rows(r1, r2, r3, a.i1[t], a.i2[t], a.i3[t]);
-      mB = fmax(mB, fabs(q));
-      mA = fmax(mA, fabs(q * a.w[t]));
-    }
-    qrow[t] = q;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < npts; t += gridDim.x * blockDim.x) {
+    const double q = qrow[t];
+    mB = fmax(mB, fabs(q));
+    mA = fmax(mA, fabs(q * w[t]));
   }
 #pragma unroll
   for (int o = 16; o; o >>= 1) {
@@ -217,7 +225,7 @@ __global__ void __launch_bounds__(256) k_tetra_q(Tetra a, int npts_pad, double* 
       mB = fmax(mB, sB[i]);
     }
     atomicMax(rowmax + n, (unsigned long long)__double_as_longlong(mA));
-    atomicMax(rowmax + a.nmodes + n, (unsigned long long)__double_as_longlong(mB));
+    atomicMax(rowmax + nm + n, (unsigned long long)__double_as_longlong(mB));
   }
 }
 
@@ -251,8 +259,9 @@ __device__ __forceinline__ int row_exponent(unsigned long long bits) {
 // K-major layout ((r / 8) * 256 + kseg * 128 + (r % 8) * 16), so consecutive
 // threads write consecutive 16 bytes; the same row's B digits go to the
 // 64-row tile of the same row.
-__global__ void __launch_bounds__(256) k_tetra_digits(const double* __restrict__ Q, const double* __restrict__ w,
-                                                      int nm, int npts, int npts_pad, int nch, int rowsA, int rowsB,
+__global__ void __launch_bounds__(256) k_tetra_digits(const double* __restrict__ Q, long long ldq,
+                                                      const double* __restrict__ w, int nm, int npts, int nch,
+                                                      int rowsA, int rowsB,
                                                       const unsigned long long* __restrict__ rowmax,
                                                       uint4* __restrict__ adig, uint4* __restrict__ bdig,
                                                       int* __restrict__ expo) {
@@ -269,7 +278,7 @@ __global__ void __launch_bounds__(256) k_tetra_digits(const double* __restrict__
   if (n < nm) {
     eA = row_exponent(rowmax[n]);
     eB = row_exponent(rowmax[nm + n]);
-    const double2* src = reinterpret_cast<const double2*>(Q + (size_t)n * npts_pad + t0);
+    const double2* src = reinterpret_cast<const double2*>(Q + (size_t)n * ldq + t0);
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const double2 v = src[j];
@@ -521,14 +530,17 @@ __global__ void k_gram_tc_reduce(const long long* __restrict__ part, int nsplit,
 // ---------------------------------------------------------------- host
 struct GramPlan {
   int npts_pad, nch, ngroups, ntA, ntB, rowsA, rowsB, npairs, nsplit, gps;
-  size_t off_q, off_max, off_exp, off_a, off_b, off_pairs, off_pid, off_part, off_err, total;
+  size_t off_max, off_exp, off_a, off_b, off_pairs, off_pid, off_part, off_err, total;
 };
 
 size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
+// Q row stride of the stored-mode layout: npts rounded up to whole 128-point groups
+long long modes_ld(int npts) { return (long long)align_up((size_t)npts, kPts); }
+
 GramPlan gram_plan(int npts, int nm) {
   GramPlan p;
-  p.npts_pad = (int)align_up((size_t)npts, kPts);
+  p.npts_pad = (int)modes_ld(npts);
   p.nch = p.npts_pad / kTK;
   p.ngroups = p.npts_pad / kPts;
   p.ntA = (nm + kTM - 1) / kTM;
@@ -548,7 +560,6 @@ GramPlan gram_plan(int npts, int nm) {
     o = align_up(o + bytes, 1024);
     return at;
   };
-  p.off_q = take((size_t)nm * p.npts_pad * sizeof(double));
   p.off_max = take((size_t)2 * nm * sizeof(unsigned long long));
   p.off_exp = take((size_t)2 * p.rowsA * sizeof(int));
   p.off_a = take((size_t)p.ntA * p.nch * kStageA);
@@ -561,30 +572,20 @@ GramPlan gram_plan(int npts, int nm) {
   return p;
 }
 
-}  // namespace
-}  // namespace aar
+size_t q_bytes(int npts, int nm) { return align_up((size_t)nm * modes_ld(npts) * sizeof(double), 1024); }
 
-using namespace aar;
-
-extern "C" {
-
-size_t aar_tetra_covariance_scratch_bytes(int32_t tetra_npts, int32_t n_modes) {
-  if (tetra_npts <= 0 || n_modes <= 0) return 0;
-  return gram_plan(tetra_npts, n_modes).total;
+int launch_modes(const Tetra& a, double* Q, long long ldq, cudaStream_t st) {
+  const long long blocks = (ldq + 255) / 256;
+  k_tetra_modes<<<dim3((unsigned)(blocks < 64 ? blocks : 64), a.nmodes), 256, 0, st>>>(a, ldq, Q);
+  return tetra_status(cudaGetLastError());
 }
 
-int aar_tetra_covariance(double* d_cov, const double* d_tetra_weights, const int32_t* d_i1, const int32_t* d_i2,
-                         const int32_t* d_i3, int32_t tetra_npts, const int32_t* d_p1, const int32_t* d_p2,
-                         const int32_t* d_p3, int32_t n_modes, const double* d_mode_evals, int32_t mode_p_max,
-                         int32_t k_npts, void* d_scratch, size_t scratch_bytes, void* stream) {
-  const Tetra a = make_tetra(d_tetra_weights, d_i1, d_i2, d_i3, tetra_npts, d_p1, d_p2, d_p3, n_modes, d_mode_evals,
-                             mode_p_max, k_npts);
-  if (!d_cov || !d_scratch || !tetra_ok(a)) return AAR_ERR_ARG;
-  if (scratch_bytes < aar_tetra_covariance_scratch_bytes(tetra_npts, n_modes)) return AAR_ERR_ARG;
-  cudaStream_t st = (cudaStream_t)stream;
-  const GramPlan p = gram_plan(tetra_npts, n_modes);
+// covariance from stored Q (row stride ldq, a multiple of 128 >= npts, zero
+// beyond npts); d_scratch: gram_plan(npts, nm).total bytes
+int gram_run(double* d_cov, const double* Q, long long ldq, const double* w, int npts, int nm, void* d_scratch,
+             cudaStream_t st) {
+  const GramPlan p = gram_plan(npts, nm);
   uint8_t* base = (uint8_t*)(((uintptr_t)d_scratch + 1023) & ~(uintptr_t)1023);
-  double* Q = (double*)(base + p.off_q);
   unsigned long long* rowmax = (unsigned long long*)(base + p.off_max);
   int* expo = (int*)(base + p.off_exp);
   uint8_t* adig = base + p.off_a;
@@ -603,15 +604,14 @@ int aar_tetra_covariance(double* d_cov, const double* d_tetra_weights, const int
     }
   cudaError_t e = cudaMemcpyAsync(pairs, hp.data(), sizeof(int2) * hp.size(), cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(pid, hid.data(), sizeof(int) * hid.size(), cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess) e = cudaMemsetAsync(rowmax, 0, (size_t)2 * n_modes * sizeof(unsigned long long), st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(rowmax, 0, (size_t)2 * nm * sizeof(unsigned long long), st);
   if (e == cudaSuccess) e = cudaMemsetAsync(err, 0, sizeof(int), st);
   if (e != cudaSuccess) return tetra_status(e);
-  const int gx = (p.npts_pad + 255) / 256 < 64 ? (p.npts_pad + 255) / 256 : 64;
-  k_tetra_q<<<dim3(gx, n_modes), 256, 0, st>>>(a, p.npts_pad, Q, rowmax);
+  const int gx = (npts + 255) / 256 < 64 ? (npts + 255) / 256 : 64;
+  k_modes_rowmax<<<dim3(gx, nm), 256, 0, st>>>(Q, ldq, w, npts, nm, rowmax);
   const long long dthreads = (long long)p.ntA * p.nch * 256;
-  k_tetra_digits<<<(unsigned)((dthreads + 255) / 256), 256, 0, st>>>(
-      Q, d_tetra_weights, n_modes, tetra_npts, p.npts_pad, p.nch, p.rowsA, p.rowsB, rowmax, (uint4*)adig,
-      (uint4*)bdig, expo);
+  k_tetra_digits<<<(unsigned)((dthreads + 255) / 256), 256, 0, st>>>(Q, ldq, w, nm, npts, p.nch, p.rowsA, p.rowsB,
+                                                                     rowmax, (uint4*)adig, (uint4*)bdig, expo);
   if ((e = cudaGetLastError()) != cudaSuccess) return tetra_status(e);
   if ((e = cudaFuncSetAttribute(k_gram_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes)) != cudaSuccess)
     return tetra_status(e);
@@ -627,13 +627,68 @@ int aar_tetra_covariance(double* d_cov, const double* d_tetra_weights, const int
   g.err = err;
   k_gram_tc<<<dim3(p.npairs, p.nsplit), kThreads, kSmemBytes, st>>>(g);
   if ((e = cudaGetLastError()) != cudaSuccess) return tetra_status(e);
-  k_gram_tc_reduce<<<1024, 256, 0, st>>>(part, p.nsplit, p.npairs, pid, p.ntB, expo, p.rowsA, n_modes, d_cov);
+  k_gram_tc_reduce<<<1024, 256, 0, st>>>(part, p.nsplit, p.npairs, pid, p.ntB, expo, p.rowsA, nm, d_cov);
   if ((e = cudaGetLastError()) != cudaSuccess) return tetra_status(e);
   int herr = 0;
   e = cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return tetra_status(e);
   return herr ? AAR_ERR_CUDA : AAR_OK;
+}
+
+}  // namespace
+}  // namespace aar
+
+using namespace aar;
+
+extern "C" {
+
+int64_t aar_tetra_modes_ld(int32_t tetra_npts) { return tetra_npts > 0 ? modes_ld(tetra_npts) : 0; }
+
+int aar_tetra_modes(double* d_Q, int64_t ldq, const int32_t* d_i1, const int32_t* d_i2, const int32_t* d_i3,
+                    int32_t tetra_npts, const int32_t* d_p1, const int32_t* d_p2, const int32_t* d_p3,
+                    int32_t n_modes, const double* d_mode_evals, int32_t mode_p_max, int32_t k_npts, void* stream) {
+  if (!d_Q || !d_i1 || !d_i2 || !d_i3 || !d_p1 || !d_p2 || !d_p3 || !d_mode_evals || tetra_npts <= 0 ||
+      n_modes <= 0 || mode_p_max <= 0 || k_npts <= 0 || ldq < tetra_npts)
+    return AAR_ERR_ARG;
+  const Tetra a = make_tetra(nullptr, d_i1, d_i2, d_i3, tetra_npts, d_p1, d_p2, d_p3, n_modes, d_mode_evals,
+                             mode_p_max, k_npts);
+  return launch_modes(a, d_Q, ldq, (cudaStream_t)stream);
+}
+
+size_t aar_modes_covariance_scratch_bytes(int32_t tetra_npts, int32_t n_modes) {
+  if (tetra_npts <= 0 || n_modes <= 0) return 0;
+  return gram_plan(tetra_npts, n_modes).total;
+}
+
+int aar_modes_covariance(double* d_cov, const double* d_Q, int64_t ldq, const double* d_tetra_weights,
+                         int32_t tetra_npts, int32_t n_modes, void* d_scratch, size_t scratch_bytes, void* stream) {
+  if (!d_cov || !d_Q || !d_tetra_weights || !d_scratch || tetra_npts <= 0 || n_modes <= 0) return AAR_ERR_ARG;
+  if (ldq != modes_ld(tetra_npts) || ((uintptr_t)d_Q & 15)) return AAR_ERR_ARG;
+  if (scratch_bytes < aar_modes_covariance_scratch_bytes(tetra_npts, n_modes)) return AAR_ERR_ARG;
+  return gram_run(d_cov, d_Q, ldq, d_tetra_weights, tetra_npts, n_modes, d_scratch, (cudaStream_t)stream);
+}
+
+size_t aar_tetra_covariance_scratch_bytes(int32_t tetra_npts, int32_t n_modes) {
+  if (tetra_npts <= 0 || n_modes <= 0) return 0;
+  return q_bytes(tetra_npts, n_modes) + gram_plan(tetra_npts, n_modes).total + 1024;
+}
+
+int aar_tetra_covariance(double* d_cov, const double* d_tetra_weights, const int32_t* d_i1, const int32_t* d_i2,
+                         const int32_t* d_i3, int32_t tetra_npts, const int32_t* d_p1, const int32_t* d_p2,
+                         const int32_t* d_p3, int32_t n_modes, const double* d_mode_evals, int32_t mode_p_max,
+                         int32_t k_npts, void* d_scratch, size_t scratch_bytes, void* stream) {
+  const Tetra a = make_tetra(d_tetra_weights, d_i1, d_i2, d_i3, tetra_npts, d_p1, d_p2, d_p3, n_modes, d_mode_evals,
+                             mode_p_max, k_npts);
+  if (!d_cov || !d_scratch || !tetra_ok(a)) return AAR_ERR_ARG;
+  if (scratch_bytes < aar_tetra_covariance_scratch_bytes(tetra_npts, n_modes)) return AAR_ERR_ARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  double* Q = (double*)(((uintptr_t)d_scratch + 1023) & ~(uintptr_t)1023);
+  const long long ldq = modes_ld(tetra_npts);
+  const int rc = launch_modes(a, Q, ldq, st);
+  if (rc != AAR_OK) return rc;
+  return gram_run(d_cov, Q, ldq, d_tetra_weights, tetra_npts, n_modes, (uint8_t*)Q + q_bytes(tetra_npts, n_modes),
+                  st);
 }
 
 }  // extern "C"

@@ -62,6 +62,8 @@ DECOMP_WORKLOADS = {
     "decomp_logres_m20": ("LogResonance", 20, 2000.0, 1536, {"w_res": 10.0, "phi": 0.0}, "logres_w10_m20_L2000_n1536"),
     "decomp_local_m20": ("Local", 20, 1000.0, 1024, {}, None),
 }
+# the covariance build alone (aar_tetra_covariance): N_modes, Lbox, Nmax, k_grid_size of the basis
+COV_WORKLOADS = {"cov_m20_L2000_n1536": (20, 2000.0, 1536, 150), "cov_m12_L1000_n512_k96": (12, 1000.0, 512, 96)}
 
 
 def parse():
@@ -71,7 +73,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
     ap.add_argument("--workload", default="scalarI_m20_n1024",
-                    choices=sorted(WORKLOADS) + sorted(BATCH_WORKLOADS) + sorted(DECOMP_WORKLOADS))
+                    choices=sorted(WORKLOADS) + sorted(BATCH_WORKLOADS) + sorted(DECOMP_WORKLOADS) + sorted(COV_WORKLOADS))
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default schedule (no aar_autotune)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -210,9 +212,10 @@ def peaks() -> dict:
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
             d = json.load(f)
-        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+        return {"hbm_gbs": float(d["hbm_gbs"]), "bf16_tflops": float(d.get("bf16_tflops", 1900.0)),
+                "source": "measured"}
     except (OSError, KeyError, ValueError):
-        return {"hbm_gbs": 6800.0, "source": "fallback"}
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "source": "fallback"}
 
 
 def traffic_for(kernel: str, N: int):
@@ -914,15 +917,76 @@ def decomp_arm(args):
                    "modes": int(inst.basis.mode_indices.shape[1]), "tetrapyd_points": int(inst.basis.tetrapyd_grid_size),
                    "pursuit_steps": len(inst.basis.omp_log), "nonzero_alpha": int(np.count_nonzero(out["AlphaTable"][:, 3]))},
         "covariance_s": inst.basis.timings["covariance_s"],
+        "pursuit_s": {(k[8:-2] or "total"): round(v, 4) for k, v in inst.basis.timings.items() if k.startswith("pursuit_")},
         "reference_decomposer_s": ref,
         "reference_decomposer_host": "8-core x86 (the table's meta.json)" if ref else None}))
+
+
+def cov_arm(args):
+    """The mode-bispectrum covariance alone (aar_tetra_covariance: FP64 mode
+    values, bf16 digit tiles, the tcgen05 split-digit GEMM, the int64
+    reduce), seconds per build with CUDA events on the launching stream;
+    roofline against the measured bf16 tensor peak with the MMA flops the
+    GEMM issues (36 digit-pair products of 128 x 64 x 16 per 16 points and
+    tile pair)."""
+    import ctypes as C
+    import torch
+    from aarambam_gb300 import _lib
+    from aarambam_gb300.basis import Basis
+    L = _lib.load(build_if_missing=True)
+    M, lbox, nmax, kgrid = COV_WORKLOADS[args.workload]
+    torch.cuda.set_device(0)
+    kF = 2 * np.pi / lbox
+    b = Basis(k_min=kF, k_max=kF * nmax, parameter_n_scalar=0.965, mode_p_max=M, k_grid_size=kgrid, verbose=False)
+    nm, npts = b.mode_indices.shape[1], b.tetrapyd_grid_size
+    nbytes = L.aar_tetra_covariance_scratch_bytes(npts, nm)
+    scratch = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    qq = torch.empty((nm, nm), dtype=torch.float64, device="cuda")
+    st = torch.cuda.current_stream()
+
+    def one():
+        b._call("aar_tetra_covariance", C.c_void_p(qq.data_ptr()), *b._tetra_args(), C.c_void_p(scratch.data_ptr()),
+                C.c_size_t(nbytes), C.c_void_p(st.cuda_stream))
+    for _ in range(max(3, args.warmup)):
+        one()
+    clocks = Clocks(0)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(args.steps):
+        one()
+    e1.record(st)
+    torch.cuda.synchronize()
+    ck = clocks.stop()
+    per = e0.elapsed_time(e1) / 1e3 / args.steps
+    ta, tb = -(-nm // 128), -(-nm // 64)
+    pairs = sum(tb - 2 * i for i in range(ta))
+    nch = -(-npts // 128) * 8
+    mma_flops = pairs * nch * 36 * 2.0 * 128 * 64 * 16
+    pk = peaks()
+    diff = np.abs(qq.cpu().numpy() - b.mode_bispectra_covariance).max()
+    print(json.dumps({
+        "metric": "seconds per mode-bispectrum covariance (aar_tetra_covariance)", "value": per, "unit": "s",
+        "n_gpus": 1, "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": 1e3 * per,
+        "higher_is_better": False, "scaling": None, "vs_baseline": None, "dtype": "bf16 digits, FP32 level sums, "
+        "int64 fixed point (FP64-accurate)", "data": "synthetic",
+        "config": {"workload": f"{args.workload}: N_modes {M} ({nm} 3D modes), Lbox {lbox}, Nmax {nmax}, "
+                               f"k_grid_size {kgrid} ({npts} tetrapyd points)", "tile_pairs": pairs,
+                   "l2": "operand digits far larger than L2 (no flush)"},
+        "roofline": {"kernel": "whole covariance call (k_tetra_q, k_tetra_digits, k_gram_tc, reduce)",
+                     "bound": "tensor", "achieved": round(mma_flops / per / 1e12, 1), "peak": pk["bf16_tflops"],
+                     "unit": "TFLOP/s", "frac": round(mma_flops / per / 1e12 / pk["bf16_tflops"], 4),
+                     "traffic": None, "peak_source": pk["source"]},
+        "mma_flops_per_build": mma_flops, "fp64_equivalent_flops": float(nm) * (nm + 1) * npts,
+        "repeat_max_abs_diff": float(diff), "clocks": ck, "gpu_launches": 4 * args.steps,
+        "cpu_baseline": None, "e2e": None}))
 
 
 def reference_arm(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    if args.workload not in WORKLOADS:  # batches / decompositions: the IC path's reference arm
+    if args.workload not in WORKLOADS:  # batches / decompositions / covariance: the IC path's reference arm
         args.workload = "scalarI_m12_n256"
     cfg = make_cfg(args.workload, 1234)
     n = args.cpu_sample_n
@@ -964,6 +1028,8 @@ if __name__ == "__main__":
         batch_arm(a)
     elif a.workload in DECOMP_WORKLOADS:
         decomp_arm(a)
+    elif a.workload in COV_WORKLOADS:
+        cov_arm(a)
     elif a.slab or a.workload in SLAB_DEFAULT:
         slab_arm(a)
     else:

@@ -259,11 +259,15 @@ int aar_r2c(aar_plan* plan, const float* d_in, void* d_out, void* stream);
    Q_n(t) is the symmetrised product of tetrapyd.c:136-152.  Return AAR_OK,
    AAR_ERR_ARG or AAR_ERR_CUDA. */
 
-/* Scratch bytes aar_tetra_covariance needs (per-slice partial sums). */
+/* Scratch bytes aar_tetra_covariance needs (the mode bispectra, their bf16
+   digit tiles and the per-range int64 sums). */
 size_t aar_tetra_covariance_scratch_bytes(int32_t tetra_npts, int32_t n_modes);
 
-/* cov[n][m] = sum_t w_t Q_n(t) Q_m(t), [n_modes][n_modes], symmetric.
-   Replaces compute_mode_bispectra_covariance (tetrapyd.c:107-236). */
+/* cov[n][m] = sum_t w_t Q_n(t) Q_m(t), [n_modes][n_modes], symmetric,
+   FP64-accurate on the bf16 tensor cores (the operands cut into eight 8-bit
+   digits, exact level sums, int64 fixed-point accumulation; deterministic).
+   Synchronises the stream.  Replaces compute_mode_bispectra_covariance
+   (tetrapyd.c:107-236). */
 int aar_tetra_covariance(double* d_cov, const double* d_tetra_weights, const int32_t* d_i1, const int32_t* d_i2,
                          const int32_t* d_i3, int32_t tetra_npts, const int32_t* d_p1, const int32_t* d_p2,
                          const int32_t* d_p3, int32_t n_modes, const double* d_mode_evals, int32_t mode_p_max,
@@ -283,6 +287,29 @@ int aar_tetra_residual(double* d_R, const double* d_S, const int32_t* d_sel, con
                        int32_t tetra_npts, const int32_t* d_p1, const int32_t* d_p2, const int32_t* d_p3,
                        int32_t n_modes, const double* d_mode_evals, int32_t mode_p_max, int32_t k_npts,
                        void* stream);
+
+/* Stored mode bispectra: Q[n][t] = Q_n(t) made once per basis and kept by
+   the caller ([n_modes][ldq] doubles, ldq = aar_tetra_modes_ld(tetra_npts),
+   the point count rounded up to a multiple of 128; zeros beyond tetra_npts,
+   16-byte aligned), read by the aar_modes_* entry points instead of
+   evaluating Q_n(t) again (the matching pursuit projects on every mode at
+   every step). */
+int64_t aar_tetra_modes_ld(int32_t tetra_npts);
+int aar_tetra_modes(double* d_Q, int64_t ldq, const int32_t* d_i1, const int32_t* d_i2, const int32_t* d_i3,
+                    int32_t tetra_npts, const int32_t* d_p1, const int32_t* d_p2, const int32_t* d_p3,
+                    int32_t n_modes, const double* d_mode_evals, int32_t mode_p_max, int32_t k_npts, void* stream);
+
+/* aar_tetra_covariance from stored mode bispectra (ldq as above). */
+size_t aar_modes_covariance_scratch_bytes(int32_t tetra_npts, int32_t n_modes);
+int aar_modes_covariance(double* d_cov, const double* d_Q, int64_t ldq, const double* d_tetra_weights,
+                         int32_t tetra_npts, int32_t n_modes, void* d_scratch, size_t scratch_bytes, void* stream);
+
+/* aar_tetra_QS and aar_tetra_residual from stored mode bispectra: the same
+   terms, order and reductions, so the same results. */
+int aar_modes_project(double* d_out, const double* d_X, int32_t n_shapes, const double* d_tetra_weights,
+                      const double* d_Q, int64_t ldq, int32_t tetra_npts, int32_t n_modes, void* stream);
+int aar_modes_residual(double* d_R, const double* d_S, const int32_t* d_sel, const double* d_coef, int32_t n_sel,
+                       const double* d_Q, int64_t ldq, int32_t tetra_npts, void* stream);
 
 /* Condition numbers lambda_max / lambda_min of the bordered symmetric
    matrices [[A, b_i], [b_i^T, c_i]], i < n_cand, given the eigenvalues lam

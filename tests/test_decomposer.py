@@ -95,13 +95,47 @@ def test_covariance_and_projection_vs_oracle(cuda):
 
 @pytest.mark.gpu
 def test_covariance_tiles_and_slices(cuda):
-    # several 64-mode tiles (M = 12: 364 modes) and several 65536-point slices
+    # several 128 x 64 tiles (M = 12: 364 modes) over several point ranges
     kF = 2 * np.pi / 1000.0
     b = B.Basis(k_min=kF, k_max=kF * 512, parameter_n_scalar=0.965, mode_p_max=12, k_grid_size=96, verbose=False)
     args = (b.tetrapyd_grid_weights, b.tetrapyd_indices, b.mode_indices, b.mode_function_evaluations)
     assert b.tetrapyd_grid_size > 65536
     want = D.covariance(*args)
     assert np.abs(b.mode_bispectra_covariance - want).max() <= 1e-12 * np.abs(want).max()
+
+
+@pytest.mark.gpu
+def test_stored_modes_match_stateless_entry_points(cuda):
+    """The stored-mode entry points the Basis uses (aar_modes_*, reading
+    Q[n][t] made once by aar_tetra_modes) against the stateless ones
+    (aar_tetra_*, evaluating Q_n(t) on the fly): the same terms in the same
+    order, so the covariance, projections and residual agree bit for bit."""
+    import ctypes as C
+
+    import torch
+    from aarambam_gb300 import _lib
+    kF = 2 * np.pi / 1000.0
+    b = B.Basis(k_min=kF, k_max=kF * 512, parameter_n_scalar=0.965, mode_p_max=12, k_grid_size=96, verbose=False)
+    L = _lib.load()
+    nm, npts = b.mode_indices.shape[1], b.tetrapyd_grid_size
+    nbytes = L.aar_tetra_covariance_scratch_bytes(npts, nm)
+    scratch = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    qq = torch.empty((nm, nm), dtype=torch.float64, device="cuda")
+    b._call("aar_tetra_covariance", B._ptr(qq), *b._tetra_args(), B._ptr(scratch), C.c_size_t(nbytes), b._stream())
+    assert np.array_equal(qq.cpu().numpy(), b.mode_bispectra_covariance)
+    rng = np.random.default_rng(5)
+    X = torch.from_numpy(rng.standard_normal((2, npts))).cuda()
+    out = torch.empty((2, nm), dtype=torch.float64, device="cuda")
+    b._call("aar_tetra_QS", B._ptr(out), B._ptr(X), 2, *b._tetra_args(), b._stream())
+    assert np.array_equal(out.cpu().numpy(), b._project_dev(X).cpu().numpy())
+    sel, coef = np.array([0, 7, 100, nm - 1]), rng.standard_normal(4)
+    S = X[:1].contiguous()
+    R = torch.empty_like(S)
+    sel_d = torch.from_numpy(sel.astype(np.int32)).cuda()
+    coef_d = torch.from_numpy(coef).cuda()
+    b._call("aar_tetra_residual", B._ptr(R), B._ptr(S), B._ptr(sel_d), B._ptr(coef_d), 4, *b._tetra_args(),
+            b._stream())
+    assert np.array_equal(R.cpu().numpy(), b._residual_dev(S, sel, coef).cpu().numpy())
 
 
 @pytest.mark.gpu

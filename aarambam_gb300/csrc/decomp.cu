@@ -71,30 +71,45 @@ __global__ void k_tetra_residual(Tetra a, const double* __restrict__ S, const in
 
 // The same two sums from stored mode bispectra Q[n][t] (row stride ldq):
 // the terms, their order and the warp reduction of k_tetra_project and
-// k_tetra_residual, with Q read instead of evaluated.  Each lane issues the
-// loads of eight of its points before their multiply-adds.
-__global__ void k_modes_project(const double* __restrict__ Q, long long ldq, const double* __restrict__ w, int npts,
-                                int nmodes, const double* __restrict__ X, int nshapes, double* __restrict__ out) {
-  const int lane = threadIdx.x & 31;
-  const int64_t wid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (wid >= (int64_t)nmodes * nshapes) return;
-  const int n = (int)(wid % nmodes), s = (int)(wid / nmodes);
-  const double* q = Q + (size_t)n * ldq;
+// k_tetra_residual, with Q read instead of evaluated.  Projection: a block of
+// eight warps takes eight modes of one shape; per tile of 512 points the
+// products x_t w_t are formed once into shared memory and every lane issues
+// its 16 loads of Q before their multiply-adds (lane l adds the points
+// l, l + 32, ... in ascending order, as k_tetra_project).
+constexpr int kProjWarps = 8;
+constexpr int kProjTile = 512;
+
+__global__ void __launch_bounds__(kProjWarps * 32) k_modes_project(const double* __restrict__ Q, long long ldq,
+                                                                   const double* __restrict__ w, int npts, int nmodes,
+                                                                   const double* __restrict__ X,
+                                                                   double* __restrict__ out) {
+  __shared__ double xw[2][kProjTile];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int n = blockIdx.x * kProjWarps + warp, s = blockIdx.y;
+  const bool row = n < nmodes;
+  const double* q = Q + (size_t)(row ? n : 0) * ldq;
   const double* x = X + (int64_t)s * npts;
   double acc = 0.0;
-  int t = lane;
-  for (; t + 7 * 32 < npts; t += 8 * 32) {
-    double xv[8], wv[8], qv[8];
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      xv[j] = x[t + 32 * j];
-      wv[j] = w[t + 32 * j];
-      qv[j] = q[t + 32 * j];
+  int buf = 0;
+  for (int t0 = 0; t0 < npts; t0 += kProjTile, buf ^= 1) {
+    for (int i = threadIdx.x; i < kProjTile; i += kProjWarps * 32) {
+      const int t = t0 + i;
+      xw[buf][i] = t < npts ? x[t] * w[t] : 0.0;
     }
+    __syncthreads();  // xw[buf] complete; xw[buf ^ 1] is rewritten only after the next barrier
+    if (row) {
+      if (t0 + kProjTile <= npts) {
+        double qv[kProjTile / 32];
 #pragma unroll
-    for (int j = 0; j < 8; ++j) acc = fma(xv[j] * wv[j], qv[j], acc);
+        for (int j = 0; j < kProjTile / 32; ++j) qv[j] = q[t0 + lane + 32 * j];
+#pragma unroll
+        for (int j = 0; j < kProjTile / 32; ++j) acc = fma(xw[buf][lane + 32 * j], qv[j], acc);
+      } else {
+        for (int j = 0; t0 + lane + 32 * j < npts; ++j) acc = fma(xw[buf][lane + 32 * j], q[t0 + lane + 32 * j], acc);
+      }
+    }
   }
-  for (; t < npts; t += 32) acc = fma(x[t] * w[t], q[t], acc);
+  if (!row) return;
 #pragma unroll
   for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
   if (lane == 0) out[(int64_t)s * nmodes + n] = acc;
@@ -217,9 +232,8 @@ int aar_modes_project(double* d_out, const double* d_X, int32_t n_shapes, const 
   if (!d_out || !d_X || !d_tetra_weights || !d_Q || n_shapes < 1 || tetra_npts < 1 || n_modes < 1 ||
       ldq < tetra_npts)
     return AAR_ERR_ARG;
-  const int64_t warps = (int64_t)n_modes * n_shapes;
-  k_modes_project<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, (cudaStream_t)stream>>>(
-      d_Q, ldq, d_tetra_weights, tetra_npts, n_modes, d_X, n_shapes, d_out);
+  k_modes_project<<<dim3((n_modes + kProjWarps - 1) / kProjWarps, n_shapes), kProjWarps * 32, 0,
+                    (cudaStream_t)stream>>>(d_Q, ldq, d_tetra_weights, tetra_npts, n_modes, d_X, d_out);
   return tetra_status(cudaGetLastError());
 }
 

@@ -973,12 +973,13 @@ def cov_arm(args):
         "config": {"workload": f"{args.workload}: N_modes {M} ({nm} 3D modes), Lbox {lbox}, Nmax {nmax}, "
                                f"k_grid_size {kgrid} ({npts} tetrapyd points)", "tile_pairs": pairs,
                    "l2": "operand digits far larger than L2 (no flush)"},
-        "roofline": {"kernel": "whole covariance call (k_tetra_q, k_tetra_digits, k_gram_tc, reduce)",
+        "roofline": {"kernel": "whole covariance call (k_tetra_modes, k_modes_rowmax, k_tetra_digits, k_gram_tc, "
+                               "k_gram_tc_reduce)",
                      "bound": "tensor", "achieved": round(mma_flops / per / 1e12, 1), "peak": pk["bf16_tflops"],
                      "unit": "TFLOP/s", "frac": round(mma_flops / per / 1e12 / pk["bf16_tflops"], 4),
                      "traffic": None, "peak_source": pk["source"]},
         "mma_flops_per_build": mma_flops, "fp64_equivalent_flops": float(nm) * (nm + 1) * npts,
-        "repeat_max_abs_diff": float(diff), "clocks": ck, "gpu_launches": 4 * args.steps,
+        "repeat_max_abs_diff": float(diff), "clocks": ck, "gpu_launches": 5 * args.steps,
         "cpu_baseline": None, "e2e": None}))
 
 

@@ -127,3 +127,49 @@ def test_split_digit_covariance_several_tiles():
     want = D.covariance(*args)
     assert got.shape == (165, 165) and np.array_equal(got, got.T)
     assert np.abs(got - want).max() <= 1e-14 * np.abs(want).max()
+
+
+# ---- host side of csrc/gram_tc.cu and the stored-mode entry points (no device work) ----
+def _lib_handle():
+    from aarambam_gb300 import _lib
+    return _lib, _lib.load(build_if_missing=True)
+
+
+def test_stored_mode_stride_and_scratch_sizes():
+    """Q rows padded to whole 128-point groups; the covariance scratch holds at
+    least the bf16 digit tiles (8 digits of 128-row A tiles and 64-row B
+    tiles per 16-point chunk) and the stateless form adds the Q it makes."""
+    _, L = _lib_handle()
+    for npts, ld in [(1, 128), (128, 128), (129, 256), (289750, 289792)]:
+        assert L.aar_tetra_modes_ld(npts) == ld
+    assert L.aar_tetra_modes_ld(0) == 0
+    nm, npts = 1540, 289750
+    nch = 289792 // 16
+    digits = (13 * nch * 8 * 4096) + (25 * nch * 8 * 2048)
+    modes = L.aar_modes_covariance_scratch_bytes(npts, nm)
+    assert digits < modes < digits * 1.05
+    assert L.aar_tetra_covariance_scratch_bytes(npts, nm) >= modes + nm * 289792 * 8
+    assert L.aar_modes_covariance_scratch_bytes(0, nm) == 0 and L.aar_modes_covariance_scratch_bytes(npts, 0) == 0
+
+
+def test_stored_mode_argument_errors():
+    """Argument checks that return before any device work: a Q stride other
+    than aar_tetra_modes_ld, a Q base that is not 16-byte aligned, too little
+    scratch, null pointers."""
+    import ctypes as C
+    _lib, L = _lib_handle()
+    p = C.c_void_p(4096)  # never dereferenced: every call below fails its checks first
+    npts, nm = 1000, 56
+    ld = L.aar_tetra_modes_ld(npts)
+    need = L.aar_modes_covariance_scratch_bytes(npts, nm)
+    bad = [
+        L.aar_modes_covariance(p, p, ld + 128, p, npts, nm, p, C.c_size_t(need), None),
+        L.aar_modes_covariance(p, C.c_void_p(4104), ld, p, npts, nm, p, C.c_size_t(need), None),
+        L.aar_modes_covariance(p, p, ld, p, npts, nm, p, C.c_size_t(need - 1), None),
+        L.aar_modes_covariance(None, p, ld, p, npts, nm, p, C.c_size_t(need), None),
+        L.aar_modes_project(p, p, 1, p, None, ld, npts, nm, None),
+        L.aar_modes_project(p, p, 1, p, p, npts - 1, npts, nm, None),
+        L.aar_modes_residual(p, p, None, None, 3, p, ld, npts, None),
+        L.aar_tetra_modes(p, npts - 1, p, p, p, npts, p, p, p, nm, p, 6, 24, None),
+    ]
+    assert all(rc == _lib.AAR_ERR_ARG for rc in bad), bad

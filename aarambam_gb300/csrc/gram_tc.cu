@@ -30,10 +30,12 @@
 //               points is exact integer arithmetic, so it does not depend on
 //               the order, and the result is deterministic.
 //
-// Accuracy (the 20-mode basis on the 1536^3 case's 150-point grid, 300 modes,
-// against a 96-bit evaluation): largest error 1.8e-16 of max |QQ|, 5.4e-15 of
-// sqrt(QQ_nn QQ_mm); an FP64 GEMM of the same operands gives 1.2e-15 and
-// 4.4e-15.
+// Accuracy of the digit cut (the 20-mode basis on the 1536^3 case's 150-point
+// grid, 300 modes, every level summed exactly, against a 96-bit evaluation):
+// largest error 1.8e-16 of max |QQ|, 5.4e-15 of sqrt(QQ_nn QQ_mm); an FP64
+// GEMM of the same operands gives 1.2e-15 and 4.4e-15.  The shared level-6/7
+// accumulator adds one FP32 rounding per 128-point group at 2^-48 of the
+// level-0 scale.
 //
 // Kernels:
 //   k_tetra_modes   Q[n][t] in FP64 (kept by the caller for the stored-mode

@@ -71,28 +71,28 @@ __global__ void k_tetra_residual(Tetra a, const double* __restrict__ S, const in
 
 // The same two sums from stored mode bispectra Q[n][t] (row stride ldq):
 // the terms, their order and the warp reduction of k_tetra_project and
-// k_tetra_residual, with Q read instead of evaluated.  Projection: a block of
-// eight warps takes eight modes of one shape; per tile of 512 points the
-// products x_t w_t are formed once into shared memory and every lane issues
-// its 16 loads of Q before their multiply-adds (lane l adds the points
-// l, l + 32, ... in ascending order, as k_tetra_project).
-constexpr int kProjWarps = 8;
+// k_tetra_residual, with Q read instead of evaluated.  Projection: one warp
+// per mode, a block of ceil(modes / SMs) warps (one wave of blocks, the rows
+// spread evenly: the sum is FP64-bound on GB300, about 2 FP64 multiply-adds
+// per clock per SM); per tile of 512 points the products x_t w_t are formed
+// once into shared memory for the block's rows and every lane issues its 16
+// loads of Q before their multiply-adds (lane l adds the points l, l + 32,
+// ... in ascending order, as k_tetra_project).
 constexpr int kProjTile = 512;
 
-__global__ void __launch_bounds__(kProjWarps * 32) k_modes_project(const double* __restrict__ Q, long long ldq,
-                                                                   const double* __restrict__ w, int npts, int nmodes,
-                                                                   const double* __restrict__ X,
-                                                                   double* __restrict__ out) {
+__global__ void __launch_bounds__(1024) k_modes_project(const double* __restrict__ Q, long long ldq,
+                                                        const double* __restrict__ w, int npts, int nmodes,
+                                                        const double* __restrict__ X, double* __restrict__ out) {
   __shared__ double xw[2][kProjTile];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int n = blockIdx.x * kProjWarps + warp, s = blockIdx.y;
+  const int n = blockIdx.x * (int)(blockDim.x >> 5) + warp, s = blockIdx.y;
   const bool row = n < nmodes;
   const double* q = Q + (size_t)(row ? n : 0) * ldq;
   const double* x = X + (int64_t)s * npts;
   double acc = 0.0;
   int buf = 0;
   for (int t0 = 0; t0 < npts; t0 += kProjTile, buf ^= 1) {
-    for (int i = threadIdx.x; i < kProjTile; i += kProjWarps * 32) {
+    for (int i = threadIdx.x; i < kProjTile; i += blockDim.x) {
       const int t = t0 + i;
       xw[buf][i] = t < npts ? x[t] * w[t] : 0.0;
     }
@@ -232,8 +232,17 @@ int aar_modes_project(double* d_out, const double* d_X, int32_t n_shapes, const 
   if (!d_out || !d_X || !d_tetra_weights || !d_Q || n_shapes < 1 || tetra_npts < 1 || n_modes < 1 ||
       ldq < tetra_npts)
     return AAR_ERR_ARG;
-  k_modes_project<<<dim3((n_modes + kProjWarps - 1) / kProjWarps, n_shapes), kProjWarps * 32, 0,
-                    (cudaStream_t)stream>>>(d_Q, ldq, d_tetra_weights, tetra_npts, n_modes, d_X, d_out);
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+                                                  cudaSuccess || sms < 1)
+      sms = 1;
+  }
+  int wpb = (n_modes + sms - 1) / sms;  // warps (modes) per block
+  wpb = wpb < 1 ? 1 : (wpb > 32 ? 32 : wpb);
+  k_modes_project<<<dim3((n_modes + wpb - 1) / wpb, n_shapes), wpb * 32, 0, (cudaStream_t)stream>>>(
+      d_Q, ldq, d_tetra_weights, tetra_npts, n_modes, d_X, d_out);
   return tetra_status(cudaGetLastError());
 }
 

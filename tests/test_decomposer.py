@@ -105,6 +105,26 @@ def test_covariance_tiles_and_slices(cuda):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("M,kgrid", [(1, 24), (2, 24), (30, 40)])
+def test_covariance_edge_shapes_vs_oracle(cuda, M, kgrid):
+    """The tensor-core covariance at the edges of its tiling: 1 and 4 modes
+    (one 128 x 64 tile, nearly every row padding) and 30 modes (4960 3D
+    modes: 39 x 78 tiles, 1560 tile pairs), against the oracle; and the
+    projection at 4960 modes (its 32-warp block cap) against it too."""
+    kF = 2 * np.pi / 1000.0
+    b = B.Basis(k_min=kF, k_max=kF * 256, parameter_n_scalar=0.965, mode_p_max=M, k_grid_size=kgrid, verbose=False)
+    args = (b.tetrapyd_grid_weights, b.tetrapyd_indices, b.mode_indices, b.mode_function_evaluations)
+    want = D.covariance(*args)
+    got = b.mode_bispectra_covariance
+    assert got.shape == want.shape == (M * (M + 1) * (M + 2) // 6,) * 2
+    assert np.array_equal(got, got.T)
+    assert np.abs(got - want).max() <= 1e-13 * np.abs(want).max()
+    S = np.random.default_rng(M).standard_normal((1, b.tetrapyd_grid_size))
+    qs, want_qs = b.compute_QS_C(S), D.project(S, *args)
+    assert np.abs(qs - want_qs).max() <= 1e-13 * np.abs(want_qs).max()
+
+
+@pytest.mark.gpu
 def test_stored_modes_match_stateless_entry_points(cuda):
     """The stored-mode entry points the Basis uses (aar_modes_*, reading
     Q[n][t] made once by aar_tetra_modes) against the stateless ones
